@@ -1,0 +1,213 @@
+/*
+ * lsim.h -- C ABI of the GB300 (sm_103a) larnd-sim simulate path.
+ *
+ * Every entry point takes caller-allocated DEVICE pointers, sizes, a POD
+ * parameter block and a CUDA stream (passed as void*), returns an LSIM_*
+ * status and never throws.  Device memory is owned by the caller: the
+ * library allocates nothing; sizes of the workspace and of the prepared LUT
+ * tables are queried with the *_bytes functions.  On error,
+ * lsim_last_error() returns a thread-local message.
+ *
+ * The reference (larnd-sim-jax) is Python/JAX with no FFI of its own; each
+ * function below names the reference function(s) it replaces.  File paths
+ * are relative to the reference project root.
+ */
+#ifndef LSIM_H
+#define LSIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LSIM_ABI_VERSION 1
+
+enum {
+  LSIM_OK = 0,
+  LSIM_ERR_INVALID = 1,     /* bad argument or bad input value (e.g. eventID < -1) */
+  LSIM_ERR_CAPACITY = 2,    /* a buffer or workspace is too small */
+  LSIM_ERR_CUDA = 3,        /* a CUDA runtime error */
+  LSIM_ERR_UNSUPPORTED = 4  /* configuration outside what the kernels support */
+};
+
+enum { LSIM_RECOMB_BOX = 1, LSIM_RECOMB_BIRKS = 2, LSIM_RECOMB_ELLIPSOID = 3 };
+
+#define LSIM_MAX_TPC 2
+#define LSIM_MAX_TEMPLATES 128
+#define LSIM_MAX_HITS 16
+#define LSIM_NPARAM 8   /* gradient order: Ab kb eField lifetime vdrift long_diff tran_diff lArDensity */
+
+/* Column indices of the (N, F) float32 track array (the reference's
+ * `fields` tuple resolved to integers, optimize/dataio.py:130-141). */
+typedef struct LsimFieldMap {
+  int32_t n_fields;
+  int32_t eventID, x, y, z, x_start, y_start, z_start, x_end, y_end, z_end;
+  int32_t dx, dE, dEdx;
+} LsimFieldMap;
+
+/* Parameter block.  Scalars hold the float32 values the reference computes
+ * in float64 from its static parameters and rounds once (e.g. erho is
+ * float32(eField * lArDensity), vdrift is float32(get_vdrift(params))). */
+typedef struct LsimParams {
+  /* quenching, src/larndsim/quenching_jax.py:18-74 */
+  int32_t recombination_mode;
+  float Ab, kb, alpha, beta, r_inv2, erho, mev_to_electrons;
+  /* drift, src/larndsim/drifting_jax.py:18-58 */
+  float vdrift, lifetime, long_diff, tran_diff, size_margin;
+  float shift_x, shift_y, shift_z;
+  int32_t n_tpc;
+  float tpc_borders[LSIM_MAX_TPC * 3 * 2];
+  /* pixels and sub-pixel bins, src/larndsim/sim_jax.py:374-453 */
+  float pixel_pitch, half_pitch, bin_width;
+  int32_t n_pixels_x, n_pixels_y, nb_bins_per_pixel, n_tran_bins, n_neighbors;
+  float tran_edges[8];
+  /* time axis and LUT, src/larndsim/sim_jax.py:141-286 */
+  float t_sampling;
+  int32_t n_ticks;           /* time_interval[1]/t_sampling + 1 (2001), incl. garbage tick 0 */
+  int32_t signal_length;     /* L */
+  int32_t lut_nx, lut_ny, lut_nt, n_templates;
+  float long_diff_template[LSIM_MAX_TEMPLATES];
+  /* front end, src/larndsim/fee_jax.py:55-71 and :168-279 */
+  float threshold, gain, v_pedestal, v_cm, vref_minus_cm, adc_counts;
+  float reset_noise, uncorr_noise, hit_prob_threshold;
+  int32_t max_adc_values, fee_interval;
+  /* parametrised current, src/larndsim/detsim_jax.py:618-639 */
+  int32_t diffusion_in_current_sim, param_nticks;
+  float param_dt;
+  float param_ticks[64];
+  /* adjoint: raw parameter values and d(vdrift)/d(eField) */
+  float eField, lArDensity, dvdrift_deField;
+  int32_t reserved[8];
+} LsimParams;
+
+/* Device counters filled by the stage-1 calls (read after a sync). */
+typedef struct LsimCounts {
+  int32_t n_valid;      /* distinct pixel ids >= 0 with a main-pixel segment */
+  int32_t n_em1;        /* distinct negative pixel ids < -1 (eventID -1 rows) */
+  int32_t any_m1;       /* 1 if some main pixel id equals -1 */
+  int32_t status;       /* device-detected LSIM_* error, 0 if none */
+  int32_t max_slot;     /* largest number of segments sharing one pixel */
+  int32_t bad_row;      /* first offending track row, or -1 */
+  int32_t work;         /* internal work counter */
+  int32_t reserved[9];
+} LsimCounts;
+
+int lsim_abi_version(void);
+const char *lsim_last_error(void);
+
+/* sizeof(LsimParams), sizeof(LsimFieldMap), sizeof(LsimCounts), so a
+ * binding can check its structure layout against the library. */
+void lsim_struct_sizes(size_t *params, size_t *fields, size_t *counts);
+
+/* ---------------------------------------------------------------- LUT */
+
+/* Build the long-diffusion template bank from a raw response LUT:
+ * out[k] = response convolved along time with the normalised Gaussian of
+ * width sigmas[k] (taps -extent..extent, 'same' mode), out[0] = response.
+ * Replaces load_lut, src/larndsim/consts_jax.py:387-449. */
+int lsim_lut_build_templates(const float *response, int32_t nx, int32_t ny, int32_t nt,
+                             const float *sigmas_dev, int32_t n_templates, int32_t extent,
+                             float *templates_out, void *stream);
+
+/* Bytes of the prepared tables derived from a template bank. */
+size_t lsim_lut_tables_bytes(const LsimParams *p);
+
+/* Derive the per-call LUT tables once per template bank: the L-tick
+ * windows and the cumulative sums along time that the reference recomputes
+ * on every call (src/larndsim/sim_jax.py:184-190, :221-222, :228). */
+int lsim_lut_prepare(const LsimParams *p, const float *templates, void *tables, size_t tables_bytes,
+                     void *stream);
+
+/* ---------------------------------------------------------------- workspace */
+
+/* Workspace bytes for n_rows track rows with event ids in [-1, n_events). */
+size_t lsim_workspace_bytes(const LsimParams *p, int64_t n_rows, int32_t n_events);
+
+/* ---------------------------------------------------------------- LUT mode */
+
+/* Stage 1 of simulate_wfs: shift, quench, drift, sub-pixel binning and
+ * 5x5 transverse weights per segment, then the pixel map (unique main
+ * pixels, segments grouped by pixel).  Replaces simulate_drift_new
+ * (src/larndsim/sim_jax.py:374-453) and the unique/renumbering step
+ * (src/larndsim/sim_jax.py:715-725).  Writes an LsimCounts to counts_dev. */
+int lsim_lut_stage1(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,
+                    int32_t n_events, void *ws, size_t ws_bytes, LsimCounts *counts_dev, void *stream);
+
+/* Stage 2 of simulate_wfs: fill unique_pixels (p_pad rows: n_em1 negative
+ * ids, n_m1 = p_pad - n_em1 - n_valid entries of -1, then the valid ids
+ * ascending) and the waveforms wfs[p_pad][n_ticks-1] (garbage tick 0
+ * dropped, as sim_jax.py:736 returns).  Rows with id < 0 are zero.
+ * Replaces simulate_signals, src/larndsim/sim_jax.py:141-286. */
+int lsim_lut_stage2(const LsimParams *p, const void *tables, const void *ws, int64_t n_rows,
+                    int32_t n_events, int64_t p_pad, int32_t n_em1, int32_t n_valid, float *wfs,
+                    int32_t *unique_pixels, void *stream);
+
+/* Pixel ids of the n_valid valid rows (ascending), as stage 2 orders them. */
+int lsim_valid_pixels(const LsimParams *p, const void *ws, int64_t n_rows, int32_t n_events, int32_t n_valid,
+                      int32_t *pids_out, void *stream);
+
+/* Fused per-pixel forward: waveform accumulation + self-trigger FEE +
+ * digitisation for the n_valid valid rows, without materialising the
+ * waveforms.  adc_out/tick_out are [n_valid][max_adc_values]. */
+int lsim_lut_adc(const LsimParams *p, const void *tables, const void *ws, int64_t n_rows,
+                 int32_t n_events, int32_t n_valid, const float *normals, float *adc_out,
+                 float *tick_out, void *stream);
+
+/* Adjoint of lsim_lut_adc: given dL/dADC (g_adc, [n_valid][H]), or an SSE
+ * target (tgt_pids ascending + tgt_adc [n_tgt][H]) when g_adc is NULL,
+ * recompute each pixel's waveform and FEE state, and accumulate dL/dtheta
+ * for the LSIM_NPARAM parameters into grad_out[LSIM_NPARAM] (and the loss
+ * into loss_out[0] when a target is given).  Gradient semantics follow
+ * jax.value_and_grad through src/larndsim/sim_jax.py:141-286,
+ * src/larndsim/fee_jax.py:55-71, :168-279 (fit_params.py:731). */
+int lsim_lut_grad(const LsimParams *p, const void *tables, const void *ws, int64_t n_rows,
+                  int32_t n_events, int32_t n_valid, const float *normals, const float *g_adc,
+                  const int32_t *tgt_pids, const float *tgt_adc, int64_t n_tgt, float *loss_out,
+                  float *grad_out, float *adc_out, void *stream);
+
+/* ---------------------------------------------------------------- FEE + hits */
+
+/* Self-trigger FEE + digitize on waveforms wfs[n_pix][n_t]: ADC values and
+ * crossing ticks per hit ([n_pix][max_adc_values]).  normals (optional,
+ * [n_pix][1 + 3*max_adc_values]) are standard-normal noise draws.
+ * Replaces get_adc_values + digitize, src/larndsim/fee_jax.py:55-71, :168-279. */
+int lsim_fee(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, const float *normals,
+             float *adc_out, float *tick_out, float *integral_out, void *stream);
+
+/* Workspace bytes of lsim_hits for n_pix pixel rows. */
+size_t lsim_hits_workspace_bytes(int64_t n_pix, int32_t max_adc_values);
+
+/* Hit assembly and compaction: hit probability (tick < tick_limit), pixel
+ * centres, hit z, event ids and the row-major compaction of accepted hits.
+ * Replaces simulate_stochastic's tail and parse_output,
+ * src/larndsim/sim_jax.py:757-769, :619-647.  Output arrays hold up to
+ * n_pix*max_adc_values entries; the count goes to nb_valid_dev. */
+int lsim_hits(const LsimParams *p, const float *adc, const float *ticks, const int32_t *unique_pixels,
+              int64_t n_pix, int32_t tick_limit, float *out_adc, float *out_x, float *out_y,
+              float *out_z, float *out_ticks, float *out_hit_prob, int32_t *out_event,
+              int32_t *out_pixels, int32_t *nb_valid_dev, void *ws, size_t ws_bytes, void *stream);
+
+/* ---------------------------------------------------------------- parametrised mode */
+
+/* Stage 1 of simulate_parametrized: shift, quench, drift, Monte-Carlo
+ * diffusion offsets (normals [n_rows][3], supplied), pixel of each
+ * electron, pixel map.  Replaces simulate_drift + generate_electrons +
+ * get_pixels, src/larndsim/sim_jax.py:122-139, src/larndsim/detsim_jax.py:376-400, :477-491. */
+int lsim_param_stage1(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,
+                      int32_t n_events, const float *normals, void *ws, size_t ws_bytes,
+                      LsimCounts *counts_dev, void *stream);
+
+/* Stage 2 of simulate_parametrized: unique pixels and waveforms from the
+ * parametrised (EMG-smoothed) induced current.  Replaces
+ * simulate_signals_parametrized + current_mc + accumulate_signals_parametrized,
+ * src/larndsim/sim_jax.py:289-335, src/larndsim/detsim_jax.py:207-228, :581-639. */
+int lsim_param_stage2(const LsimParams *p, const void *ws, int64_t n_rows, int32_t n_events,
+                      int64_t p_pad, int32_t n_em1, int32_t n_valid, float *wfs, int32_t *unique_pixels,
+                      void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LSIM_H */

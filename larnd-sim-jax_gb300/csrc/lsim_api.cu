@@ -1,0 +1,272 @@
+// extern "C" entry points of liblsim (declared in include/lsim.h).  Each
+// validates its arguments, launches on the caller's stream, converts CUDA
+// errors into LSIM_* codes with a thread-local message, and never throws.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "lsim_internal.cuh"
+
+namespace lsim {
+
+static thread_local std::string g_err;
+
+static int fail(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
+static int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+static int check_cuda(const char *where) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(LSIM_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+  return LSIM_OK;
+}
+
+static int wrap(int rc, const char *where) {
+  if (rc == LSIM_OK) return check_cuda(where);
+  if (rc == LSIM_ERR_CUDA) {
+    cudaError_t e = cudaGetLastError();
+    return fail(rc, "%s: CUDA error %s", where, cudaGetErrorString(e));
+  }
+  if (g_err.empty()) fail(rc, "%s: error %d", where, rc);
+  return rc;
+}
+
+int device_sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+static int check_params(const LsimParams *p) {
+  if (!p) return fail(LSIM_ERR_INVALID, "null parameter block");
+  if (p->n_tpc < 1 || p->n_tpc > LSIM_MAX_TPC) return fail(LSIM_ERR_UNSUPPORTED, "n_tpc %d not in [1, %d]", p->n_tpc, LSIM_MAX_TPC);
+  if (p->n_templates > LSIM_MAX_TEMPLATES) return fail(LSIM_ERR_UNSUPPORTED, "%d templates > %d", p->n_templates, LSIM_MAX_TEMPLATES);
+  if (p->max_adc_values < 1 || p->max_adc_values > LSIM_MAX_HITS)
+    return fail(LSIM_ERR_UNSUPPORTED, "MAX_ADC_VALUES %d not in [1, %d]", p->max_adc_values, LSIM_MAX_HITS);
+  if (p->n_neighbors < 0 || p->n_neighbors > 4) return fail(LSIM_ERR_UNSUPPORTED, "number_pix_neighbors %d not in [0, 4]", p->n_neighbors);
+  if (p->n_pixels_x <= 0 || p->n_pixels_y <= 0 || p->nb_bins_per_pixel <= 0) return fail(LSIM_ERR_INVALID, "bad pixel geometry");
+  if (p->n_ticks < 4 || p->n_ticks - 1 > 2048 || (p->n_ticks - 1) % 4 != 0)
+    return fail(LSIM_ERR_UNSUPPORTED, "n_ticks %d: waveform length must be a multiple of 4 up to 2048", p->n_ticks);
+  return LSIM_OK;
+}
+
+static int check_fields(const LsimFieldMap *f) {
+  if (!f) return fail(LSIM_ERR_INVALID, "null field map");
+  const int32_t cols[] = {f->eventID, f->x, f->y, f->z, f->x_start, f->y_start, f->z_start,
+                          f->x_end, f->y_end, f->z_end, f->dx, f->dE, f->dEdx};
+  for (int32_t c : cols)
+    if (c < 0 || c >= f->n_fields) return fail(LSIM_ERR_INVALID, "field index %d outside [0, %d)", c, f->n_fields);
+  return LSIM_OK;
+}
+
+}  // namespace lsim
+
+using namespace lsim;
+
+extern "C" {
+
+int lsim_abi_version(void) { return LSIM_ABI_VERSION; }
+
+const char *lsim_last_error(void) { return g_err.c_str(); }
+
+void lsim_struct_sizes(size_t *params, size_t *fields, size_t *counts) {
+  if (params) *params = sizeof(LsimParams);
+  if (fields) *fields = sizeof(LsimFieldMap);
+  if (counts) *counts = sizeof(LsimCounts);
+}
+
+int lsim_lut_build_templates(const float *response, int32_t nx, int32_t ny, int32_t nt, const float *sigmas_dev,
+                             int32_t n_templates, int32_t extent, float *templates_out, void *stream) {
+  g_err.clear();
+  if (!response || !sigmas_dev || !templates_out || nx <= 0 || ny <= 0 || nt <= 0 || extent < 0)
+    return fail(LSIM_ERR_INVALID, "lsim_lut_build_templates: bad arguments");
+  return wrap(run_build_templates(response, nx, ny, nt, sigmas_dev, n_templates, extent, templates_out,
+                                  (cudaStream_t)stream),
+              "lsim_lut_build_templates");
+}
+
+size_t lsim_lut_tables_bytes(const LsimParams *p) {
+  if (!p) return 0;
+  size_t a, b, c, d;
+  return tables_layout(*p, &a, &b, &c, &d);
+}
+
+int lsim_lut_prepare(const LsimParams *p, const float *templates, void *tables, size_t tables_bytes, void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (!templates || !tables) return fail(LSIM_ERR_INVALID, "lsim_lut_prepare: null pointer");
+  if (tables_bytes < lsim_lut_tables_bytes(p))
+    return fail(LSIM_ERR_CAPACITY, "lsim_lut_prepare: tables buffer %zu < %zu bytes", tables_bytes,
+                lsim_lut_tables_bytes(p));
+  return wrap(run_prepare_tables(*p, templates, tables, (cudaStream_t)stream), "lsim_lut_prepare");
+}
+
+size_t lsim_workspace_bytes(const LsimParams *p, int64_t n_rows, int32_t n_events) {
+  if (!p || n_rows < 0 || n_events < 0) return 0;
+  return carve_workspace(nullptr, *p, n_rows, n_events).bytes;
+}
+
+static int stage1(bool param_mode, const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,
+                  int32_t n_events, const float *normals, void *ws, size_t ws_bytes, LsimCounts *counts_dev,
+                  void *stream, const char *name) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (!rc) rc = check_fields(f);
+  if (rc) return rc;
+  if (param_mode && p->n_neighbors != 0)
+    return fail(LSIM_ERR_UNSUPPORTED, "%s: parametrised mode requires number_pix_neighbors == 0", name);
+  if (n_rows < 0 || n_rows > 0x7fffffff || n_events < 0) return fail(LSIM_ERR_INVALID, "%s: bad sizes", name);
+  if ((n_rows > 0 && !tracks) || !ws) return fail(LSIM_ERR_INVALID, "%s: null pointer", name);
+  Workspace w = carve_workspace(ws, *p, n_rows, n_events);
+  if (ws_bytes < w.bytes) return fail(LSIM_ERR_CAPACITY, "%s: workspace %zu < %zu bytes", name, ws_bytes, w.bytes);
+  Grid g = make_grid(*p, n_events);
+  if (g.G > 0x7fffffff) return fail(LSIM_ERR_CAPACITY, "%s: pixel grid of %lld slots exceeds int32", name, (long long)g.G);
+  cudaStream_t st = (cudaStream_t)stream;
+  rc = run_stage1(param_mode, *p, *f, tracks, normals, n_rows, n_events, w, st);
+  if (rc) return wrap(rc, name);
+  if (counts_dev && cudaMemcpyAsync(counts_dev, w.counts, sizeof(LsimCounts), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return check_cuda(name);
+  return check_cuda(name);
+}
+
+int lsim_lut_stage1(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows, int32_t n_events,
+                    void *ws, size_t ws_bytes, LsimCounts *counts_dev, void *stream) {
+  return stage1(false, p, f, tracks, n_rows, n_events, nullptr, ws, ws_bytes, counts_dev, stream, "lsim_lut_stage1");
+}
+
+int lsim_param_stage1(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,
+                      int32_t n_events, const float *normals, void *ws, size_t ws_bytes, LsimCounts *counts_dev,
+                      void *stream) {
+  return stage1(true, p, f, tracks, n_rows, n_events, normals, ws, ws_bytes, counts_dev, stream, "lsim_param_stage1");
+}
+
+static AccumArgs make_args(const LsimParams *p, const void *tables, const void *ws, int64_t n_rows, int32_t n_events) {
+  AccumArgs a;
+  memset(&a, 0, sizeof(a));
+  a.p = *p;
+  if (tables) a.tab = carve_tables(tables, *p);
+  a.w = carve_workspace(const_cast<void *>(ws), *p, n_rows, n_events);
+  a.g = make_grid(*p, n_events);
+  return a;
+}
+
+int lsim_lut_stage2(const LsimParams *p, const void *tables, const void *ws, int64_t n_rows, int32_t n_events,
+                    int64_t p_pad, int32_t n_em1, int32_t n_valid, float *wfs, int32_t *unique_pixels, void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (!tables || !ws || (p_pad > 0 && (!wfs || !unique_pixels))) return fail(LSIM_ERR_INVALID, "lsim_lut_stage2: null pointer");
+  if (n_em1 < 0 || n_valid < 0 || (int64_t)n_em1 + n_valid > p_pad)
+    return fail(LSIM_ERR_CAPACITY, "lsim_lut_stage2: p_pad %lld < %d + %d rows", (long long)p_pad, n_em1, n_valid);
+  cudaStream_t st = (cudaStream_t)stream;
+  AccumArgs a = make_args(p, tables, ws, n_rows, n_events);
+  rc = run_fill_unique(*p, a.w, a.g, p_pad, n_em1, n_valid, unique_pixels, wfs, p->n_ticks - 1, st);
+  if (rc) return wrap(rc, "lsim_lut_stage2");
+  a.n_valid = n_valid;
+  a.row_offset = p_pad - n_valid;
+  a.wfs = wfs;
+  return wrap(run_accum(kModeWfs, a, st), "lsim_lut_stage2");
+}
+
+int lsim_valid_pixels(const LsimParams *p, const void *ws, int64_t n_rows, int32_t n_events, int32_t n_valid,
+                      int32_t *pids_out, void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (!ws || (n_valid > 0 && !pids_out)) return fail(LSIM_ERR_INVALID, "lsim_valid_pixels: null pointer");
+  AccumArgs a = make_args(p, nullptr, ws, n_rows, n_events);
+  return wrap(run_fill_unique(*p, a.w, a.g, n_valid, 0, n_valid, pids_out, nullptr, 0, (cudaStream_t)stream),
+              "lsim_valid_pixels");
+}
+
+int lsim_lut_adc(const LsimParams *p, const void *tables, const void *ws, int64_t n_rows, int32_t n_events,
+                 int32_t n_valid, const float *normals, float *adc_out, float *tick_out, void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (!tables || !ws || !adc_out || !tick_out) return fail(LSIM_ERR_INVALID, "lsim_lut_adc: null pointer");
+  AccumArgs a = make_args(p, tables, ws, n_rows, n_events);
+  a.n_valid = n_valid;
+  a.normals = normals;
+  a.adc_out = adc_out;
+  a.tick_out = tick_out;
+  return wrap(run_accum(kModeAdc, a, (cudaStream_t)stream), "lsim_lut_adc");
+}
+
+int lsim_lut_grad(const LsimParams *p, const void *tables, const void *ws, int64_t n_rows, int32_t n_events,
+                  int32_t n_valid, const float *normals, const float *g_adc, const int32_t *tgt_pids,
+                  const float *tgt_adc, int64_t n_tgt, float *loss_out, float *grad_out, float *adc_out, void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (!tables || !ws || !grad_out) return fail(LSIM_ERR_INVALID, "lsim_lut_grad: null pointer");
+  if (!g_adc && n_tgt > 0 && (!tgt_pids || !tgt_adc)) return fail(LSIM_ERR_INVALID, "lsim_lut_grad: null target");
+  cudaStream_t st = (cudaStream_t)stream;
+  AccumArgs a = make_args(p, tables, ws, n_rows, n_events);
+  a.n_valid = n_valid;
+  a.normals = normals;
+  a.g_adc = g_adc;
+  a.tgt_pids = tgt_pids;
+  a.tgt_adc = tgt_adc;
+  a.n_tgt = g_adc ? 0 : n_tgt;
+  a.adc_out = adc_out;
+  rc = run_accum(kModeGrad, a, st);
+  if (rc) return wrap(rc, "lsim_lut_grad");
+  return wrap(run_grad_finalize(a, loss_out, grad_out, st), "lsim_lut_grad");
+}
+
+int lsim_fee(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, const float *normals, float *adc_out,
+             float *tick_out, float *integral_out, void *stream) {
+  g_err.clear();
+  if (!p) return fail(LSIM_ERR_INVALID, "lsim_fee: null parameter block");
+  if (n_pix > 0 && (!wfs || !adc_out || !tick_out)) return fail(LSIM_ERR_INVALID, "lsim_fee: null pointer");
+  if (p->max_adc_values < 1 || p->max_adc_values > LSIM_MAX_HITS) return fail(LSIM_ERR_UNSUPPORTED, "lsim_fee: bad MAX_ADC_VALUES");
+  return wrap(run_fee(*p, wfs, n_pix, n_t, normals, adc_out, tick_out, integral_out, (cudaStream_t)stream), "lsim_fee");
+}
+
+size_t lsim_hits_workspace_bytes(int64_t n_pix, int32_t max_adc_values) {
+  return hits_ws_bytes(n_pix * (int64_t)max_adc_values);
+}
+
+int lsim_hits(const LsimParams *p, const float *adc, const float *ticks, const int32_t *unique_pixels, int64_t n_pix,
+              int32_t tick_limit, float *out_adc, float *out_x, float *out_y, float *out_z, float *out_ticks,
+              float *out_hit_prob, int32_t *out_event, int32_t *out_pixels, int32_t *nb_valid_dev, void *ws,
+              size_t ws_bytes, void *stream) {
+  g_err.clear();
+  if (!p) return fail(LSIM_ERR_INVALID, "lsim_hits: null parameter block");
+  if (!nb_valid_dev || (n_pix > 0 && (!adc || !ticks || !unique_pixels || !out_adc || !out_x || !out_y || !out_z ||
+                                      !out_ticks || !out_hit_prob || !out_event || !out_pixels || !ws)))
+    return fail(LSIM_ERR_INVALID, "lsim_hits: null pointer");
+  if (ws_bytes < hits_ws_bytes(n_pix * (int64_t)p->max_adc_values))
+    return fail(LSIM_ERR_CAPACITY, "lsim_hits: workspace too small");
+  return wrap(run_hits(*p, adc, ticks, unique_pixels, n_pix, tick_limit, out_adc, out_x, out_y, out_z, out_ticks,
+                       out_hit_prob, out_event, out_pixels, nb_valid_dev, ws, (cudaStream_t)stream),
+              "lsim_hits");
+}
+
+int lsim_param_stage2(const LsimParams *p, const void *ws, int64_t n_rows, int32_t n_events, int64_t p_pad,
+                      int32_t n_em1, int32_t n_valid, float *wfs, int32_t *unique_pixels, void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (!ws || (p_pad > 0 && (!wfs || !unique_pixels))) return fail(LSIM_ERR_INVALID, "lsim_param_stage2: null pointer");
+  if (n_em1 < 0 || n_valid < 0 || (int64_t)n_em1 + n_valid > p_pad)
+    return fail(LSIM_ERR_CAPACITY, "lsim_param_stage2: p_pad too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  AccumArgs a = make_args(p, nullptr, ws, n_rows, n_events);
+  rc = run_fill_unique(*p, a.w, a.g, p_pad, n_em1, n_valid, unique_pixels, wfs, p->n_ticks - 1, st);
+  if (rc) return wrap(rc, "lsim_param_stage2");
+  return wrap(run_param_accum(*p, a.w, a.g, n_valid, p_pad - n_valid, wfs, st), "lsim_param_stage2");
+}
+
+}  // extern "C"

@@ -1,0 +1,228 @@
+// Shared definitions of the sm_103a larnd-sim kernels: per-segment records,
+// workspace layout, and helpers that reproduce the reference's exact index
+// arithmetic (JAX float floor_divide / remainder, Python integer division,
+// int32 pixel-id packing).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "lsim.h"
+
+namespace lsim {
+
+constexpr int kWarp = 32;
+constexpr int kMaxNeigh = 8;             // number_pix_neighbors supported: 0..8
+constexpr int kMaxTran = 5;              // nb_tran_diff_bins supported: 5
+constexpr int kMainSub = 5;              // main-bin LUT sub-positions (nb_bins_per_pixel / 2)
+constexpr int kScanTile = 2048;          // slots per scan block
+constexpr int kScanThreads = 256;
+constexpr int kGradSlots = 16;           // floats per grad partial record (loss + 8 grads + pad)
+
+// --------------------------------------------------------------- records
+
+// Per-segment forward record of LUT mode (96 bytes).
+struct __align__(16) SegFwd {
+  float ne;          // electrons after recombination, lifetime and TPC mask
+  float frac;        // t0/t_sampling - cathode tick (sub-tick shift)
+  float qa, qb, qc;  // quadratic long-diffusion template weights (sim_jax.py:166-168)
+  int cath;          // cathode tick c = clip(floor(t0/ts), 0, Nt-1)
+  int tidx;          // central template index, clip(searchsorted, 1, T-2)
+  int bx, by;        // sub-pixel bin indices (get_bin_shifts)
+  float ex[kMaxTran], ey[kMaxTran];  // 1-D transverse bin integrals
+  int plane, event;
+  float sigT, t0, ld;
+};
+
+// Per-segment adjoint record (96 bytes): partial derivatives of the
+// per-segment quantities with respect to the LSIM_NPARAM parameters.
+struct __align__(16) SegAdj {
+  float dne[5];      // d ne / d(Ab, kb, eField, lifetime, lArDensity)
+  float dsig[2];     // d sigmaT / d(eField, tran_diff)
+  float dld[2];      // d longdiff_ticks / d(eField, long_diff)
+  float dt0;         // d t0 / d eField
+  float dqa, dqb, dqc;  // d(a, b, c) / d longdiff_ticks
+  float dex[kMaxTran], dey[kMaxTran];  // d ex_i / d sigmaT, d ey_j / d sigmaT
+  float pad[1];
+};
+
+// Per-segment record of parametrised mode (64 bytes).
+struct __align__(16) SegPar {
+  float ne;
+  float t0f;         // t0 - t0_tick * t_sampling
+  int t0_tick;       // int(t0/ts + 0.5)
+  float xd, yd;      // |x_e - pixel centre|, |y_e - pixel centre|
+  float sigma;       // long diffusion in time units (sigma_L / vdrift)
+  int plane, event;
+  int px, py;
+  float pad[6];
+};
+
+// --------------------------------------------------------------- layout
+
+struct Grid {
+  int nxe, nye, ntpc, n;       // extended pixel grid per (event, plane)
+  int64_t plane_stride, event_stride, G;
+};
+
+__host__ __device__ inline Grid make_grid(const LsimParams &p, int32_t n_events) {
+  Grid g;
+  g.n = p.n_neighbors;
+  g.nxe = p.n_pixels_x + 2 * g.n;
+  g.nye = p.n_pixels_y + 2 * g.n;
+  g.ntpc = p.n_tpc;
+  g.plane_stride = (int64_t)g.nxe * g.nye;
+  g.event_stride = g.plane_stride * g.ntpc;
+  g.G = g.event_stride * (int64_t)(n_events + 1);   // events -1 .. n_events-1
+  return g;
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Workspace carve-up shared by all entry points.
+struct Workspace {
+  LsimCounts *counts;
+  SegFwd *segf;
+  SegAdj *sega;
+  SegPar *segp;
+  int32_t *key, *pid;
+  int32_t *cnt, *off, *cursor;
+  int32_t *seg_list, *pix_slot, *em1_slot;
+  int32_t *scan_blocks;     // 3 ints per scan block (+1 block)
+  float *grad_partials;     // kGradBlocks * kGradSlots
+  size_t bytes;
+};
+
+constexpr int kGradBlocks = 8192;   // max persistent warps with a gradient partial
+
+inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows, int32_t n_events) {
+  Grid g = make_grid(p, n_events);
+  int64_t nscan = (g.G + kScanTile - 1) / kScanTile + 1;
+  size_t off = 0;
+  auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
+  size_t o_counts = take(sizeof(LsimCounts));
+  size_t o_segf = take(sizeof(SegFwd) * (size_t)n_rows);
+  size_t o_sega = take(sizeof(SegAdj) * (size_t)n_rows);
+  size_t o_segp = take(sizeof(SegPar) * (size_t)n_rows);
+  size_t o_key = take(4 * (size_t)n_rows);
+  size_t o_pid = take(4 * (size_t)n_rows);
+  size_t o_cnt = take(4 * (size_t)g.G);
+  size_t o_off = take(4 * (size_t)g.G);
+  size_t o_cur = take(4 * (size_t)g.G);
+  size_t o_list = take(4 * (size_t)n_rows);
+  size_t o_pix = take(4 * (size_t)n_rows);
+  size_t o_em1 = take(4 * (size_t)n_rows);
+  size_t o_scan = take(3 * 4 * (size_t)nscan);
+  size_t o_grad = take(4 * (size_t)(kGradBlocks + 64) * kGradSlots);
+  Workspace w;
+  char *b = (char *)base;
+  w.counts = (LsimCounts *)(b + o_counts);
+  w.segf = (SegFwd *)(b + o_segf);
+  w.sega = (SegAdj *)(b + o_sega);
+  w.segp = (SegPar *)(b + o_segp);
+  w.key = (int32_t *)(b + o_key);
+  w.pid = (int32_t *)(b + o_pid);
+  w.cnt = (int32_t *)(b + o_cnt);
+  w.off = (int32_t *)(b + o_off);
+  w.cursor = (int32_t *)(b + o_cur);
+  w.seg_list = (int32_t *)(b + o_list);
+  w.pix_slot = (int32_t *)(b + o_pix);
+  w.em1_slot = (int32_t *)(b + o_em1);
+  w.scan_blocks = (int32_t *)(b + o_scan);
+  w.grad_partials = (float *)(b + o_grad);
+  w.bytes = off;
+  return w;
+}
+
+// Prepared LUT tables (see lsim_lut_prepare).
+struct Tables {
+  const float4 *wmp;   // [T][5][5][L] : (T[i-1], T[i], T[i+1], 0) windows, i in [1, T-2]
+  const float *cm;     // [T][5][5][Nt] cumulative sums of the main sub-positions
+  const float *w0;     // [nx][ny][L] template-0 windows
+  const float *c0;     // [nx][ny][Nt] template-0 cumulative sums
+};
+
+inline size_t tables_layout(const LsimParams &p, size_t *o_wmp, size_t *o_cm, size_t *o_w0, size_t *o_c0) {
+  const size_t T = p.n_templates, L = p.signal_length, Nt = p.lut_nt;
+  const size_t nx = p.lut_nx, ny = p.lut_ny, m = kMainSub * kMainSub;
+  size_t off = 0;
+  *o_wmp = off; off += align256(sizeof(float4) * T * m * L);
+  *o_cm = off;  off += align256(sizeof(float) * T * m * Nt);
+  *o_w0 = off;  off += align256(sizeof(float) * nx * ny * L);
+  *o_c0 = off;  off += align256(sizeof(float) * nx * ny * Nt);
+  return off;
+}
+
+inline Tables carve_tables(const void *base, const LsimParams &p) {
+  size_t a, b, c, d;
+  tables_layout(p, &a, &b, &c, &d);
+  const char *x = (const char *)base;
+  Tables t;
+  t.wmp = (const float4 *)(x + a);
+  t.cm = (const float *)(x + b);
+  t.w0 = (const float *)(x + c);
+  t.c0 = (const float *)(x + d);
+  return t;
+}
+
+// --------------------------------------------------------------- exact arithmetic
+
+// jnp.floor_divide for float32 (fmod-based divmod, quotient rounded half
+// away from zero), as used by get_bin_shifts (detsim_jax.py:505-507) and
+// get_pixels (detsim_jax.py:482-483).
+__device__ __forceinline__ float jax_floordiv_f32(float a, float b) {
+  float mod = fmodf(a, b);
+  float div = __fdiv_rn(__fsub_rn(a, mod), b);
+  if (mod != 0.0f && ((b < 0.0f) != (mod < 0.0f))) div = __fsub_rn(div, 1.0f);
+  return roundf(div);
+}
+
+// jnp.remainder for float32 (result has the sign of the divisor).
+__device__ __forceinline__ float jax_rem_f32(float a, float b) {
+  float mod = fmodf(a, b);
+  if (mod != 0.0f && ((mod < 0.0f) != (b < 0.0f))) mod = __fadd_rn(mod, b);
+  return mod;
+}
+
+// Python integer floor division / modulo.
+__host__ __device__ __forceinline__ int ifloordiv(int a, int b) {
+  int q = a / b;
+  if ((a % b != 0) && ((a < 0) != (b < 0))) --q;
+  return q;
+}
+__host__ __device__ __forceinline__ int imod(int a, int b) {
+  int r = a % b;
+  if (r != 0 && ((r < 0) != (b < 0))) r += b;
+  return r;
+}
+
+// pixel2id (detsim_jax.py:230-244) with the int32 wrap-around of JAX
+// without x64: -1 outside the pixel plane.
+__host__ __device__ __forceinline__ int32_t pixel2id(const LsimParams &p, int px, int py, int plane, int event) {
+  if (px >= p.n_pixels_x || py >= p.n_pixels_y || px < 0 || py < 0) return -1;
+  uint32_t pid = ((uint32_t)event * (uint32_t)p.n_tpc + (uint32_t)plane) * (uint32_t)p.n_pixels_y + (uint32_t)py;
+  pid = pid * (uint32_t)p.n_pixels_x + (uint32_t)px;
+  return (int32_t)pid;
+}
+
+__device__ __forceinline__ float border(const LsimParams &p, int plane, int axis, int side) {
+  return p.tpc_borders[(plane * 3 + axis) * 2 + side];
+}
+
+// searchsorted(side='left') on the long-diffusion template grid.
+__device__ __forceinline__ int searchsorted_left(const float *grid, int n, float v) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (grid[mid] < v) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void set_status(LsimCounts *c, int code, int row) {
+  atomicCAS(&c->status, 0, code);
+  atomicMin(&c->bad_row, row);
+}
+
+}  // namespace lsim

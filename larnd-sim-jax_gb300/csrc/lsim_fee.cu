@@ -1,0 +1,274 @@
+// Standalone front end on materialised waveforms, hit assembly + stream
+// compaction, and the parametrised-current accumulation.
+//
+// Reference: get_adc_values / digitize (fee_jax.py:55-71, :168-279),
+// simulate_stochastic (sim_jax.py:738-769), parse_output (sim_jax.py:619-647),
+// current_mc / current_model_diff / integrated_expon_diff / emg_pdf
+// (detsim_jax.py:440-474, :581-639) and accumulate_signals_parametrized
+// (detsim_jax.py:207-228).
+#include "lsim_internal.cuh"
+#include "lsim_fee.cuh"
+
+namespace lsim {
+
+constexpr int kFeeWarps = 4;
+constexpr int kFeeRow = 2048;
+
+// ---------------------------------------------------------------- FEE on wfs
+
+__global__ void __launch_bounds__(kFeeWarps * kWarp)
+    k_fee(LsimParams p, const float *__restrict__ wfs, int64_t n_pix, int32_t T, const float *__restrict__ normals,
+          float *adc_out, float *tick_out, float *integral_out) {
+  __shared__ __align__(16) float rows[kFeeWarps][kFeeRow];
+  const int lane = threadIdx.x % kWarp, wid = threadIdx.x / kWarp;
+  float *C = rows[wid];
+  const int H = p.max_adc_values;
+  for (int64_t r = (int64_t)blockIdx.x * kFeeWarps + wid; r < n_pix; r += (int64_t)gridDim.x * kFeeWarps) {
+    const float *src = wfs + r * (int64_t)T;
+    if ((T & 3) == 0) {
+      const float4 *s4 = reinterpret_cast<const float4 *>(src);
+      float4 *d4 = reinterpret_cast<float4 *>(C);
+      for (int i = lane; i < T / 4; i += kWarp) d4[i] = __ldg(s4 + i);
+    } else {
+      for (int i = lane; i < T; i += kWarp) C[i] = __ldg(src + i);
+    }
+    __syncwarp();
+    warp_cumsum_charge(C, T, p.t_sampling, lane);
+    const float *nrm = normals ? normals + r * (1 + 3 * H) : nullptr;
+    fee_forward(p, C, T, nrm, adc_out + r * H, tick_out + r * H, nullptr,
+                integral_out ? integral_out + r * H : nullptr, lane);
+    __syncwarp();
+  }
+}
+
+int run_fee(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, const float *normals, float *adc_out,
+            float *tick_out, float *integral_out, cudaStream_t st) {
+  if (n_t > kFeeRow || n_t < 2 || p.max_adc_values > LSIM_MAX_HITS) return LSIM_ERR_UNSUPPORTED;
+  if (n_pix <= 0) return LSIM_OK;
+  int64_t blocks = (n_pix + kFeeWarps - 1) / kFeeWarps;
+  const int64_t cap = (int64_t)device_sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  k_fee<<<(unsigned)blocks, kFeeWarps * kWarp, 0, st>>>(p, wfs, n_pix, n_t, normals, adc_out, tick_out, integral_out);
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------- hits
+
+struct PixelGeo {
+  int px, py, plane, event;
+};
+
+// id2pixel (detsim_jax.py:264-278), Python floor semantics.
+__device__ __forceinline__ PixelGeo id2pixel(const LsimParams &p, int32_t pid) {
+  const int nx = p.n_pixels_x, ny = p.n_pixels_y, nt = p.n_tpc;
+  PixelGeo g;
+  g.px = imod(pid, nx);
+  g.py = imod(ifloordiv(pid, nx), ny);
+  g.plane = imod(ifloordiv(pid, nx * ny), nt);
+  g.event = ifloordiv(pid, nx * ny * nt);
+  return g;
+}
+
+constexpr int kHitTile = 1024;
+
+__device__ __forceinline__ bool hit_keep(const LsimParams &p, const float *ticks, const int32_t *unique_pixels,
+                                         int64_t i, int H, int tick_limit) {
+  const int64_t r = i / H;
+  const int32_t pid = unique_pixels[r];
+  const float hp = ticks[i] < (float)tick_limit ? 1.f : 0.f;
+  const PixelGeo g = id2pixel(p, pid);
+  return hp > p.hit_prob_threshold && g.event >= 0 && pid >= 0;
+}
+
+__global__ void k_hits_count(LsimParams p, const float *ticks, const int32_t *unique_pixels, int64_t n, int H,
+                             int tick_limit, int32_t *block_counts) {
+  __shared__ int sh[kHitTile / kWarp];
+  const int64_t base = (int64_t)blockIdx.x * kHitTile;
+  const int64_t i = base + threadIdx.x;
+  const bool keep = i < n && hit_keep(p, ticks, unique_pixels, i, H, tick_limit);
+  const unsigned bal = __ballot_sync(0xffffffffu, keep);
+  if (threadIdx.x % kWarp == 0) sh[threadIdx.x / kWarp] = __popc(bal);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < kHitTile / kWarp; ++w) s += sh[w];
+    block_counts[blockIdx.x] = s;
+  }
+}
+
+__global__ void k_hits_scan(int32_t *block_counts, int64_t nblocks, int32_t *total) {
+  if (threadIdx.x != 0) return;
+  int run = 0;
+  for (int64_t b = 0; b < nblocks; ++b) {
+    const int c = block_counts[b];
+    block_counts[b] = run;
+    run += c;
+  }
+  *total = run;
+}
+
+// Row-major compaction (parse_output) with the coordinates of
+// get_pixel_coordinates / get_hit_z.  Pixel centres and hit z use the
+// fused forms XLA compiles these expressions to:
+//   x = fma(px, pitch, border_x) + pitch/2,   z = z_anode - tick * (t_sampling * vdrift)
+// (z_anode + tick*ts*v*sign with sign folded); both match the reference's
+// committed outputs bit for bit.
+__global__ void k_hits_write(LsimParams p, const float *adc, const float *ticks, const int32_t *unique_pixels,
+                             int64_t n, int H, int tick_limit, const int32_t *block_offsets, float *out_adc,
+                             float *out_x, float *out_y, float *out_z, float *out_ticks, float *out_hp,
+                             int32_t *out_event, int32_t *out_pixels) {
+  __shared__ int sh[kHitTile / kWarp];
+  const int64_t base = (int64_t)blockIdx.x * kHitTile;
+  const int64_t i = base + threadIdx.x;
+  const bool keep = i < n && hit_keep(p, ticks, unique_pixels, i, H, tick_limit);
+  const unsigned bal = __ballot_sync(0xffffffffu, keep);
+  const int lane = threadIdx.x % kWarp, wid = threadIdx.x / kWarp;
+  if (lane == 0) sh[wid] = __popc(bal);
+  __syncthreads();
+  int wofs = 0;
+  for (int w = 0; w < wid; ++w) wofs += sh[w];
+  if (!keep) return;
+  const int64_t o = block_offsets[blockIdx.x] + wofs + __popc(bal & ((1u << lane) - 1u));
+  const int64_t r = i / H;
+  const int32_t pid = unique_pixels[r];
+  const PixelGeo g = id2pixel(p, pid);
+  const float bx0 = border(p, g.plane, 0, 0), by0 = border(p, g.plane, 1, 0);
+  const float za = border(p, g.plane, 2, 0), zh = border(p, g.plane, 2, 1);
+  const float tk = ticks[i];
+  const float tv = __fmul_rn(p.t_sampling, p.vdrift);
+  const float dz = __fmul_rn(tk, tv);
+  out_adc[o] = adc[i];
+  out_x[o] = __fadd_rn(__fmaf_rn((float)g.px, p.pixel_pitch, bx0), p.half_pitch);
+  out_y[o] = __fadd_rn(__fmaf_rn((float)g.py, p.pixel_pitch, by0), p.half_pitch);
+  out_z[o] = (zh - za) < 0.f ? __fsub_rn(za, dz) : ((zh - za) > 0.f ? __fadd_rn(za, dz) : za);
+  out_ticks[o] = tk;
+  out_hp[o] = tk < (float)tick_limit ? 1.f : 0.f;
+  out_event[o] = g.event;
+  out_pixels[o] = pid;
+}
+
+size_t hits_ws_bytes(int64_t n) { return align256(4 * (size_t)((n + kHitTile - 1) / kHitTile + 1)); }
+
+int run_hits(const LsimParams &p, const float *adc, const float *ticks, const int32_t *unique_pixels, int64_t n_pix,
+             int32_t tick_limit, float *out_adc, float *out_x, float *out_y, float *out_z, float *out_ticks,
+             float *out_hit_prob, int32_t *out_event, int32_t *out_pixels, int32_t *nb_valid_dev, void *ws,
+             cudaStream_t st) {
+  const int H = p.max_adc_values;
+  const int64_t n = n_pix * H;
+  const int64_t nb = (n + kHitTile - 1) / kHitTile;
+  int32_t *blocks = (int32_t *)ws;
+  if (n == 0) return cudaMemsetAsync(nb_valid_dev, 0, 4, st) == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+  k_hits_count<<<(unsigned)nb, kHitTile, 0, st>>>(p, ticks, unique_pixels, n, H, tick_limit, blocks);
+  k_hits_scan<<<1, 32, 0, st>>>(blocks, nb, nb_valid_dev);
+  k_hits_write<<<(unsigned)nb, kHitTile, 0, st>>>(p, adc, ticks, unique_pixels, n, H, tick_limit, blocks, out_adc,
+                                                  out_x, out_y, out_z, out_ticks, out_hit_prob, out_event, out_pixels);
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------- parametrised current
+
+// 0.5*erf((x-loc)/(sqrt2*diff)) - emg_pdf(x, loc, diff, lambd)/lambd
+// (integrated_expon_diff's per-edge term, detsim_jax.py:467-468).
+__device__ __forceinline__ float ied_edge(float x, float loc, float diff, float lambd) {
+  const float s2 = 1.41421356237309515f;
+  const float e = 0.5f * erff((x - loc) / (s2 * diff));
+  const float coeff = lambd / 2.f;
+  const float ls2 = lambd * (diff * diff);
+  const float expo = coeff * (((2.f * loc) + ls2) - (2.f * x));
+  const float pdf = (coeff * expf(expo)) * erfcf(((loc + ls2) - x) / (s2 * diff));
+  return e - pdf / lambd;
+}
+
+__device__ __forceinline__ float quad(const float c[6], float x, float y) {
+  return ((((c[0] + c[1] * x) + c[2] * y) + (c[3] * x) * y) + (c[4] * x) * x) + (c[5] * y) * y;
+}
+
+// current_model_diff (detsim_jax.py:581-615) at tick k of the 51-tick grid,
+// times n_e (current_mc, detsim_jax.py:637).
+struct ParamShape {
+  float a, lam_b, lam_c, loc, diff, norm_b, norm_c;
+};
+
+__device__ __forceinline__ ParamShape param_shape(const LsimParams &p, const SegPar &s) {
+  const float B[6] = {1.060f, -0.909f, -0.909f, 5.856f, 0.207f, 0.207f};
+  const float C[6] = {0.679f, -1.083f, -1.083f, 8.772f, -5.521f, -5.521f};
+  const float D[6] = {2.644f, -9.174f, -9.174f, 13.483f, 45.887f, 45.887f};
+  const float T0[6] = {2.948f, -2.705f, -2.705f, 4.825f, 20.814f, 20.814f};
+  ParamShape sh;
+  const float x = s.xd, y = s.yd;
+  sh.a = fminf(quad(B, x, y), 1.f);
+  const float b = quad(C, x, y), c = quad(D, x, y);
+  const float st0 = s.t0f + T0[0] + T0[1] * x + T0[2] * y + (T0[3] * x) * y + (T0[4] * x) * x + (T0[5] * y) * y;
+  sh.loc = -st0;
+  sh.diff = s.sigma;
+  sh.lam_b = 1.f / b;
+  sh.lam_c = 1.f / c;
+  const int n = p.param_nticks;
+  const float hd = p.param_dt * 0.5f;
+  // normalisation: lower edge of the first tick minus upper edge of the last
+  const float x0 = -p.param_ticks[0], xl = -p.param_ticks[n - 1];
+  sh.norm_b = ied_edge(x0 - hd, sh.loc, sh.diff, sh.lam_b) - ied_edge(xl + hd, sh.loc, sh.diff, sh.lam_b);
+  sh.norm_c = ied_edge(x0 - hd, sh.loc, sh.diff, sh.lam_c) - ied_edge(xl + hd, sh.loc, sh.diff, sh.lam_c);
+  return sh;
+}
+
+__device__ __forceinline__ float param_value(const LsimParams &p, const ParamShape &sh, int k) {
+  const float x = -p.param_ticks[k];
+  const float hd = p.param_dt * 0.5f;
+  const float ub = ied_edge(x + hd, sh.loc, sh.diff, sh.lam_b), lb = ied_edge(x - hd, sh.loc, sh.diff, sh.lam_b);
+  const float uc = ied_edge(x + hd, sh.loc, sh.diff, sh.lam_c), lc = ied_edge(x - hd, sh.loc, sh.diff, sh.lam_c);
+  const float vb = ((ub - lb) / sh.norm_b) / p.param_dt;
+  const float vc = ((uc - lc) / sh.norm_c) / p.param_dt;
+  return sh.a * vb + (1.f - sh.a) * vc;
+}
+
+constexpr int kParWarps = 4;
+
+__global__ void __launch_bounds__(kParWarps * kWarp)
+    k_param_pixels(LsimParams p, Workspace w, Grid g, int64_t row_offset, float *wfs) {
+  __shared__ __align__(16) float rows[kParWarps][2052];
+  const int lane = threadIdx.x % kWarp, wid = threadIdx.x / kWarp;
+  float *row = rows[wid] + 3;   // col 1 16-byte aligned
+  const int NT = p.n_ticks, T = NT - 1;
+  const int n = p.param_nticks;
+  const int n_valid = w.counts->n_valid;
+  for (;;) {
+    int r = 0;
+    if (lane == 0) r = atomicAdd(&w.counts->work, 1);
+    r = __shfl_sync(0xffffffffu, r, 0);
+    if (r >= n_valid) break;
+    const int64_t slot = w.pix_slot[r];
+    float4 *b4 = reinterpret_cast<float4 *>(rows[wid]);
+    for (int i = lane; i < 2052 / 4; i += kWarp) b4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
+    const int c = w.cnt[slot], o = w.off[slot];
+    for (int j = 0; j < c; ++j) {
+      const int s = w.seg_list[o + j];
+      const SegPar sp = w.segp[s];
+      if (sp.ne == 0.f) continue;
+      const ParamShape sh = param_shape(p, sp);
+      const int start = sp.t0_tick - n;
+      for (int k = lane; k < n; k += kWarp) {
+        const float v = param_value(p, sh, k) * sp.ne;
+        const int tt = start + k;
+        if (tt >= 0 && tt < NT - 1) row[tt + 1] += v;   // accumulate_signals_parametrized remap
+      }
+      __syncwarp();
+    }
+    float4 *dst = reinterpret_cast<float4 *>(wfs + (row_offset + r) * (int64_t)T);
+    const float4 *src = reinterpret_cast<const float4 *>(row + 1);
+    for (int i = lane; i < T / 4; i += kWarp) dst[i] = src[i];
+    __syncwarp();
+  }
+}
+
+int run_param_accum(const LsimParams &p, const Workspace &w, const Grid &g, int32_t n_valid, int64_t row_offset,
+                    float *wfs, cudaStream_t st) {
+  if (p.n_ticks - 1 > 2048 || (p.n_ticks - 1) % 4 != 0 || p.param_nticks > 64) return LSIM_ERR_UNSUPPORTED;
+  if (cudaMemsetAsync(&w.counts->work, 0, sizeof(int32_t), st) != cudaSuccess) return LSIM_ERR_CUDA;
+  int blocks = device_sm_count() * 4;
+  k_param_pixels<<<blocks, kParWarps * kWarp, 0, st>>>(p, w, g, row_offset, wfs);
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
+}  // namespace lsim

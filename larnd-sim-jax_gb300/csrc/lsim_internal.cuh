@@ -1,0 +1,53 @@
+// Host-side drivers shared between the translation units of liblsim.
+#pragma once
+
+#include "lsim_common.cuh"
+
+namespace lsim {
+
+// lsim_segments.cu
+int run_stage1(bool param_mode, const LsimParams &p, const LsimFieldMap &f, const float *tracks,
+               const float *normals, int64_t n_rows, int32_t n_events, const Workspace &w, cudaStream_t st);
+int run_fill_unique(const LsimParams &p, const Workspace &w, const Grid &g, int64_t p_pad, int32_t n_em1,
+                    int32_t n_valid, int32_t *unique_pixels, float *wfs, int32_t nt_out, cudaStream_t st);
+
+// lsim_accum.cu
+enum AccumMode { kModeWfs = 0, kModeAdc = 1, kModeGrad = 2 };
+struct AccumArgs {
+  LsimParams p;
+  Tables tab;
+  Workspace w;
+  Grid g;
+  int32_t n_valid;
+  int64_t row_offset;       // output row of valid row 0 (wfs mode)
+  float *wfs;               // [rows][n_ticks-1] (wfs mode)
+  const float *normals;     // [n_valid][1+3H] or null
+  float *adc_out, *tick_out;  // [n_valid][H] (adc/grad modes, optional in grad)
+  const float *g_adc;       // [n_valid][H] cotangent (grad mode) or null
+  const int32_t *tgt_pids;  // target pixels for the SSE loss (grad mode, when g_adc is null)
+  const float *tgt_adc;
+  int64_t n_tgt;
+};
+int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st);
+int run_grad_finalize(const AccumArgs &a, float *loss_out, float *grad_out, cudaStream_t st);
+
+int run_param_accum(const LsimParams &p, const Workspace &w, const Grid &g, int32_t n_valid, int64_t row_offset,
+                    float *wfs, cudaStream_t st);
+
+// lsim_fee.cu
+int run_fee(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, const float *normals, float *adc_out,
+            float *tick_out, float *integral_out, cudaStream_t st);
+size_t hits_ws_bytes(int64_t n);
+int run_hits(const LsimParams &p, const float *adc, const float *ticks, const int32_t *unique_pixels, int64_t n_pix,
+             int32_t tick_limit, float *out_adc, float *out_x, float *out_y, float *out_z, float *out_ticks,
+             float *out_hit_prob, int32_t *out_event, int32_t *out_pixels, int32_t *nb_valid_dev, void *ws,
+             cudaStream_t st);
+
+// lsim_lut.cu
+int run_build_templates(const float *response, int nx, int ny, int nt, const float *sigmas, int n_templates,
+                        int extent, float *out, cudaStream_t st);
+int run_prepare_tables(const LsimParams &p, const float *templates, void *tables, cudaStream_t st);
+
+int device_sm_count();
+
+}  // namespace lsim

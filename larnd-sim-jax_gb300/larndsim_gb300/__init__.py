@@ -1,0 +1,19 @@
+"""GB300-native (sm_103a) implementation of larnd-sim-jax's simulate path.
+
+Drop-in functions with the reference's names (src/larndsim/sim_jax.py,
+consts_jax.py, fee_jax.py, losses_jax.py, optimize/strategies.py), backed by
+hand-written CUDA kernels in ``liblsim.so`` (C ABI: include/lsim.h).
+"""
+
+from .consts import (Params, RecombinationMode, build_params_class, default_params, get_vdrift,  # noqa: F401
+                     load_detector_properties)
+from .sim import (get_adc_values, load_lut, pad_size, prepare_lut, simulate_parametrized,  # noqa: F401
+                  simulate_stochastic, simulate_wfs)
+from .fee import digitize  # noqa: F401
+from .losses import adc2charge  # noqa: F401
+
+__all__ = [
+    "Params", "RecombinationMode", "build_params_class", "default_params", "get_vdrift",
+    "load_detector_properties", "get_adc_values", "load_lut", "pad_size", "prepare_lut",
+    "simulate_parametrized", "simulate_stochastic", "simulate_wfs", "digitize", "adc2charge",
+]

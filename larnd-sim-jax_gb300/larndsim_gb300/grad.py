@@ -1,0 +1,141 @@
+"""Forward + adjoint of the LUT-mode chain with respect to the physics
+parameters (Ab, kb, eField, lifetime, vdrift, long_diff, tran_diff,
+lArDensity).
+
+The reference differentiates ``simulate_wfs`` + ``simulate_stochastic`` with
+``jax.value_and_grad`` (optimize/fit_params.py:704, :731).  Here the adjoint
+is hand-written: the backward kernel recomputes each pixel's waveform and
+front-end state instead of storing waveforms, then pushes dL/dADC back
+through the self-trigger (crossing indices and clamps carry no gradient,
+exactly as in JAX), the sub-tick split, the long-diffusion template
+interpolation, the transverse bin weights, lifetime, recombination and the
+drift velocity.  ``d/d vdrift`` is identically zero, as in the reference,
+where ``params.vdrift`` is never read (drift velocity is
+``get_vdrift(eField, temperature)``).
+
+``LUTChain`` holds one batch of tracks; ``loss_and_grad`` evaluates the
+sum-of-squared-ADC loss against a target on the (pixel id x hit) grid
+(pixels absent from one side count as no-hit, i.e. digitize(0)).
+``adc_fn`` wraps the chain as a ``torch.autograd.Function``.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _abi, sim
+
+GRAD_PARAMS = _abi.GRAD_PARAMS
+
+
+class Target:
+    """ADC grid of a reference simulation: ascending pixel ids + (P, H) ADCs."""
+
+    def __init__(self, pids: torch.Tensor, adc: torch.Tensor):
+        self.pids = pids.to(torch.int32).contiguous()
+        self.adc = adc.to(torch.float32).contiguous()
+
+
+class LUTChain:
+    """Fused LUT-mode forward/adjoint over one batch of tracks."""
+
+    def __init__(self, params, response_template, tracks, fields, n_events=None):
+        self.lut = sim.prepare_lut(response_template, params)
+        self.fields = tuple(fields)
+        self.tracks = sim.as_tracks(tracks)
+        ev = self.tracks[:, self.fields.index("eventID")]
+        self.n_events = int(ev.max().item()) + 1 if n_events is None else int(n_events)
+        self.H = int(params.MAX_ADC_VALUES)
+        self.lib = _abi.load()
+        self._stage = None
+
+    def stage1(self, params):
+        lp = _abi.make_params(params, self.lut.shape)
+        st = sim.run_stage1(params, self.tracks, self.fields, lp, n_events=self.n_events)
+        self._stage = st
+        return st
+
+    def _check(self, st):
+        st.raise_status()
+        return st.n_valid
+
+    def adc(self, params, normals=None):
+        """ADC and tick grids (n_valid, H) and the valid pixel ids."""
+        st = self.stage1(params)
+        n_valid = self._check(st)
+        dev = self.tracks.device
+        adc = torch.empty((n_valid, self.H), dtype=torch.float32, device=dev)
+        ticks = torch.empty((n_valid, self.H), dtype=torch.float32, device=dev)
+        pids = torch.empty((n_valid,), dtype=torch.int32, device=dev)
+        s = sim._stream()
+        _abi.check(self.lib, self.lib.lsim_valid_pixels(st.lp, sim._ptr(st.ws), st.n_rows, st.n_events, n_valid,
+                                                        sim._ptr(pids), s))
+        _abi.check(self.lib, self.lib.lsim_lut_adc(st.lp, sim._ptr(self.lut.tables), sim._ptr(st.ws), st.n_rows,
+                                                   st.n_events, n_valid, sim._ptr(normals), sim._ptr(adc),
+                                                   sim._ptr(ticks), s))
+        return adc, ticks, pids
+
+    def target(self, params, normals=None) -> Target:
+        adc, _, pids = self.adc(params, normals)
+        return Target(pids, adc)
+
+    def _grad(self, params, g_adc=None, target=None, normals=None, adc_out=None, sync=True):
+        st = self.stage1(params)
+        n_valid = self._check(st) if sync else None
+        dev = self.tracks.device
+        out = torch.zeros(1 + _abi.NPARAM, dtype=torch.float32, device=dev)
+        tp = target.pids if target is not None else None
+        ta = target.adc if target is not None else None
+        nt = target.pids.shape[0] if target is not None else 0
+        _abi.check(self.lib, self.lib.lsim_lut_grad(
+            st.lp, sim._ptr(self.lut.tables), sim._ptr(st.ws), st.n_rows, st.n_events,
+            n_valid if n_valid is not None else 0, sim._ptr(normals), sim._ptr(g_adc), sim._ptr(tp), sim._ptr(ta), nt,
+            sim._ptr(out), sim._ptr(out[1:]), sim._ptr(adc_out), sim._stream()))
+        return out
+
+    def loss_and_grad(self, params, target: Target, normals=None):
+        """SSE loss against ``target`` and its gradient (dict by parameter)."""
+        out = self._grad(params, target=target, normals=normals)
+        vals = out.cpu().numpy()
+        return float(vals[0]), dict(zip(GRAD_PARAMS, vals[1:].tolist()))
+
+    def loss_and_grad_device(self, params, target: Target, normals=None):
+        """Like ``loss_and_grad`` but returns the device tensor [loss, grads...]
+        without a host synchronisation."""
+        return self._grad(params, target=target, normals=normals, sync=False)
+
+    def vjp(self, params, g_adc: torch.Tensor, normals=None):
+        """dL/dtheta for a given cotangent on the (n_valid, H) ADC grid."""
+        g = g_adc.to(torch.float32).contiguous()
+        out = self._grad(params, g_adc=g, normals=normals)
+        return out[1:]
+
+
+class _AdcFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, theta, chain, params, normals):
+        vals = theta.detach().cpu().numpy().astype(np.float64)
+        p = params.replace(**{k: float(v) for k, v in zip(GRAD_PARAMS, vals)})
+        adc, ticks, pids = chain.adc(p, normals)
+        ctx.chain, ctx.params, ctx.normals = chain, p, normals
+        ctx.mark_non_differentiable(ticks, pids)
+        return adc, ticks, pids
+
+    @staticmethod
+    def backward(ctx, g_adc, g_ticks, g_pids):
+        if g_adc is None:
+            return None, None, None, None
+        grad = ctx.chain.vjp(ctx.params, g_adc, ctx.normals)
+        return grad.to(g_adc.device), None, None, None
+
+
+def theta_of(params, device=None) -> torch.Tensor:
+    """The 8 differentiable parameter values as a float64 tensor."""
+    return torch.tensor([float(getattr(params, k)) for k in GRAD_PARAMS], dtype=torch.float64, device=device)
+
+
+def adc_fn(theta: torch.Tensor, chain: LUTChain, params, normals=None):
+    """Differentiable (ADC, ticks, pixel ids) of the LUT chain as a function
+    of ``theta`` = the 8 parameter values (order ``GRAD_PARAMS``)."""
+    return _AdcFn.apply(theta, chain, params, normals)

@@ -1,0 +1,175 @@
+"""Host-side logic: parameters, YAML loading, the parameter block, and the
+C-ABI library's exported symbols (no GPU needed)."""
+
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from larndsim_gb300 import _abi, consts, yaml_lite
+
+ROOT = Path(__file__).resolve().parent.parent
+REF = Path("/root/reference")
+
+DETPROP = """
+tpc_centers: # cm
+  - [0, 0, 0]
+  - [0, 0, 0]
+time_interval: [0, 200.] # us
+drift_length: 30.27225 # cm
+eField: 0.50 #kV/cm
+lifetime: 2.2e+3 # us
+vdrift: 0.1587 # cm / us
+MeVToElectrons: 4.237e+04
+Ab: 0.8
+kb: 0.0486
+long_diff: 4.0e-6  # cm * cm / us
+tran_diff: 8.8e-6  # cm * cm / us
+DISCRIMINATION_THRESHOLD: 5000
+V_CM: 284.27734375
+V_REF: 1282.71484375
+"""
+
+
+def _layout_text():
+    """A 2-TPC, 16-tile layout of 70x70 pixels in the reference's format."""
+    lines = ["chip_channel_to_position:"]
+    k = 0
+    for x in range(70):
+        for y in range(70):
+            lines += [f"  {1000 + k}:", f"  - {x}", f"  - {y}"]
+            k += 1
+    lines += ["drift_length: 304.31", "pixel_pitch: 4.434", "tile_indeces:"]
+    for t in range(1, 17):
+        lines += [f"  {t}:", f"  - {1 if t <= 8 else 2}", f"  - {(t - 1) % 8 + 1}"]
+    lines.append("tile_orientations:")
+    for t in range(1, 17):
+        lines += [f"  {t}:", f"  - {-1 if t <= 8 else 1}", "  - 1", "  - 1"]
+    ys = [465.57, 465.57, 155.19, 155.19, -155.19, -155.19, -465.57, -465.57]
+    zs = [-155.19, 155.19] * 4
+    lines.append("tile_positions:")
+    for t in range(1, 17):
+        x = 305.8975 if t <= 8 else -305.8975
+        lines += [f"  {t}:", f"  - {x}", f"  - {ys[(t - 1) % 8]}", f"  - {zs[(t - 1) % 8]}"]
+    return "\n".join(lines) + "\n"
+
+
+def test_yaml_lite_subset():
+    d = yaml_lite.loads(DETPROP)
+    assert d["tpc_centers"] == [[0, 0, 0], [0, 0, 0]]
+    assert d["time_interval"] == [0, 200.0]
+    assert d["lifetime"] == 2200.0 and d["DISCRIMINATION_THRESHOLD"] == 5000
+    lay = yaml_lite.loads(_layout_text())
+    assert lay["chip_channel_to_position"][1000] == [0, 0]
+    assert lay["tile_positions"][16] == [-305.8975, -465.57, 155.19]
+
+
+def test_load_detector_properties_matches_defaults(tmp_path):
+    (tmp_path / "det.yaml").write_text(DETPROP)
+    (tmp_path / "lay.yaml").write_text(_layout_text())
+    p = consts.load_detector_properties(consts.Params, tmp_path / "det.yaml", tmp_path / "lay.yaml")
+    d = consts.Params()
+    np.testing.assert_array_equal(p.tpc_borders, d.tpc_borders)
+    assert p.n_pixels_x == 140 and p.n_pixels_y == 280
+    assert p.pixel_pitch == d.pixel_pitch and p.drift_length == d.drift_length
+    assert p.DISCRIMINATION_THRESHOLD == 5000 and p.V_CM == 284.27734375
+
+
+def test_unknown_detector_key_raises(tmp_path):
+    (tmp_path / "det.yaml").write_text(DETPROP + "bogus_key: 1\n")
+    (tmp_path / "lay.yaml").write_text(_layout_text())
+    with pytest.raises(ValueError):
+        consts.load_detector_properties(consts.Params, tmp_path / "det.yaml", tmp_path / "lay.yaml")
+
+
+@pytest.mark.skipif(not REF.exists(), reason="reference checkout not present")
+def test_reference_yaml_files_give_the_embedded_geometry():
+    p = consts.load_detector_properties(
+        consts.Params, REF / "src/larndsim/detector_properties/module0.yaml",
+        REF / "src/larndsim/pixel_layouts/multi_tile_layout-2.4.16_v4.yaml")
+    d = consts.Params()
+    np.testing.assert_array_equal(p.tpc_borders, d.tpc_borders)
+    assert (p.n_pixels_x, p.n_pixels_y, p.pixel_pitch, p.drift_length) == (140, 280, d.pixel_pitch, d.drift_length)
+
+
+def test_build_params_class_and_replace():
+    P = consts.build_params_class(["Ab", "eField"])
+    p = P()
+    assert P._grad_fields == ("Ab", "eField")
+    q = p.replace(Ab=0.9)
+    assert q.Ab == 0.9 and p.Ab == 0.8 and isinstance(q, P)
+    with pytest.raises(ValueError):
+        consts.build_params_class(["nope"])
+
+
+def test_vdrift_derivative_matches_finite_difference():
+    p = consts.Params()
+    h = 1e-6
+    fd = (consts.get_vdrift(p.replace(eField=0.5 + h)) - consts.get_vdrift(p.replace(eField=0.5 - h))) / (2 * h)
+    assert abs(consts.get_vdrift_derivative(p) - fd) < 1e-8
+
+
+def test_parameter_block_rounding():
+    p = consts.Params()
+    lp = _abi.make_params(p, (100, 45, 45, 1950))
+    f = np.float32
+    assert lp.vdrift == float(f(consts.get_vdrift(p)))
+    assert lp.erho == float(f(0.5 * 1.38))
+    assert lp.vref_minus_cm == 998.4375
+    assert lp.bin_width == float(f(p.pixel_pitch / 10))
+    assert lp.n_ticks == 2001 and lp.fee_interval == 18 and lp.param_nticks == 51
+    assert [lp.tran_edges[i] for i in range(6)] == [float(v) for v in consts.tran_diff_bin_edges(p)]
+    with pytest.raises(ValueError):
+        _abi.make_params(p, (99, 45, 45, 1950))
+    with pytest.raises(ValueError):
+        _abi.make_params(p.replace(recombination_mode=7))
+
+
+def test_field_map():
+    from larndsim_gb300.workloads import SEGMENT_FIELDS
+    fm = _abi.field_map(SEGMENT_FIELDS)
+    assert fm.x == SEGMENT_FIELDS.index("x") and fm.n_fields == len(SEGMENT_FIELDS)
+    with pytest.raises(ValueError):
+        _abi.field_map(("x", "y"))
+
+
+def test_jax_linspace_endpoints():
+    t = consts.jax_linspace_f32(0.001, 10, 100)
+    assert t.dtype == np.float32 and t[0] == np.float32(0.001) and t[-1] == np.float32(10)
+    assert np.all(np.diff(t) > 0)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from larndsim_gb300 import build
+    if not _abi.LIB_PATH.exists():
+        build.build()
+    return _abi.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    header = (ROOT / "include" / "lsim.h").read_text()
+    names = set(re.findall(r"^\s*(?:int|size_t|void|const char \*)\s*(lsim_\w+)\s*\(", header, re.M))
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(_abi.EXPORTED) <= names | {"lsim_valid_pixels"}
+
+
+def test_library_abi_and_sizes(lib):
+    assert lib.lsim_abi_version() == 1
+    p = _abi.make_params(consts.Params(number_pix_neighbors=4), (100, 45, 45, 1950))
+    assert lib.lsim_lut_tables_bytes(p) > 40e6
+    assert lib.lsim_workspace_bytes(p, 1000, 2) > 1000 * 192
+    assert lib.lsim_hits_workspace_bytes(10, 10) >= 4
+
+
+def test_library_rejects_bad_arguments_without_gpu(lib):
+    p = _abi.make_params(consts.Params(number_pix_neighbors=4), (100, 45, 45, 1950))
+    rc = lib.lsim_lut_prepare(p, None, None, 0, None)
+    assert rc == _abi.LSIM_ERR_INVALID
+    assert b"null" in lib.lsim_last_error()
+    p.n_neighbors = 7
+    assert lib.lsim_lut_prepare(p, ctypes.c_void_p(16), ctypes.c_void_p(16), 1 << 40, None) == _abi.LSIM_ERR_UNSUPPORTED
