@@ -16,6 +16,16 @@
 // Nt-L+k] * n_e; corr is the matching cumulative-sum boundary correction.
 // Value parts land only in waveform columns [2, Nticks-1], correction parts
 // only in [1, Nticks-2] (the index remaps of sim_jax.py:177-178, :243-244).
+//
+// Work split.  Neighbour parts (every slot of the (2n+1)^2 neighbourhood but
+// the centre, ~300 per pixel on dense events) go through a batched path:
+// 32 contributions at a time, lane j computes contribution j's descriptor
+// (LUT row, window origin, sub-tick fraction, charge, boundary correction,
+// adjoint partials) so the per-contribution L2 latency overlaps across
+// lanes; the window pass then streams two contributions' LUT rows with all
+// loads in flight.  Main-bin parts (segments in the 3x3 slots whose bins
+// fall on the pixel) take a per-contribution path over up to 5x5 grouped
+// LUT sub-positions.
 #include "lsim_internal.cuh"
 #include "lsim_fee.cuh"
 
@@ -25,35 +35,24 @@ constexpr int kAccWarps = 4;
 constexpr int kRowPad = 3;            // row[col] at buf[kRowPad + col]: col 1 is 16-byte aligned
 constexpr int kRowFloats = 2052;      // >= kRowPad + n_ticks (2001), multiple of 4
 constexpr int kMaxList = 81;          // (2 * 4 + 1)^2 neighbourhood slots
+constexpr int kChunks = 5;            // ceil((L + 2) / 32) for L <= 158
+
+// Descriptors of one batch of 32 neighbour contributions (structure of arrays).
+struct NBatch {
+  int row[kWarp];       // LUT row (cx * ny + cy) of template 0, -1 = skip
+  int cb[kWarp];        // window origin column
+  float frac[kWarp], ne[kWarp], D[kWarp], dl[kWarp];
+  float dne[5][kWarp], dt0[kWarp];   // adjoint only
+};
 
 struct ListSmem {
   int off[kMaxList];
   int cnt[kMaxList];
   int dxy[kMaxList];
+  int pre_n[kMaxList + 1];   // prefix of neighbour contributions (centre slot excluded)
   int n;
 };
 
-template <bool GRAD>
-struct WarpSmem;
-template <>
-struct WarpSmem<false> {
-  float buf[kRowFloats];
-  ListSmem list;
-  float adc[LSIM_MAX_HITS];
-};
-template <>
-struct WarpSmem<true> {
-  float buf[kRowFloats];
-  ListSmem list;
-  float adc[LSIM_MAX_HITS];
-  float gint[LSIM_MAX_HITS];
-  FeeState fee;
-};
-
-struct Theta {
-  float v[LSIM_NPARAM];
-  float loss;
-};
 
 // Sub-pixel LUT index of a bin, int(|b % nb - nb//2 + 0.5 - shift|)
 // (sim_jax.py:435, :443).
@@ -82,61 +81,6 @@ __device__ __forceinline__ void axis_weights(const float e[kMaxTran], const floa
   *umask = um;
 }
 
-struct Contribution {
-  // segment quantities
-  float ne, frac, qa, qb, qc;
-  int cath, tidx;
-  // neighbour part
-  bool has_n;
-  int n_off;              // (cx * ny + cy)
-  // main part
-  unsigned umask, vmask;
-  float Xw[kMainSub], Yw[kMainSub], dXw[kMainSub], dYw[kMainSub];
-  // window
-  int cb;                 // window origin column (s0 - 1)
-  float corr;             // boundary correction (forward)
-};
-
-__device__ __forceinline__ bool setup_contribution(const LsimParams &p, const SegFwd *__restrict__ segf,
-                                                   const SegAdj *__restrict__ sega, int s, int dx, int dy,
-                                                   bool need_deriv, Contribution &c) {
-  const SegFwd &f = segf[s];
-  c.ne = f.ne;
-  if (c.ne == 0.f) return false;
-  c.frac = f.frac; c.qa = f.qa; c.qb = f.qb; c.qc = f.qc;
-  c.cath = f.cath; c.tidx = f.tidx;
-  const int nb = p.nb_bins_per_pixel;
-  c.has_n = (dx != 0 || dy != 0);
-  if (c.has_n) {
-    const int cx = lut_index(f.bx, nb, dx * nb);
-    const int cy = lut_index(f.by, nb, dy * nb);
-    c.n_off = cx * p.lut_ny + cy;
-  }
-  c.umask = 0; c.vmask = 0;
-  if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1) {
-    float ex[kMaxTran], ey[kMaxTran], dex[kMaxTran], dey[kMaxTran];
-#pragma unroll
-    for (int i = 0; i < kMaxTran; ++i) {
-      ex[i] = f.ex[i]; ey[i] = f.ey[i];
-      dex[i] = need_deriv ? sega[s].dex[i] : 0.f;
-      dey[i] = need_deriv ? sega[s].dey[i] : 0.f;
-    }
-    axis_weights(ex, dex, f.bx, nb, dx, c.Xw, c.dXw, &c.umask);
-    axis_weights(ey, dey, f.by, nb, dy, c.Yw, c.dYw, &c.vmask);
-    if (!c.umask || !c.vmask) { c.umask = 0; c.vmask = 0; }
-  }
-  if (!c.has_n && !c.umask) return false;
-  c.cb = p.lut_nt - p.signal_length - c.cath - 1;
-  return true;
-}
-
-// Boundary correction of a contribution (sim_jax.py:236-261), and for the
-// adjoint its per-part derivative pieces.
-struct CorrParts {
-  float Dn;      // neighbour: Cum0[Nt-L] - lerp
-  float dCn;     // neighbour: Cum0[c] - Cum0[c+1]
-};
-
 __device__ __forceinline__ float cum_terms(const float *row, int cath, int Nt, int L, float frac, float *dlerp) {
   const float v0 = __ldg(row + cath);
   const float v1 = __ldg(row + min(cath + 1, Nt - 1));
@@ -145,70 +89,94 @@ __device__ __forceinline__ float cum_terms(const float *row, int cath, int Nt, i
   return vs - (v0 * (1.f - frac) + v1 * frac);
 }
 
-__device__ __forceinline__ float correction(const LsimParams &p, const Tables &tab, const Contribution &c) {
-  const int Nt = p.lut_nt, L = p.signal_length;
-  float corr = 0.f, dl;
-  if (c.has_n) corr += cum_terms(tab.c0 + (size_t)c.n_off * Nt, c.cath, Nt, L, c.frac, &dl) * c.ne;
-  if (c.umask) {
-    float cm = 0.f;
-#pragma unroll
-    for (int u = 0; u < kMainSub; ++u) {
-      if (!((c.umask >> u) & 1u)) continue;
-#pragma unroll
-      for (int v = 0; v < kMainSub; ++v) {
-        if (!((c.vmask >> v) & 1u)) continue;
-        const float *row = tab.cm + ((size_t)(c.tidx * kMainSub + u) * kMainSub + v) * Nt;
-        cm += (c.Xw[u] * c.Yw[v]) * cum_terms(row, c.cath, Nt, L, c.frac, &dl);
-      }
-    }
-    corr += cm * c.ne;
+// ---------------------------------------------------------------- neighbour batches
+
+// Decode global neighbour-contribution index g into (segment, dx, dy).
+__device__ __forceinline__ bool neigh_lookup(const ListSmem &ls, const int32_t *__restrict__ seg_list, int g, int *s,
+                                             int *dx, int *dy) {
+  int lo = 0, hi = ls.n;                 // last entry with pre_n <= g
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (ls.pre_n[mid] <= g) lo = mid; else hi = mid;
   }
-  return corr;
+  const int dxy = ls.dxy[lo];
+  *dx = (dxy & 0xff) - 16;
+  *dy = ((dxy >> 8) & 0xff) - 16;
+  if (*dx == 0 && *dy == 0) return false;
+  *s = __ldg(seg_list + ls.off[lo] + (g - ls.pre_n[lo]));
+  return true;
 }
 
-// V[k] of a contribution (k in [0, L)).
-__device__ __forceinline__ float value_at(const LsimParams &p, const Tables &tab, const Contribution &c, int k) {
-  const int L = p.signal_length;
-  float V = 0.f;
-  if (c.has_n) V = __ldg(tab.w0 + (size_t)c.n_off * L + k) * c.ne;
-  if (c.umask) {
-    float vm = 0.f;
+// Lane-parallel descriptor setup for neighbour contributions [g0, g0 + 32).
+template <bool GRAD>
+__device__ __forceinline__ void neigh_setup(const LsimParams &p, const Tables &tab, const Workspace &w,
+                                            const ListSmem &ls, NBatch &nb, int g0, int n_total, int lane) {
+  const int g = g0 + lane;
+  int row = -1, cb = 0, s = 0, dx = 0, dy = 0;
+  float frac = 0.f, ne = 0.f, D = 0.f, dl = 0.f;
+  if (g < n_total && neigh_lookup(ls, w.seg_list, g, &s, &dx, &dy)) {
+    const SegFwd &f = w.segf[s];
+    ne = __ldg(&f.ne);
+    if (ne != 0.f) {
+      const int nbp = p.nb_bins_per_pixel;
+      const int cx = lut_index(__ldg(&f.bx), nbp, dx * nbp);
+      const int cy = lut_index(__ldg(&f.by), nbp, dy * nbp);
+      row = cx * p.lut_ny + cy;
+      const int cath = __ldg(&f.cath);
+      frac = __ldg(&f.frac);
+      cb = p.lut_nt - p.signal_length - cath - 1;
+      D = cum_terms(tab.c0 + (size_t)row * p.lut_nt, cath, p.lut_nt, p.signal_length, frac, &dl);
+      if (GRAD) {
+        const SegAdj &a = w.sega[s];
 #pragma unroll
-    for (int u = 0; u < kMainSub; ++u) {
-      if (!((c.umask >> u) & 1u)) continue;
-#pragma unroll
-      for (int v = 0; v < kMainSub; ++v) {
-        if (!((c.vmask >> v) & 1u)) continue;
-        const float4 t = __ldg(tab.wmp + ((size_t)(c.tidx * kMainSub + u) * kMainSub + v) * L + k);
-        const float B = (t.y * c.qb + t.x * c.qa) + t.z * c.qc;
-        vm += (c.Xw[u] * c.Yw[v]) * B;
+        for (int i = 0; i < 5; ++i) nb.dne[i][lane] = __ldg(&a.dne[i]);
+        nb.dt0[lane] = __ldg(&a.dt0);
       }
     }
-    V += vm * c.ne;
   }
-  return V;
+  nb.row[lane] = row;
+  nb.cb[lane] = cb;
+  nb.frac[lane] = frac;
+  nb.ne[lane] = ne;
+  nb.D[lane] = D;
+  nb.dl[lane] = dl;
+  __syncwarp();
 }
 
-// Forward: add one contribution's L+2 window into the pixel row.
-__device__ __forceinline__ void add_window(const LsimParams &p, const Tables &tab, const Contribution &c, float *row,
-                                           int lane) {
+// Forward window of one contribution given its samples V[k] (v[m] holds
+// V[32m + lane - 1]).  Interior windows (the whole window inside columns
+// [1, Nticks-2]) take the fast path: the boundary correction is the
+// leading sample U[-1] of the window and val[r] = U[r-2](1-f) + U[r-1] f.
+__device__ __forceinline__ void window_apply(const LsimParams &p, const float v[kChunks], int cb, float frac,
+                                             float corr, float *row, int lane) {
   const int L = p.signal_length, NT = p.n_ticks;
-  const float corr = correction(p, tab, c);
-  const float f = c.frac, f1 = 1.f - c.frac;
+  const float f1 = 1.f - frac;
   float carry = 0.f;
-  for (int r0 = 0; r0 < L + 2; r0 += kWarp) {
-    const int r = r0 + lane;
-    const int k = r - 1;
-    const float Vk = (k >= 0 && k < L) ? value_at(p, tab, c, k) : 0.f;
+  if (cb >= 1 && cb + L + 1 <= NT - 2) {
+#pragma unroll
+    for (int m = 0; m < kChunks; ++m) {
+      float U = v[m];
+      if (m == 0 && lane == 0) U = corr;
+      float prev = __shfl_up_sync(0xffffffffu, U, 1);
+      if (lane == 0) prev = carry;
+      carry = __shfl_sync(0xffffffffu, U, kWarp - 1);
+      row[cb + m * kWarp + lane] += prev * f1 + U * frac;
+    }
+    return;
+  }
+#pragma unroll
+  for (int m = 0; m < kChunks; ++m) {
+    const int r = m * kWarp + lane;
+    const float Vk = v[m];
     float prev = __shfl_up_sync(0xffffffffu, Vk, 1);
     if (lane == 0) prev = carry;
     carry = __shfl_sync(0xffffffffu, Vk, kWarp - 1);
-    const int col = c.cb + r;
+    const int col = cb + r;
     if (r < L + 2) {
       float val = 0.f;
-      if (col >= 2 && col <= NT - 1) val = prev * f1 + Vk * f;
+      if (col >= 2 && col <= NT - 1) val = prev * f1 + Vk * frac;
       if (col >= 1 && col <= NT - 2) {
-        if (r == 0) val += corr * f;
+        if (r == 0) val += corr * frac;
         else if (r == 1) val += corr * f1;
       }
       if (col >= 1 && col <= NT - 1) row[col] += val;
@@ -216,134 +184,365 @@ __device__ __forceinline__ void add_window(const LsimParams &p, const Tables &ta
   }
 }
 
-// Adjoint: accumulate dL/dtheta of one contribution given the waveform
-// cotangent grow[col] (zero outside [1, Nticks-1]).
-__device__ __forceinline__ void window_vjp(const LsimParams &p, const Tables &tab, const Contribution &c,
-                                           const SegAdj &a, const float *grow, Theta &th, int lane) {
-  const int L = p.signal_length, NT = p.n_ticks, Nt = p.lut_nt;
-  const float f = c.frac, f1 = 1.f - c.frac;
-  auto Gv = [&](int col) { return (col >= 2 && col <= NT - 1) ? grow[col] : 0.f; };
-  auto Gc = [&](int col) { return (col >= 1 && col <= NT - 2) ? grow[col] : 0.f; };
-  // acc_fr holds frac terms already scaled by ne; acc_frm main-part terms
-  // still to be multiplied by ne (as are acc_sig, acc_a, acc_b, acc_c).
-  float acc_ne = 0.f, acc_sig = 0.f, acc_a = 0.f, acc_b = 0.f, acc_c = 0.f, acc_fr = 0.f, acc_frm = 0.f;
-  for (int k = lane; k < L; k += kWarp) {
-    const float gA = Gv(c.cb + k + 1);   // V[k] * frac lands at col cb + k + 1
-    const float gB = Gv(c.cb + k + 2);   // V[k] * (1 - frac) at col cb + k + 2
-    const float dV = gA * f + gB * f1;
-    const float dG = gA - gB;
-    if (c.has_n) {
-      const float t0 = __ldg(tab.w0 + (size_t)c.n_off * L + k);
-      acc_ne += dV * t0;
-      acc_fr += (t0 * c.ne) * dG;
-    }
-    if (c.umask) {
+__device__ __forceinline__ void neigh_load(const LsimParams &p, const Tables &tab, int rowidx, float v[kChunks],
+                                           int lane) {
+  const int L = p.signal_length;
+  const float *src = tab.w0 + (size_t)(rowidx < 0 ? 0 : rowidx) * L;
 #pragma unroll
-      for (int u = 0; u < kMainSub; ++u) {
-        if (!((c.umask >> u) & 1u)) continue;
+  for (int m = 0; m < kChunks; ++m) {
+    const int k = m * kWarp + lane - 1;
+    v[m] = (rowidx >= 0 && k >= 0 && k < L) ? __ldg(src + k) : 0.f;
+  }
+}
+
+__device__ __forceinline__ void scale(float v[kChunks], float a) {
 #pragma unroll
-        for (int v = 0; v < kMainSub; ++v) {
-          if (!((c.vmask >> v) & 1u)) continue;
-          const float4 t = __ldg(tab.wmp + ((size_t)(c.tidx * kMainSub + u) * kMainSub + v) * L + k);
-          const float B = (t.y * c.qb + t.x * c.qa) + t.z * c.qc;
-          const float W = c.Xw[u] * c.Yw[v];
-          const float dW = c.dXw[u] * c.Yw[v] + c.Xw[u] * c.dYw[v];
-          const float dVB = dV * B;
-          acc_ne += W * dVB;
-          acc_sig += dW * dVB;
-          const float dVW = dV * W;
-          acc_a += dVW * t.x;
-          acc_b += dVW * t.y;
-          acc_c += dVW * t.z;
-          acc_frm += (W * B) * dG;
-        }
+  for (int m = 0; m < kChunks; ++m) v[m] *= a;
+}
+
+// Forward: all neighbour parts of the pixel, four contributions in flight.
+__device__ __forceinline__ void neigh_forward(const LsimParams &p, const Tables &tab, const Workspace &w,
+                                              const ListSmem &ls, NBatch &nb, float *row, int lane) {
+  const int n_total = ls.pre_n[ls.n];
+  for (int g0 = 0; g0 < n_total; g0 += kWarp) {
+    neigh_setup<false>(p, tab, w, ls, nb, g0, n_total, lane);
+    const int m = min(kWarp, n_total - g0);
+    for (int j = 0; j < m; j += 4) {
+      float v0[kChunks], v1[kChunks], v2[kChunks], v3[kChunks];
+      const int r0 = nb.row[j];
+      const int r1 = j + 1 < m ? nb.row[j + 1] : -1;
+      const int r2 = j + 2 < m ? nb.row[j + 2] : -1;
+      const int r3 = j + 3 < m ? nb.row[j + 3] : -1;
+      neigh_load(p, tab, r0, v0, lane);
+      neigh_load(p, tab, r1, v1, lane);
+      neigh_load(p, tab, r2, v2, lane);
+      neigh_load(p, tab, r3, v3, lane);
+      if (r0 >= 0) {
+        scale(v0, nb.ne[j]);
+        window_apply(p, v0, nb.cb[j], nb.frac[j], nb.D[j] * nb.ne[j], row, lane);
+        __syncwarp();
+      }
+      if (r1 >= 0) {
+        scale(v1, nb.ne[j + 1]);
+        window_apply(p, v1, nb.cb[j + 1], nb.frac[j + 1], nb.D[j + 1] * nb.ne[j + 1], row, lane);
+        __syncwarp();
+      }
+      if (r2 >= 0) {
+        scale(v2, nb.ne[j + 2]);
+        window_apply(p, v2, nb.cb[j + 2], nb.frac[j + 2], nb.D[j + 2] * nb.ne[j + 2], row, lane);
+        __syncwarp();
+      }
+      if (r3 >= 0) {
+        scale(v3, nb.ne[j + 3]);
+        window_apply(p, v3, nb.cb[j + 3], nb.frac[j + 3], nb.D[j + 3] * nb.ne[j + 3], row, lane);
+        __syncwarp();
       }
     }
   }
-  // boundary corrections (per contribution, counted once by lane 0)
-  if (lane == 0) {
-    const int cb = c.cb;
-    const float gc0 = Gc(cb), gc1 = Gc(cb + 1);
-    const float dcorr = gc0 * f + gc1 * f1;
-    const float dgc = gc0 - gc1;
+}
+
+struct Theta {
+  float v[LSIM_NPARAM];
+};
+
+// Adjoint: all neighbour parts, given the waveform cotangent grow[col].
+__device__ __forceinline__ void neigh_backward(const LsimParams &p, const Tables &tab, const Workspace &w,
+                                               const ListSmem &ls, NBatch &nb, const float *grow, Theta &th,
+                                               int lane) {
+  const int L = p.signal_length, NT = p.n_ticks;
+  const int n_total = ls.pre_n[ls.n];
+  const float inv_ts = 1.f / p.t_sampling;
+  for (int g0 = 0; g0 < n_total; g0 += kWarp) {
+    neigh_setup<true>(p, tab, w, ls, nb, g0, n_total, lane);
+    const int m = min(kWarp, n_total - g0);
+    for (int j = 0; j < m; ++j) {
+      const int rowidx = nb.row[j];
+      if (rowidx < 0) continue;
+      const int cb = nb.cb[j];
+      const float f = nb.frac[j], f1 = 1.f - f, ne = nb.ne[j];
+      float v[kChunks];
+      const float *src = tab.w0 + (size_t)rowidx * L;
+#pragma unroll
+      for (int c = 0; c < kChunks; ++c) {
+        const int k = c * kWarp + lane;
+        v[c] = k < L ? __ldg(src + k) : 0.f;
+      }
+      float acc_ne = 0.f, acc_fr = 0.f;
+      if (cb >= 1 && cb + L + 1 <= NT - 2) {
+        // interior window: every column in range; samples past L are zero
+#pragma unroll
+        for (int c = 0; c < kChunks; ++c) {
+          const int k = c * kWarp + lane;
+          const float gA = grow[cb + k + 1], gB = grow[cb + k + 2];
+          acc_ne += (gA * f + gB * f1) * v[c];
+          acc_fr += v[c] * (gA - gB);
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < kChunks; ++c) {
+          const int k = c * kWarp + lane;
+          if (k < L) {
+            const int ca = cb + k + 1, cbb = cb + k + 2;
+            const float gA = (ca >= 2 && ca <= NT - 1) ? grow[ca] : 0.f;
+            const float gB = (cbb >= 2 && cbb <= NT - 1) ? grow[cbb] : 0.f;
+            acc_ne += (gA * f + gB * f1) * v[c];
+            acc_fr += v[c] * (gA - gB);
+          }
+        }
+      }
+      if (lane == 0) {
+        const float gc0 = (cb >= 1 && cb <= NT - 2) ? grow[cb] : 0.f;
+        const float gc1 = (cb + 1 >= 1 && cb + 1 <= NT - 2) ? grow[cb + 1] : 0.f;
+        const float dcorr = gc0 * f + gc1 * f1;
+        acc_ne += dcorr * nb.D[j];
+        acc_fr += dcorr * nb.dl[j] + nb.D[j] * (gc0 - gc1);
+      }
+      const float dt = acc_fr * ne * inv_ts;
+      th.v[0] += acc_ne * nb.dne[0][j];
+      th.v[1] += acc_ne * nb.dne[1][j];
+      th.v[2] += acc_ne * nb.dne[2][j] + dt * nb.dt0[j];
+      th.v[3] += acc_ne * nb.dne[3][j];
+      th.v[7] += acc_ne * nb.dne[4][j];
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- main bins
+
+// The current main-bin contribution: its distinct LUT sub-positions (u, v),
+// compacted by one lane each, with weight W = Xw[u] Yw[v] (summed 1-D bin
+// integrals of the bins on the pixel), dW/dsigma_T, and the boundary terms.
+struct MainSmem {
+  int off[kMainSub * kMainSub];     // (tidx*5 + u)*5 + v
+  float W[kMainSub * kMainSub], dW[kMainSub * kMainSub];
+  float D[kMainSub * kMainSub], dl[kMainSub * kMainSub];
+};
+
+struct MainHead {
+  float ne, frac, qa, qb, qc, corr;
+  int cb, n;
+};
+
+template <bool GRAD>
+__device__ __forceinline__ bool main_setup(const LsimParams &p, const Tables &tab, const Workspace &w, int s, int dx,
+                                           int dy, MainHead &h, MainSmem &ms, int lane) {
+  const SegFwd &f = w.segf[s];
+  h.ne = f.ne;
+  if (h.ne == 0.f) return false;
+  const int nbp = p.nb_bins_per_pixel;
+  float ex[kMaxTran], ey[kMaxTran], dex[kMaxTran], dey[kMaxTran];
+#pragma unroll
+  for (int i = 0; i < kMaxTran; ++i) {
+    ex[i] = f.ex[i];
+    ey[i] = f.ey[i];
+    dex[i] = GRAD ? w.sega[s].dex[i] : 0.f;
+    dey[i] = GRAD ? w.sega[s].dey[i] : 0.f;
+  }
+  float Xw[kMainSub], Yw[kMainSub], dXw[kMainSub], dYw[kMainSub];
+  unsigned um, vm;
+  axis_weights(ex, dex, f.bx, nbp, dx, Xw, dXw, &um);
+  axis_weights(ey, dey, f.by, nbp, dy, Yw, dYw, &vm);
+  if (!um || !vm) return false;
+  h.frac = f.frac; h.qa = f.qa; h.qb = f.qb; h.qc = f.qc;
+  const int cath = f.cath, tidx = f.tidx;
+  h.cb = p.lut_nt - p.signal_length - cath - 1;
+  // lane l < 25 owns sub-position (u, v) = (l / 5, l % 5)
+  const int u = lane / kMainSub, v = lane % kMainSub;
+  const bool mine = lane < kMainSub * kMainSub && ((um >> u) & 1u) && ((vm >> v) & 1u);
+  float xw = 0.f, yw = 0.f, dxw = 0.f, dyw = 0.f;
+#pragma unroll
+  for (int q = 0; q < kMainSub; ++q) {
+    if (q == u) { xw = Xw[q]; dxw = dXw[q]; }
+    if (q == v) { yw = Yw[q]; dyw = dYw[q]; }
+  }
+  const unsigned bal = __ballot_sync(0xffffffffu, mine);
+  float wd = 0.f;
+  if (mine) {
+    const int pos = __popc(bal & ((1u << lane) - 1u));
+    const int off = (tidx * kMainSub + u) * kMainSub + v;
     float dl;
-    if (c.has_n) {
-      const float Dn = cum_terms(tab.c0 + (size_t)c.n_off * Nt, c.cath, Nt, L, f, &dl);
-      acc_ne += dcorr * Dn;
-      acc_fr += (dcorr * dl + Dn * dgc) * c.ne;
-    }
-    if (c.umask) {
+    const float D = cum_terms(tab.cm + (size_t)off * p.lut_nt, cath, p.lut_nt, p.signal_length, h.frac, &dl);
+    ms.off[pos] = off;
+    ms.W[pos] = xw * yw;
+    ms.dW[pos] = dxw * yw + xw * dyw;
+    ms.D[pos] = D;
+    ms.dl[pos] = dl;
+    wd = (xw * yw) * D;
+  }
+  h.corr = warp_sum(wd) * h.ne;
+  h.n = __popc(bal);
+  __syncwarp();
+  return true;
+}
+
+__device__ __forceinline__ void main_forward_one(const LsimParams &p, const Tables &tab, const MainHead &h,
+                                                 const MainSmem &ms, float *row, int lane) {
+  const int L = p.signal_length;
+  float acc[kChunks];
 #pragma unroll
-      for (int u = 0; u < kMainSub; ++u) {
-        if (!((c.umask >> u) & 1u)) continue;
+  for (int m = 0; m < kChunks; ++m) acc[m] = 0.f;
+  for (int e = 0; e < h.n; ++e) {
+    const float4 *src = tab.wmp + (size_t)ms.off[e] * L;
+    const float W = ms.W[e];
 #pragma unroll
-        for (int v = 0; v < kMainSub; ++v) {
-          if (!((c.vmask >> v) & 1u)) continue;
-          const float *row = tab.cm + ((size_t)(c.tidx * kMainSub + u) * kMainSub + v) * Nt;
-          const float D = cum_terms(row, c.cath, Nt, L, f, &dl);
-          const float W = c.Xw[u] * c.Yw[v];
-          const float dW = c.dXw[u] * c.Yw[v] + c.Xw[u] * c.dYw[v];
-          acc_ne += dcorr * W * D;
-          acc_sig += dcorr * dW * D;
-          acc_frm += W * (dcorr * dl + D * dgc);
-        }
+    for (int m = 0; m < kChunks; ++m) {
+      const int k = m * kWarp + lane - 1;
+      if (k >= 0 && k < L) {
+        const float4 t = __ldg(src + k);
+        acc[m] += W * ((t.y * h.qb + t.x * h.qa) + t.z * h.qc);
       }
     }
   }
-  const float ne = c.ne;
+  scale(acc, h.ne);
+  window_apply(p, acc, h.cb, h.frac, h.corr, row, lane);
+  __syncwarp();
+}
+
+__device__ __forceinline__ void main_backward_one(const LsimParams &p, const Tables &tab, const MainHead &h,
+                                                  const MainSmem &ms, const SegAdj &a, const float *grow, Theta &th,
+                                                  int lane) {
+  const int L = p.signal_length, NT = p.n_ticks;
+  const float f = h.frac, f1 = 1.f - h.frac;
+  const int cb = h.cb;
+  float dV[kChunks], dG[kChunks];
+#pragma unroll
+  for (int m = 0; m < kChunks; ++m) {
+    const int k = m * kWarp + lane;
+    const int ca = cb + k + 1, cbb = cb + k + 2;
+    const float gA = (k < L && ca >= 2 && ca <= NT - 1) ? grow[ca] : 0.f;
+    const float gB = (k < L && cbb >= 2 && cbb <= NT - 1) ? grow[cbb] : 0.f;
+    dV[m] = gA * f + gB * f1;
+    dG[m] = gA - gB;
+  }
+  float acc_ne = 0.f, acc_sig = 0.f, acc_a = 0.f, acc_b = 0.f, acc_c = 0.f, acc_fr = 0.f;
+  for (int e = 0; e < h.n; ++e) {
+    const float4 *src = tab.wmp + (size_t)ms.off[e] * L;
+    const float W = ms.W[e], dW = ms.dW[e];
+#pragma unroll
+    for (int m = 0; m < kChunks; ++m) {
+      const int k = m * kWarp + lane;
+      if (k < L) {
+        const float4 t = __ldg(src + k);
+        const float B = (t.y * h.qb + t.x * h.qa) + t.z * h.qc;
+        const float dVB = dV[m] * B;
+        acc_ne += W * dVB;
+        acc_sig += dW * dVB;
+        const float dVW = dV[m] * W;
+        acc_a += dVW * t.x;
+        acc_b += dVW * t.y;
+        acc_c += dVW * t.z;
+        acc_fr += (W * B) * dG[m];
+      }
+    }
+  }
+  // boundary corrections: lane e owns sub-position entry e
+  if (lane < h.n) {
+    const float gc0 = (cb >= 1 && cb <= NT - 2) ? grow[cb] : 0.f;
+    const float gc1 = (cb + 1 >= 1 && cb + 1 <= NT - 2) ? grow[cb + 1] : 0.f;
+    const float dcorr = gc0 * f + gc1 * f1;
+    const float W = ms.W[lane], D = ms.D[lane];
+    acc_ne += dcorr * W * D;
+    acc_sig += dcorr * ms.dW[lane] * D;
+    acc_fr += W * (dcorr * ms.dl[lane] + D * (gc0 - gc1));
+  }
+  // q_uv = ne * W: all terms but acc_ne carry a factor ne
+  const float ne = h.ne;
   const float sig = acc_sig * ne;
   const float lsum = (acc_a * a.dqa + acc_b * a.dqb + acc_c * a.dqc) * ne;
-  const float dt0 = (acc_fr + acc_frm * ne) / p.t_sampling;
+  const float dt = acc_fr * ne / p.t_sampling;
   th.v[0] += acc_ne * a.dne[0];
   th.v[1] += acc_ne * a.dne[1];
-  th.v[2] += acc_ne * a.dne[2] + sig * a.dsig[0] + lsum * a.dld[0] + dt0 * a.dt0;
+  th.v[2] += acc_ne * a.dne[2] + sig * a.dsig[0] + lsum * a.dld[0] + dt * a.dt0;
   th.v[3] += acc_ne * a.dne[3];
   th.v[5] += lsum * a.dld[1];
   th.v[6] += sig * a.dsig[1];
   th.v[7] += acc_ne * a.dne[4];
+  __syncwarp();
 }
 
-// Build the neighbourhood slot list of a pixel (compacted, fixed order).
+// Per-warp shared memory.  Warps index an array of these and access the
+// row with float4, so the size must keep every element 16-byte aligned.
+template <bool GRAD>
+struct __align__(16) WarpSmem {
+  float buf[kRowFloats];
+  ListSmem list;
+  NBatch nb;
+  MainSmem ms;
+};
+template <>
+struct __align__(16) WarpSmem<true> {
+  float buf[kRowFloats];
+  ListSmem list;
+  NBatch nb;
+  MainSmem ms;
+  float gint[LSIM_MAX_HITS];
+  FeeState fee;
+};
+static_assert(sizeof(WarpSmem<false>) % 16 == 0, "per-warp shared memory must keep 16-byte alignment");
+static_assert(sizeof(WarpSmem<true>) % 16 == 0, "per-warp shared memory must keep 16-byte alignment");
+static_assert(offsetof(WarpSmem<false>, buf) == 0 && offsetof(WarpSmem<true>, buf) == 0, "row first");
+static_assert((kRowPad + 1) % 4 == 0 && kRowFloats % 4 == 0, "output column 1 of the row must be 16-byte aligned");
+
+// Walk the segments of the 3x3 slots; run fn on those with bins on the pixel.
+template <typename F>
+__device__ __forceinline__ void for_each_main(const Workspace &w, const ListSmem &ls, int lane, F &&fn) {
+  for (int e = 0; e < ls.n; ++e) {
+    const int dxy = ls.dxy[e];
+    const int dx = (dxy & 0xff) - 16, dy = ((dxy >> 8) & 0xff) - 16;
+    if (dx < -1 || dx > 1 || dy < -1 || dy > 1) continue;
+    const int o = ls.off[e], c = ls.cnt[e];
+    for (int j0 = 0; j0 < c; j0 += kWarp) {
+      const int mine = (j0 + lane < c) ? __ldg(w.seg_list + o + j0 + lane) : -1;
+      const int m = min(kWarp, c - j0);
+      for (int jj = 0; jj < m; ++jj) fn(__shfl_sync(0xffffffffu, mine, jj), dx, dy);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- per pixel
+
+// Neighbourhood slot list of a pixel (compacted, fixed order) with the
+// prefix count of neighbour contributions.
 __device__ __forceinline__ void build_list(const Grid &g, const int32_t *__restrict__ cnt,
                                            const int32_t *__restrict__ off, int64_t slot, ListSmem &ls, int lane) {
   const int D = 2 * g.n + 1;
-  int base = 0;
+  int base = 0, nbase = 0;
   for (int i0 = 0; i0 < D * D; i0 += kWarp) {
     const int idx = i0 + lane;
     int c = 0, o = 0, dxy = 0;
+    bool centre = false;
     if (idx < D * D) {
       const int dx = idx / D - g.n, dy = idx % D - g.n;
       const int64_t q = slot - (int64_t)dy * g.nxe - dx;
       c = __ldg(cnt + q);
       if (c > 0) o = __ldg(off + q);
       dxy = (dx + 16) | ((dy + 16) << 8);
+      centre = (dx == 0 && dy == 0);
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, c > 0);
-    if (c > 0) {
+    const bool has = c > 0;
+    const unsigned bal = __ballot_sync(0xffffffffu, has);
+    const int nc = (has && !centre) ? c : 0;
+    int incl = nc;   // inclusive scan of neighbour counts over the compacted entries
+    for (int o2 = 1; o2 < kWarp; o2 <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o2);
+      if (lane >= o2) incl += y;
+    }
+    if (has) {
       const int pos = base + __popc(bal & ((1u << lane) - 1u));
-      ls.off[pos] = o; ls.cnt[pos] = c; ls.dxy[pos] = dxy;
+      ls.off[pos] = o;
+      ls.cnt[pos] = c;
+      ls.dxy[pos] = dxy;
+      ls.pre_n[pos] = nbase + incl - nc;
     }
     base += __popc(bal);
+    nbase += __shfl_sync(0xffffffffu, incl, kWarp - 1);
   }
-  if (lane == 0) ls.n = base;
+  if (lane == 0) {
+    ls.n = base;
+    ls.pre_n[base] = nbase;
+  }
   __syncwarp();
-}
-
-template <typename F>
-__device__ __forceinline__ void for_each_contribution(const int32_t *__restrict__ seg_list, const ListSmem &ls,
-                                                      int lane, F &&fn) {
-  for (int e = 0; e < ls.n; ++e) {
-    const int o = ls.off[e], c = ls.cnt[e], dxy = ls.dxy[e];
-    const int dx = (dxy & 0xff) - 16, dy = ((dxy >> 8) & 0xff) - 16;
-    for (int j0 = 0; j0 < c; j0 += kWarp) {
-      const int mine = (j0 + lane < c) ? __ldg(seg_list + o + j0 + lane) : -1;
-      const int m = min(kWarp, c - j0);
-      for (int jj = 0; jj < m; ++jj) {
-        const int s = __shfl_sync(0xffffffffu, mine, jj);
-        fn(s, dx, dy);
-      }
-    }
-  }
 }
 
 __device__ __forceinline__ int32_t slot_pid(const LsimParams &p, const Grid &g, int64_t slot) {
@@ -356,7 +555,7 @@ __device__ __forceinline__ int32_t slot_pid(const LsimParams &p, const Grid &g, 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kAccWarps * kWarp) k_lut_pixels(AccumArgs a) {
+__global__ void __launch_bounds__(kAccWarps * kWarp, 3) k_lut_pixels(AccumArgs a) {
   constexpr bool GRAD = (MODE == kModeGrad);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x % kWarp, wid = threadIdx.x / kWarp;
@@ -367,24 +566,21 @@ __global__ void __launch_bounds__(kAccWarps * kWarp) k_lut_pixels(AccumArgs a) {
   const int T = NT - 1;
   const int H = p.max_adc_values;
   const int n_valid = a.w.counts->n_valid;
-  Theta th;
-#pragma unroll
-  for (int i = 0; i < LSIM_NPARAM; ++i) th.v[i] = 0.f;
-  th.loss = 0.f;
+  const bool early_exit = (a.normals == nullptr) && p.threshold > 0.f;
   for (;;) {
     int r = 0;
     if (lane == 0) r = atomicAdd(&a.w.counts->work, 1);
     r = __shfl_sync(0xffffffffu, r, 0);
     if (r >= n_valid) break;
     const int64_t slot = a.w.pix_slot[r];
-    // zero the row
     float4 *b4 = reinterpret_cast<float4 *>(sm.buf);
     for (int i = lane; i < kRowFloats / 4; i += kWarp) b4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     build_list(a.g, a.w.cnt, a.w.off, slot, sm.list, lane);
-    __syncwarp();
-    for_each_contribution(a.w.seg_list, sm.list, lane, [&](int s, int dx, int dy) {
-      Contribution c;
-      if (setup_contribution(p, a.w.segf, a.w.sega, s, dx, dy, false, c)) add_window(p, a.tab, c, row, lane);
+    // ---- forward: neighbour parts, then main-bin parts
+    neigh_forward(p, a.tab, a.w, sm.list, sm.nb, row, lane);
+    for_each_main(a.w, sm.list, lane, [&](int s, int dx, int dy) {
+      MainHead h;
+      if (main_setup<false>(p, a.tab, a.w, s, dx, dy, h, sm.ms, lane)) main_forward_one(p, a.tab, h, sm.ms, row, lane);
     });
     __syncwarp();
     if (MODE == kModeWfs) {
@@ -399,20 +595,19 @@ __global__ void __launch_bounds__(kAccWarps * kWarp) k_lut_pixels(AccumArgs a) {
     float *tick_dst = a.tick_out ? a.tick_out + (int64_t)r * H : nullptr;
     warp_cumsum_charge(row + 1, T, p.t_sampling, lane);
     if (MODE == kModeAdc) {
-      fee_forward(p, row + 1, T, nrm, adc_dst, tick_dst, nullptr, nullptr, lane);
+      fee_forward(p, row + 1, T, nrm, adc_dst, tick_dst, nullptr, nullptr, early_exit, lane);
       continue;
     }
     if constexpr (GRAD) {
-      fee_forward(p, row + 1, T, nrm, adc_dst, tick_dst, &sm.fee, nullptr, lane);
-      // cotangent of the integrated charges
+      fee_forward(p, row + 1, T, nrm, adc_dst, tick_dst, &sm.fee, nullptr, early_exit, lane);
+      float loss = 0.f;
       if (lane == 0) {
-        int32_t pid = -2;
         int64_t tr = -1;
         if (!a.g_adc) {
-          pid = slot_pid(p, a.g, slot);
+          const int32_t pid = slot_pid(p, a.g, slot);
           int64_t lo = 0, hi = a.n_tgt;
           while (lo < hi) {
-            int64_t mid = (lo + hi) >> 1;
+            const int64_t mid = (lo + hi) >> 1;
             if (a.tgt_pids[mid] < pid) lo = mid + 1; else hi = mid;
           }
           if (lo < a.n_tgt && a.tgt_pids[lo] == pid) tr = lo;
@@ -427,94 +622,119 @@ __global__ void __launch_bounds__(kAccWarps * kWarp) k_lut_pixels(AccumArgs a) {
           } else {
             const float tgt = tr >= 0 ? a.tgt_adc[tr * H + h] : adc0;
             const float d = adc - tgt;
-            th.loss += d * d;
+            loss += d * d;
             g = 2.f * d;
           }
           sm.gint[h] = digitize_vjp(p, raw, g);
         }
       }
       __syncwarp();
-      // dL/dW over output ticks, in place (row + 1), column 0 and tail zeroed
       fee_backward(p, row + 1, T, &sm.fee, sm.gint, lane);
       if (lane == 0) row[0] = 0.f;
       __syncwarp();
-      for_each_contribution(a.w.seg_list, sm.list, lane, [&](int s, int dx, int dy) {
-        Contribution c;
-        if (setup_contribution(p, a.w.segf, a.w.sega, s, dx, dy, true, c)) {
-          const SegAdj &adj = a.w.sega[s];
-          window_vjp(p, a.tab, c, adj, row, th, lane);
-        }
+      Theta th;
+#pragma unroll
+      for (int i = 0; i < LSIM_NPARAM; ++i) th.v[i] = 0.f;
+      neigh_backward(p, a.tab, a.w, sm.list, sm.nb, row, th, lane);
+      for_each_main(a.w, sm.list, lane, [&](int s, int dx, int dy) {
+        MainHead h;
+        if (main_setup<true>(p, a.tab, a.w, s, dx, dy, h, sm.ms, lane))
+          main_backward_one(p, a.tab, h, sm.ms, a.w.sega[s], row, th, lane);
       });
+      // per-pixel record [loss, dL/dtheta]
+#pragma unroll
+      for (int i = 0; i < LSIM_NPARAM; ++i) th.v[i] = warp_sum(th.v[i]);
+      if (lane == 0) {
+        float *dst = a.w.pix_out + (size_t)r * kPixRec;
+        dst[0] = loss;
+#pragma unroll
+        for (int i = 0; i < LSIM_NPARAM; ++i) dst[1 + i] = th.v[i];
+      }
       __syncwarp();
     }
   }
-  if constexpr (GRAD) {
-    const int gw = blockIdx.x * kAccWarps + wid;
-    for (int i = 0; i < LSIM_NPARAM; ++i) th.v[i] = warp_sum(th.v[i]);
-    th.loss = warp_sum(th.loss);
-    if (lane == 0) {
-      float *dst = a.w.grad_partials + (size_t)gw * kGradSlots;
-      dst[0] = th.loss;
-      for (int i = 0; i < LSIM_NPARAM; ++i) dst[1 + i] = th.v[i];
+}
+
+// ---------------------------------------------------------------- reductions
+
+constexpr int kRedThreads = 256;
+constexpr int kPixBlocks = 1024;     // reduction blocks over pixel records
+constexpr int kTgtBlocks = 256;      // reduction blocks over target-only rows
+
+// Fixed-order float64 sum of the per-pixel records: block b reduces a
+// contiguous chunk; the chunking depends only on n_valid.
+__global__ void k_reduce_pixels(const float *__restrict__ pix, const LsimCounts *counts, double *partials) {
+  __shared__ double sh[kRedThreads];
+  const int n = counts->n_valid;
+  const int64_t chunk = ((int64_t)n + gridDim.x - 1) / gridDim.x;
+  const int64_t lo = blockIdx.x * chunk, hi = min((int64_t)n, lo + chunk);
+  for (int q = 0; q <= LSIM_NPARAM; ++q) {
+    double s = 0.0;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) s += (double)pix[i * kPixRec + q];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = kRedThreads / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
     }
+    if (threadIdx.x == 0) partials[(size_t)blockIdx.x * 16 + q] = sh[0];
+    __syncthreads();
   }
 }
 
 // Loss terms of target pixels that the prediction does not have.
-__global__ void k_target_only(AccumArgs a, float *partials) {
-  __shared__ float sh[256 / kWarp];
+__global__ void k_target_only(AccumArgs a, double *partials) {
+  __shared__ double sh[kRedThreads];
   const LsimParams &p = a.p;
   const int H = p.max_adc_values;
   const float adc0 = digitize(p, 0.f);
   const int n_valid = a.w.counts->n_valid;
-  float acc = 0.f;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < a.n_tgt; t += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t chunk = (a.n_tgt + gridDim.x - 1) / gridDim.x;
+  const int64_t lo = blockIdx.x * chunk, hi = min(a.n_tgt, lo + chunk);
+  double acc = 0.0;
+  for (int64_t t = lo + threadIdx.x; t < hi; t += kRedThreads) {
     const int32_t pid = a.tgt_pids[t];
-    int lo = 0, hi = n_valid;
-    while (lo < hi) {
-      int mid = (lo + hi) >> 1;
-      if (slot_pid(p, a.g, a.w.pix_slot[mid]) < pid) lo = mid + 1; else hi = mid;
+    int l = 0, h2 = n_valid;
+    while (l < h2) {
+      const int mid = (l + h2) >> 1;
+      if (slot_pid(p, a.g, a.w.pix_slot[mid]) < pid) l = mid + 1; else h2 = mid;
     }
-    const bool present = lo < n_valid && slot_pid(p, a.g, a.w.pix_slot[lo]) == pid;
+    const bool present = l < n_valid && slot_pid(p, a.g, a.w.pix_slot[l]) == pid;
     if (!present && pid >= 0)
       for (int h = 0; h < H; ++h) {
         const float d = adc0 - a.tgt_adc[t * H + h];
-        acc += d * d;
+        acc += (double)(d * d);
       }
   }
-  acc = warp_sum(acc);
-  if (threadIdx.x % kWarp == 0) sh[threadIdx.x / kWarp] = acc;
+  sh[threadIdx.x] = acc;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    float s = 0.f;
-    for (int i = 0; i < 256 / kWarp; ++i) s += sh[i];
-    partials[blockIdx.x] = s;
+  for (int o = kRedThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) partials[(size_t)blockIdx.x * 16] = sh[0];
 }
 
-__global__ void k_grad_finalize(const float *grad_partials, int n_warps, const float *tgt_partials, int n_tgt_blocks,
-                                float *loss_out, float *grad_out) {
-  const int i = threadIdx.x;   // 0: loss, 1..8: grads
-  if (i > LSIM_NPARAM) return;
-  float s = 0.f;
-  for (int w = 0; w < n_warps; ++w) s += grad_partials[(size_t)w * kGradSlots + i];
-  if (i == 0) {
-    for (int b = 0; b < n_tgt_blocks; ++b) s += tgt_partials[b];
-    if (loss_out) loss_out[0] = s;
+__global__ void k_grad_finalize(const double *pix_partials, int n_pix_blocks, const double *tgt_partials,
+                                int n_tgt_blocks, float *loss_out, float *grad_out) {
+  const int q = threadIdx.x;   // 0: loss, 1..8: gradient
+  if (q > LSIM_NPARAM) return;
+  double s = 0.0;
+  for (int b = 0; b < n_pix_blocks; ++b) s += pix_partials[(size_t)b * 16 + q];
+  if (q == 0) {
+    for (int b = 0; b < n_tgt_blocks; ++b) s += tgt_partials[(size_t)b * 16];
+    if (loss_out) loss_out[0] = (float)s;
   } else if (grad_out) {
-    grad_out[i - 1] = s;
+    grad_out[q - 1] = (float)s;
   }
 }
 
 // ---------------------------------------------------------------- launch
 
-// Persistent grid: every SM filled to its occupancy limit, capped so the
-// per-warp gradient partials fit their buffer.  A pure function of the
-// device and the mode, so it is the same at launch and at finalisation.
+// Persistent grid: every SM filled to its occupancy limit.
 template <int MODE>
-static int grid_blocks(int *blocks) {
-  constexpr bool GRAD = (MODE == kModeGrad);
-  const size_t smem = sizeof(WarpSmem<GRAD>) * kAccWarps;
+static int grid_blocks(int *blocks, size_t *smem_out) {
+  const size_t smem = sizeof(WarpSmem<MODE == kModeGrad>) * kAccWarps;
   if (cudaFuncSetAttribute(k_lut_pixels<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return LSIM_ERR_CUDA;
@@ -523,20 +743,17 @@ static int grid_blocks(int *blocks) {
       cudaSuccess)
     return LSIM_ERR_CUDA;
   if (per_sm < 1) per_sm = 1;
-  int b = device_sm_count() * per_sm;
-  const int max_blocks = kGradBlocks / kAccWarps;
-  *blocks = b > max_blocks ? max_blocks : b;
+  *blocks = device_sm_count() * per_sm;
+  *smem_out = smem;
   return LSIM_OK;
 }
 
 template <int MODE>
 static int launch_mode(const AccumArgs &a, cudaStream_t st) {
-  constexpr bool GRAD = (MODE == kModeGrad);
-  const size_t smem = sizeof(WarpSmem<GRAD>) * kAccWarps;
   int blocks = 0;
-  int rc = grid_blocks<MODE>(&blocks);
+  size_t smem = 0;
+  int rc = grid_blocks<MODE>(&blocks, &smem);
   if (rc != LSIM_OK) return rc;
-  // reset the work counter
   if (cudaMemsetAsync(&a.w.counts->work, 0, sizeof(int32_t), st) != cudaSuccess) return LSIM_ERR_CUDA;
   k_lut_pixels<MODE><<<blocks, kAccWarps * kWarp, smem, st>>>(a);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
@@ -544,7 +761,12 @@ static int launch_mode(const AccumArgs &a, cudaStream_t st) {
 
 int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st) {
   if (a.p.n_neighbors > 4 || a.p.n_tran_bins != kMaxTran || a.p.nb_bins_per_pixel != 2 * kMainSub ||
-      a.p.n_ticks - 1 + kRowPad > kRowFloats || (a.p.n_ticks - 1) % 4 != 0 || a.p.max_adc_values > LSIM_MAX_HITS)
+      a.p.n_ticks - 1 + kRowPad > kRowFloats || (a.p.n_ticks - 1) % 4 != 0 || a.p.max_adc_values > LSIM_MAX_HITS ||
+      a.p.signal_length + 2 > kChunks * kWarp || a.p.signal_length > a.p.lut_nt)
+    return LSIM_ERR_UNSUPPORTED;
+  // neighbour LUT indices reach nb*n + nb/2 - 1 (sim_jax.py:443)
+  const int need = a.p.nb_bins_per_pixel * a.p.n_neighbors + a.p.nb_bins_per_pixel / 2;
+  if (a.p.lut_nx < need || a.p.lut_ny < need || a.p.lut_nx < kMainSub || a.p.lut_ny < kMainSub)
     return LSIM_ERR_UNSUPPORTED;
   switch (mode) {
     case kModeWfs: return launch_mode<kModeWfs>(a, st);
@@ -555,18 +777,15 @@ int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st) {
 }
 
 int run_grad_finalize(const AccumArgs &a, float *loss_out, float *grad_out, cudaStream_t st) {
-  int blocks = 0;
-  int rc = grid_blocks<kModeGrad>(&blocks);
-  if (rc != LSIM_OK) return rc;
-  const int n_warps = blocks * kAccWarps;
-  // target-only partials reuse the tail of the grad-partials buffer
-  float *tgt_partials = a.w.grad_partials + (size_t)n_warps * kGradSlots;
+  double *pix_partials = a.w.red_partials;
+  double *tgt_partials = a.w.red_partials + (size_t)kPixBlocks * 16;
+  k_reduce_pixels<<<kPixBlocks, kRedThreads, 0, st>>>(a.w.pix_out, a.w.counts, pix_partials);
   int tb = 0;
   if (!a.g_adc && a.n_tgt > 0) {
-    tb = 64;
-    k_target_only<<<tb, 256, 0, st>>>(a, tgt_partials);
+    tb = kTgtBlocks;
+    k_target_only<<<tb, kRedThreads, 0, st>>>(a, tgt_partials);
   }
-  k_grad_finalize<<<1, 32, 0, st>>>(a.w.grad_partials, n_warps, tgt_partials, tb, loss_out, grad_out);
+  k_grad_finalize<<<1, 32, 0, st>>>(pix_partials, kPixBlocks, tgt_partials, tb, loss_out, grad_out);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 

@@ -18,7 +18,6 @@ constexpr int kMaxTran = 5;              // nb_tran_diff_bins supported: 5
 constexpr int kMainSub = 5;              // main-bin LUT sub-positions (nb_bins_per_pixel / 2)
 constexpr int kScanTile = 2048;          // slots per scan block
 constexpr int kScanThreads = 256;
-constexpr int kGradSlots = 16;           // floats per grad partial record (loss + 8 grads + pad)
 
 // --------------------------------------------------------------- records
 
@@ -90,11 +89,13 @@ struct Workspace {
   int32_t *cnt, *off, *cursor;
   int32_t *seg_list, *pix_slot, *em1_slot;
   int32_t *scan_blocks;     // 3 ints per scan block (+1 block)
-  float *grad_partials;     // kGradBlocks * kGradSlots
+  float *pix_out;           // per valid pixel: [loss, 8 gradient terms] (kPixRec floats)
+  double *red_partials;     // fixed-order reduction partials (kRedSlots * 16 doubles)
   size_t bytes;
 };
 
-constexpr int kGradBlocks = 8192;   // max persistent warps with a gradient partial
+constexpr int kPixRec = 12;      // floats per per-pixel record (loss + 8 grads, padded)
+constexpr int kRedSlots = 2048;  // reduction blocks (pixels + target-only)
 
 inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows, int32_t n_events) {
   Grid g = make_grid(p, n_events);
@@ -111,10 +112,11 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   size_t o_off = take(4 * (size_t)g.G);
   size_t o_cur = take(4 * (size_t)g.G);
   size_t o_list = take(4 * (size_t)n_rows);
-  size_t o_pix = take(4 * (size_t)n_rows);
+  size_t o_pixs = take(4 * (size_t)n_rows);
   size_t o_em1 = take(4 * (size_t)n_rows);
   size_t o_scan = take(3 * 4 * (size_t)nscan);
-  size_t o_grad = take(4 * (size_t)(kGradBlocks + 64) * kGradSlots);
+  size_t o_pix = take(4 * (size_t)kPixRec * (size_t)n_rows);
+  size_t o_red = take(8 * (size_t)kRedSlots * 16);
   Workspace w;
   char *b = (char *)base;
   w.counts = (LsimCounts *)(b + o_counts);
@@ -127,10 +129,11 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   w.off = (int32_t *)(b + o_off);
   w.cursor = (int32_t *)(b + o_cur);
   w.seg_list = (int32_t *)(b + o_list);
-  w.pix_slot = (int32_t *)(b + o_pix);
+  w.pix_slot = (int32_t *)(b + o_pixs);
   w.em1_slot = (int32_t *)(b + o_em1);
   w.scan_blocks = (int32_t *)(b + o_scan);
-  w.grad_partials = (float *)(b + o_grad);
+  w.pix_out = (float *)(b + o_pix);
+  w.red_partials = (double *)(b + o_red);
   w.bytes = off;
   return w;
 }

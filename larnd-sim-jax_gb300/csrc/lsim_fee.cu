@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(kFeeWarps * kWarp)
     warp_cumsum_charge(C, T, p.t_sampling, lane);
     const float *nrm = normals ? normals + r * (1 + 3 * H) : nullptr;
     fee_forward(p, C, T, nrm, adc_out + r * H, tick_out + r * H, nullptr,
-                integral_out ? integral_out + r * H : nullptr, lane);
+                integral_out ? integral_out + r * H : nullptr, normals == nullptr && p.threshold > 0.f, lane);
     __syncwarp();
   }
 }

@@ -17,6 +17,7 @@ namespace lsim {
 constexpr int kMaskWords = 64;   // bits per hit for T <= 2048
 
 struct FeeState {
+  int n_done;                  // hits evaluated before the early exit (the rest are empty)
   int e[LSIM_MAX_HITS];        // integration end index
   int e2[LSIM_MAX_HITS];       // reset index
   int cond[LSIM_MAX_HITS];     // 1 = rejected (adc forced to 0)
@@ -71,9 +72,14 @@ __device__ __forceinline__ void warp_cumsum_charge(float *X, int T, float ts, in
 // Forward self-trigger on C (in place).  normals: per-pixel standard
 // normals [1 + 3H] or null (noise off).  Writes adc (digitized) and tick
 // per hit through lane 0; fills st when non-null.
+//
+// early_exit (noise off, threshold > 0): once a rejected hit leaves C all
+// zero, every later hit is provably empty (no crossing of a positive
+// threshold, C[e] = 0, reset by 0 keeps C zero), so the remaining hits are
+// written as empty without sweeping the row again.
 __device__ __forceinline__ void fee_forward(const LsimParams &p, float *C, int T, const float *normals,
                                             float *adc_out, float *tick_out, FeeState *st, float *raw_out,
-                                            int lane) {
+                                            bool early_exit, int lane) {
   const float thr = p.threshold;
   const int H = p.max_adc_values;
   float base = normals ? normals[0] * p.reset_noise : 0.f;
@@ -105,6 +111,7 @@ __device__ __forceinline__ void fee_forward(const LsimParams &p, float *C, int T
     if (e2 >= T) e2 = T - 1;
     const float R = C[e2];
     __syncwarp();
+    bool nz = false;
     for (int m = 0; m < nwords; ++m) {
       int i = m * kWarp + lane;
       bool keep = true;
@@ -112,6 +119,7 @@ __device__ __forceinline__ void fee_forward(const LsimParams &p, float *C, int T
         float c = C[i] - R;
         keep = !(c < 0.f);
         C[i] = keep ? c : 0.f;
+        nz |= keep && c != 0.f;
       }
       if (st) {
         unsigned bal = __ballot_sync(0xffffffffu, keep);
@@ -125,7 +133,22 @@ __device__ __forceinline__ void fee_forward(const LsimParams &p, float *C, int T
       if (raw_out) raw_out[h] = adc;
       if (st) { st->e[h] = e; st->e2[h] = e2; st->cond[h] = cond ? 1 : 0; st->raw[h] = adc; }
     }
+    if (early_exit && cond && !__any_sync(0xffffffffu, nz)) {
+      if (lane == 0) {
+        const float a0 = digitize(p, 0.f);
+        for (int k = h + 1; k < H; ++k) {
+          if (adc_out) adc_out[k] = a0;
+          if (tick_out) tick_out[k] = (float)(T - 2);
+          if (raw_out) raw_out[k] = 0.f;
+          if (st) { st->e[k] = T - 1; st->e2[k] = T - 1; st->cond[k] = 1; st->raw[k] = 0.f; }
+        }
+        if (st) st->n_done = h + 1;
+      }
+      __syncwarp();
+      return;
+    }
   }
+  if (st && lane == 0) st->n_done = H;
   __syncwarp();
 }
 
@@ -137,7 +160,16 @@ __device__ __forceinline__ void fee_backward(const LsimParams &p, float *G, int 
   const int nwords = (T + kWarp - 1) / kWarp;
   for (int i = lane; i < T; i += kWarp) G[i] = 0.f;
   __syncwarp();
-  for (int h = H - 1; h >= 0; --h) {
+  // hits skipped by the early exit: all-true masks, reset index T-1, rejected
+  for (int h = H - 1; h >= st->n_done; --h) {
+    float S = 0.f;
+    for (int i = lane; i < T; i += kWarp) S += G[i];
+    S = warp_sum(S);
+    __syncwarp();
+    if (lane == 0) G[T - 1] -= S;
+    __syncwarp();
+  }
+  for (int h = st->n_done - 1; h >= 0; --h) {
     float S = 0.f;
     for (int m = 0; m < nwords; ++m) {
       int i = m * kWarp + lane;

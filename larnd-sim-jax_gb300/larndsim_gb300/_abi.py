@@ -205,6 +205,10 @@ def make_params(params, lut_shape=None) -> LsimParams:
         nt_, nx, ny, nt = (int(v) for v in lut_shape)
         if nt_ != tmpl.shape[0]:
             raise ValueError(f"template bank has {nt_} templates but long_diff_template has {tmpl.shape[0]}")
+        need = nb * int(params.number_pix_neighbors) + nb // 2
+        if nx < need or ny < need:
+            raise ValueError(f"a {nx}x{ny} LUT covers fewer than the {need} sub-pixel positions that "
+                             f"number_pix_neighbors={params.number_pix_neighbors} reads")
         lp.lut_nx, lp.lut_ny, lp.lut_nt = nx, ny, nt
     lp.threshold = _f32(params.DISCRIMINATION_THRESHOLD)
     lp.gain = _f32(params.GAIN)

@@ -80,18 +80,22 @@ class LUTChain:
         adc, _, pids = self.adc(params, normals)
         return Target(pids, adc)
 
-    def _grad(self, params, g_adc=None, target=None, normals=None, adc_out=None, sync=True):
+    def _grad(self, params, g_adc=None, target=None, normals=None, adc_out=None, sync=True, events=None):
         st = self.stage1(params)
         n_valid = self._check(st) if sync else None
         dev = self.tracks.device
-        out = torch.zeros(1 + _abi.NPARAM, dtype=torch.float32, device=dev)
+        out = torch.empty(1 + _abi.NPARAM, dtype=torch.float32, device=dev)
         tp = target.pids if target is not None else None
         ta = target.adc if target is not None else None
         nt = target.pids.shape[0] if target is not None else 0
+        if events is not None:
+            events[0].record()
         _abi.check(self.lib, self.lib.lsim_lut_grad(
             st.lp, sim._ptr(self.lut.tables), sim._ptr(st.ws), st.n_rows, st.n_events,
             n_valid if n_valid is not None else 0, sim._ptr(normals), sim._ptr(g_adc), sim._ptr(tp), sim._ptr(ta), nt,
             sim._ptr(out), sim._ptr(out[1:]), sim._ptr(adc_out), sim._stream()))
+        if events is not None:
+            events[1].record()
         return out
 
     def loss_and_grad(self, params, target: Target, normals=None):
@@ -100,10 +104,18 @@ class LUTChain:
         vals = out.cpu().numpy()
         return float(vals[0]), dict(zip(GRAD_PARAMS, vals[1:].tolist()))
 
-    def loss_and_grad_device(self, params, target: Target, normals=None):
+    def loss_and_grad_device(self, params, target: Target, normals=None, events=None):
         """Like ``loss_and_grad`` but returns the device tensor [loss, grads...]
-        without a host synchronisation."""
-        return self._grad(params, target=target, normals=normals, sync=False)
+        without a host synchronisation.  ``events`` (start, end) CUDA events,
+        if given, bracket the fused forward+adjoint kernel."""
+        return self._grad(params, target=target, normals=normals, sync=False, events=events)
+
+    def set_tracks(self, tracks):
+        """Replace the batch (same shape); host tensors are copied asynchronously."""
+        src = torch.as_tensor(tracks)
+        if tuple(src.shape) != tuple(self.tracks.shape):
+            raise ValueError("set_tracks needs the shape of the original batch")
+        self.tracks.copy_(src, non_blocking=True)
 
     def vjp(self, params, g_adc: torch.Tensor, normals=None):
         """dL/dtheta for a given cotangent on the (n_valid, H) ADC grid."""
@@ -119,6 +131,7 @@ class _AdcFn(torch.autograd.Function):
         p = params.replace(**{k: float(v) for k, v in zip(GRAD_PARAMS, vals)})
         adc, ticks, pids = chain.adc(p, normals)
         ctx.chain, ctx.params, ctx.normals = chain, p, normals
+        ctx.theta_device, ctx.theta_dtype = theta.device, theta.dtype
         ctx.mark_non_differentiable(ticks, pids)
         return adc, ticks, pids
 
@@ -127,7 +140,19 @@ class _AdcFn(torch.autograd.Function):
         if g_adc is None:
             return None, None, None, None
         grad = ctx.chain.vjp(ctx.params, g_adc, ctx.normals)
-        return grad.to(g_adc.device), None, None, None
+        return grad.to(device=ctx.theta_device, dtype=ctx.theta_dtype), None, None, None
+
+
+def lut_value_and_grad(params, response_template, tracks, fields, target: Target, n_events=None):
+    """Loss and gradient of one fit step through the public API.
+
+    Mirrors the reference's ``value_and_grad(loss_wrapper)`` over
+    LUTSimulation.predict (optimize/fit_params.py:704-731) for the SSE-ADC
+    loss: ``tracks`` may live on the host (copied to the device here); the
+    result comes back to the host.  Returns (loss, {param: dL/dparam}).
+    """
+    chain = LUTChain(params, response_template, tracks, fields, n_events=n_events)
+    return chain.loss_and_grad(params, target)
 
 
 def theta_of(params, device=None) -> torch.Tensor:

@@ -28,10 +28,18 @@ def compare_wfs(wfs_gpu, unique_gpu, wfs_ref, unique_ref):
     return float((np.abs(w - r) / scale).max()) if w.size else 0.0
 
 
-def compare_fee(adc_gpu, ticks_gpu, adc_ref, ticks_ref):
-    """(fraction of hit slots whose tick differs, max rel ADC error where ticks agree)."""
+def compare_fee(adc_gpu, ticks_gpu, adc_ref, ticks_ref, params=None):
+    """(fraction of hit slots whose tick differs, max rel ADC error where ticks agree).
+
+    With ``params`` the inputs are raw integrated charges and are digitised
+    first: the raw integral after a reset is a difference of two large
+    cumulative sums, so its float32 rounding depends on the summation order
+    in both implementations; the contract is on the ADC."""
     tg, tr = np.asarray(ticks_gpu), np.asarray(ticks_ref)
     ag, ar = np.asarray(adc_gpu), np.asarray(adc_ref)
+    if params is not None:
+        from oracle import reference_np as R
+        ag, ar = R.digitize(params, ag), R.digitize(params, ar)
     # a row whose tick differs at hit h differs afterwards as well: compare
     # rows up to their first disagreement
     same_row = np.cumprod(tg == tr, axis=1).astype(bool)

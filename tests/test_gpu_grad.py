@@ -1,0 +1,145 @@
+"""Adjoint parity: the GPU forward+backward of the LUT chain against the
+float64 pathwise gradient of the frozen-decision loss (oracle/grad64.py:
+reverse-mode adjoint, checked against complex-step derivatives and central
+finite differences) -- the gradient jax.value_and_grad computes
+(fit_params.py:731).  Tolerance: 1e-4 relative per parameter.
+
+The loss gradient is sum 2 (ADC - target) dADC/dtheta; close to the target
+the residuals are a few % of the ADC, so float32 rounding of the forward
+ADC (~3e-6 relative) moves the residuals by ~1e-4.  The loss test therefore
+compares against the float64 vector-Jacobian product at the GPU's own
+residuals, and the end-to-end finite-difference test uses a 20 % parameter
+offset where residuals dominate rounding."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_common import small_params
+
+pytestmark = pytest.mark.gpu
+
+GRAD_RTOL = 1e-4
+
+
+def _setup(n_neighbors=1, seed=3, n_tracks=3, shower=0):
+    from larndsim_gb300 import grad, workloads
+    from oracle import reference_np as R
+    p = small_params(n_neighbors=n_neighbors)
+    nx = 10 * n_neighbors + 5
+    resp = workloads.synthetic_response(seed=0, nx=nx, ny=nx)
+    tmpl = R.load_lut_templates(resp, p)
+    tracks, fields = workloads.muon_event(seed=seed, n_tracks=n_tracks)
+    if shower:
+        sh, _ = workloads.shower_event(seed=seed + 100, n_segments=shower)
+        tracks = np.concatenate([tracks, sh])
+    chain = grad.LUTChain(p, torch.from_numpy(tmpl).cuda(), tracks, fields)
+    target = chain.target(p)
+    return p, tmpl, tracks, fields, chain, target
+
+
+def _perturbed(p):
+    return p.replace(Ab=0.83, kb=0.05, eField=0.52, lifetime=2000.0, long_diff=5e-6, tran_diff=9e-6,
+                     lArDensity=1.39)
+
+
+def _check(g_gpu, g_fd, theta):
+    names = list(g_fd)
+    sens = max(abs(g_fd[k] * theta[k]) for k in names)
+    for k in names:
+        err = abs(g_gpu[k] - g_fd[k])
+        ok = err <= GRAD_RTOL * abs(g_fd[k]) or err * abs(theta[k]) <= GRAD_RTOL * sens * 1e-2
+        assert ok, (k, g_gpu[k], g_fd[k])
+
+
+@pytest.mark.parametrize("case", [dict(n_neighbors=1), dict(n_neighbors=2, seed=5, n_tracks=2, shower=300)])
+def test_loss_and_grad_vs_fp64_adjoint(cuda, case):
+    from oracle import grad64 as G
+    p, tmpl, tracks, fields, chain, target = _setup(**case)
+    pp = _perturbed(p)
+    loss, g = chain.loss_and_grad(pp, target)
+    fr = G.Frozen(pp, tmpl, tracks, fields, target.pids.cpu().numpy(), target.adc.cpu().numpy())
+    th = G.theta_dict(pp)
+    # the GPU forward takes the same discrete decisions as the oracle's
+    adc, ticks, pids = chain.adc(pp)
+    assert np.array_equal(pids.cpu().numpy(), fr.unique[fr.valid])
+    acc = ~fr.cond[fr.valid]
+    assert np.array_equal(ticks.cpu().numpy()[acc], fr.idx[fr.valid][acc].astype(np.float32))
+    L64 = G.loss64(fr, th)
+    assert abs(loss - L64) <= 1e-3 * L64 + 1e-3
+    assert g["vdrift"] == 0.0
+    resid = 2.0 * (adc.cpu().numpy().astype(np.float64) - fr.tgt)
+    g_ref = G.adjoint64(fr, th, g_adc=resid)
+    _check(g, g_ref, th)
+
+
+def test_fp64_adjoint_matches_complex_step_and_fd(cuda):
+    """The oracle's reverse mode equals its complex-step and FD gradients."""
+    from oracle import grad64 as G
+    p, tmpl, tracks, fields, chain, target = _setup()
+    pp = _perturbed(p)
+    fr = G.Frozen(pp, tmpl, tracks, fields, target.pids.cpu().numpy(), target.adc.cpu().numpy())
+    th = G.theta_dict(pp)
+    adj, cs, fd = G.adjoint64(fr, th), G.complex_step_gradient(fr, th), G.fd_gradient(fr, th, 1e-6)
+    for k in G.GRAD_PARAMS:
+        assert abs(adj[k] - cs[k]) <= 1e-9 * abs(cs[k]) + 1e-12
+        assert abs(adj[k] - fd[k]) <= 1e-5 * abs(cs[k]) + 1e-9
+
+
+def test_loss_gradient_vs_fd_far_from_target(cuda):
+    """End to end: GPU loss gradient vs FP64 central differences at a 20 %
+    offset, where the residuals are large compared with float32 rounding."""
+    from oracle import grad64 as G
+    p, tmpl, tracks, fields, chain, target = _setup()
+    pp = p.replace(Ab=0.8 * 1.2, kb=0.0486 * 0.8, eField=0.6, lifetime=1800.0, long_diff=6e-6, tran_diff=1.1e-5,
+                   lArDensity=1.38 * 1.02)
+    loss, g = chain.loss_and_grad(pp, target)
+    fr = G.Frozen(pp, tmpl, tracks, fields, target.pids.cpu().numpy(), target.adc.cpu().numpy())
+    th = G.theta_dict(pp)
+    _check(g, G.complex_step_gradient(fr, th), th)
+
+
+def test_autograd_function_matches_fd(cuda):
+    """torch.autograd path with an arbitrary cotangent on the ADC grid."""
+    from larndsim_gb300 import grad
+    from oracle import grad64 as G
+    p, tmpl, tracks, fields, chain, target = _setup()
+    pp = _perturbed(p)
+    theta = grad.theta_of(pp).requires_grad_(True)
+    adc, ticks, pids = grad.adc_fn(theta, chain, pp)
+    rng = np.random.default_rng(1)
+    c = torch.from_numpy(rng.standard_normal(tuple(adc.shape)).astype(np.float32)).cuda()
+    (adc * c).sum().backward()
+    g_gpu = dict(zip(grad.GRAD_PARAMS, theta.grad.cpu().numpy().tolist()))
+    fr = G.Frozen(pp, tmpl, tracks, fields, target.pids.cpu().numpy(), target.adc.cpu().numpy())
+    cc = c.cpu().numpy().astype(np.float64)
+    th = G.theta_dict(pp)
+
+    def lin(t):
+        return float((G.adc64(fr, t)[fr.valid] * cc).sum())
+
+    g_fd = {}
+    for k in G.GRAD_PARAMS:
+        h = 1e-4 * abs(th[k])
+        tp, tm = dict(th), dict(th)
+        tp[k] += h
+        tm[k] -= h
+        g_fd[k] = (lin(tp) - lin(tm)) / (2 * h)
+    _check(g_gpu, g_fd, th)
+
+
+def test_gradient_is_deterministic(cuda):
+    p, tmpl, tracks, fields, chain, target = _setup()
+    pp = _perturbed(p)
+    a = chain.loss_and_grad(pp, target)
+    b = chain.loss_and_grad(pp, target)
+    assert a == b
+
+
+def test_loss_zero_at_target_params(cuda):
+    p, tmpl, tracks, fields, chain, target = _setup()
+    loss, g = chain.loss_and_grad(p, target)
+    assert loss == 0.0
+    assert all(v == 0.0 for v in g.values())

@@ -48,9 +48,13 @@ def test_fee_on_same_waveforms(cuda, small_lut):
     w, u, wo, uo = _run(p, tmpl, tracks, fields)
     integral, ticks = sim.get_adc_values(p, torch.from_numpy(w).cuda())
     ai, ti = R.get_adc_values(p, w)
-    frac, err = compare_fee(integral.cpu().numpy(), ticks.cpu().numpy(), ai, ti)
+    frac, err = compare_fee(integral.cpu().numpy(), ticks.cpu().numpy(), ai, ti, p)
     assert frac < 0.005, frac
     assert err < ADC_RTOL, err
+    # raw integrals: within a few float32 ulps of the row's cumulative charge
+    same = np.cumprod(ticks.cpu().numpy() == ti, axis=1).astype(bool)
+    cmax = np.abs(np.cumsum(w * np.float32(p.t_sampling), axis=1)).max(axis=1, keepdims=True)
+    assert np.all(np.abs(integral.cpu().numpy() - ai)[same] <= (4e-6 * cmax + 1e-3).repeat(ai.shape[1], 1)[same])
     assert (ti < 1998).sum() > 50        # the case has real hits
 
 
@@ -134,7 +138,7 @@ def test_noise_with_supplied_normals(cuda, small_lut):
     normals = rng.standard_normal((w.shape[0], 1 + 3 * p.MAX_ADC_VALUES)).astype(np.float32)
     integral, ticks = sim.get_adc_values(p, torch.from_numpy(w).cuda(), normals=normals)
     ai, ti = R.get_adc_values(p, w, normals)
-    frac, err = compare_fee(integral.cpu().numpy(), ticks.cpu().numpy(), ai, ti)
+    frac, err = compare_fee(integral.cpu().numpy(), ticks.cpu().numpy(), ai, ti, p)
     assert frac < 0.005 and err < ADC_RTOL
 
 

@@ -31,6 +31,6 @@ def test_param_waveforms_and_hits(cuda, kind):
     assert compare_wfs(wfs.cpu().numpy(), unique.cpu().numpy(), ref["wfs"], ref["unique_pixels"]) < WFS_RTOL
     integral, ticks = sim.get_adc_values(p, wfs)
     ai, ti = R.get_adc_values(p, wfs.cpu().numpy())
-    frac, err = compare_fee(integral.cpu().numpy(), ticks.cpu().numpy(), ai, ti)
+    frac, err = compare_fee(integral.cpu().numpy(), ticks.cpu().numpy(), ai, ti, p)
     assert frac < 0.005 and err < ADC_RTOL
     assert out[0].shape[0] > 0
