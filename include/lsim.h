@@ -189,6 +189,28 @@ int lsim_hits(const LsimParams *p, const float *adc, const float *ticks, const i
               float *out_z, float *out_ticks, float *out_hit_prob, int32_t *out_event,
               int32_t *out_pixels, int32_t *nb_valid_dev, void *ws, size_t ws_bytes, void *stream);
 
+/* Hit assembly and compaction like lsim_hits, for callers that cannot
+ * allocate device memory: a caller embedded in a framework that has
+ * reserved the device memory for its own pool (JAX, for one, preallocates
+ * most of the GPU at start-up, so a fresh cudaMalloc from a plug-in in that
+ * process can fail), or code running under a fixed device-memory budget.
+ * No counterpart in the reference (larnd-sim-jax allocates through XLA).
+ * Instead of a workspace it uses a fixed scratch array compiled into the
+ * library (64 KiB, held on every device that loads the library until the
+ * process exits), so it accepts at most 16384 * 1024 = 16,777,216 hit
+ * slots (n_pix * max_adc_values) and returns LSIM_ERR_CAPACITY beyond that.
+ * It calls no cudaMalloc/cudaFree.  The first call on each device looks up
+ * the scratch's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  Every call on a
+ * device shares the one scratch array: calls that overlap on the GPU (for
+ * example on two streams) race and must be serialised by the caller.  The
+ * scratch needs no clearing between calls: every entry a call reads is
+ * written by the same call first. */
+int lsim_hits_noalloc(const LsimParams *p, const float *adc, const float *ticks, const int32_t *unique_pixels,
+                      int64_t n_pix, int32_t tick_limit, float *out_adc, float *out_x, float *out_y,
+                      float *out_z, float *out_ticks, float *out_hit_prob, int32_t *out_event,
+                      int32_t *out_pixels, int32_t *nb_valid_dev, void *stream);
+
 /* ---------------------------------------------------------------- parametrised mode */
 
 /* Stage 1 of simulate_parametrized: shift, quench, drift, Monte-Carlo

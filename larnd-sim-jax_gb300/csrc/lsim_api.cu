@@ -23,6 +23,13 @@ static int fail(int code, const char *fmt, ...) {
   return code;
 }
 
+int set_error(int code, const char *msg) {
+  g_err = msg;
+  return code;
+}
+
+void clear_error() { g_err.clear(); }
+
 static int check_cuda(const char *where) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(LSIM_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));

@@ -6,6 +6,9 @@
 // current_mc / current_model_diff / integrated_expon_diff / emg_pdf
 // (detsim_jax.py:440-474, :581-639) and accumulate_signals_parametrized
 // (detsim_jax.py:207-228).
+#include <cstdio>
+#include <mutex>
+
 #include "lsim_internal.cuh"
 #include "lsim_fee.cuh"
 
@@ -165,6 +168,34 @@ int run_hits(const LsimParams &p, const float *adc, const float *ticks, const in
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------- hits without allocation
+
+// Fixed scratch for lsim_hits_noalloc: one int per 1024 hit slots (the
+// per-tile counts of the two-pass compaction).  64 KiB, resident on every
+// device that loads the library until the process exits.
+constexpr int64_t kHitsStaticTiles = 16384;
+static __device__ __align__(256) int32_t g_hits_static_scratch[kHitsStaticTiles];
+
+constexpr int kMaxDevices = 64;
+static std::mutex g_hits_static_mu;
+static int32_t *g_hits_static_ptr[kMaxDevices] = {};
+
+// Device address of g_hits_static_scratch on the current device, looked up
+// once per device (cudaGetSymbolAddress with that device current).
+static int hits_static_scratch(int32_t **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return LSIM_ERR_CUDA;
+  if (dev < 0 || dev >= kMaxDevices) return LSIM_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_hits_static_mu);
+  if (!g_hits_static_ptr[dev]) {
+    void *ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_hits_static_scratch) != cudaSuccess || !ptr) return LSIM_ERR_CUDA;
+    g_hits_static_ptr[dev] = (int32_t *)ptr;
+  }
+  *out = g_hits_static_ptr[dev];
+  return LSIM_OK;
+}
+
 // ---------------------------------------------------------------- parametrised current
 
 // 0.5*erf((x-loc)/(sqrt2*diff)) - emg_pdf(x, loc, diff, lambd)/lambd
@@ -272,3 +303,37 @@ int run_param_accum(const LsimParams &p, const Workspace &w, const Grid &g, int3
 }
 
 }  // namespace lsim
+
+extern "C" int lsim_hits_noalloc(const LsimParams *p, const float *adc, const float *ticks,
+                                 const int32_t *unique_pixels, int64_t n_pix, int32_t tick_limit, float *out_adc,
+                                 float *out_x, float *out_y, float *out_z, float *out_ticks, float *out_hit_prob,
+                                 int32_t *out_event, int32_t *out_pixels, int32_t *nb_valid_dev, void *stream) {
+  using namespace lsim;
+  clear_error();
+  if (!p) return set_error(LSIM_ERR_INVALID, "lsim_hits_noalloc: null parameter block");
+  if (!nb_valid_dev || (n_pix > 0 && (!adc || !ticks || !unique_pixels || !out_adc || !out_x || !out_y || !out_z ||
+                                      !out_ticks || !out_hit_prob || !out_event || !out_pixels)))
+    return set_error(LSIM_ERR_INVALID, "lsim_hits_noalloc: null pointer");
+  if (n_pix < 0) return set_error(LSIM_ERR_INVALID, "lsim_hits_noalloc: negative pixel count");
+  const int64_t slots = n_pix * (int64_t)p->max_adc_values;
+  if (slots > kHitsStaticTiles * (int64_t)kHitTile) {
+    char msg[256];
+    snprintf(msg, sizeof(msg),
+             "lsim_hits_noalloc: %lld hit slots (%lld pixels x %d hits) exceed the fixed scratch limit of %lld "
+             "slots; use lsim_hits with a caller-allocated workspace",
+             (long long)slots, (long long)n_pix, p->max_adc_values, (long long)(kHitsStaticTiles * kHitTile));
+    return set_error(LSIM_ERR_CAPACITY, msg);
+  }
+  int32_t *scratch = nullptr;
+  if (hits_static_scratch(&scratch) != LSIM_OK)
+    return set_error(LSIM_ERR_CUDA, "lsim_hits_noalloc: cannot resolve the device address of the fixed scratch");
+  int rc = run_hits(*p, adc, ticks, unique_pixels, n_pix, tick_limit, out_adc, out_x, out_y, out_z, out_ticks,
+                    out_hit_prob, out_event, out_pixels, nb_valid_dev, scratch, (cudaStream_t)stream);
+  if (rc != LSIM_OK) {
+    cudaError_t e = cudaGetLastError();
+    char msg[256];
+    snprintf(msg, sizeof(msg), "lsim_hits_noalloc: CUDA error %s", cudaGetErrorString(e));
+    return set_error(rc, msg);
+  }
+  return LSIM_OK;
+}

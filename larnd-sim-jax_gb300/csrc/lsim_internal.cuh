@@ -50,4 +50,8 @@ int run_prepare_tables(const LsimParams &p, const float *templates, void *tables
 
 int device_sm_count();
 
+// lsim_api.cu: thread-local error message shared by all entry points
+int set_error(int code, const char *msg);
+void clear_error();
+
 }  // namespace lsim

@@ -85,6 +85,8 @@ _SIGNATURES = {
     "lsim_hits_workspace_bytes": (_sz, [_i64, _i32]),
     "lsim_hits": (C.c_int, [_PP, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz,
                             _vp]),
+    "lsim_hits_noalloc": (C.c_int, [_PP, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                    _vp]),
     "lsim_param_stage1": (C.c_int, [_PP, _PF, _vp, _i64, _i32, _vp, _vp, _sz, _vp, _vp]),
     "lsim_param_stage2": (C.c_int, [_PP, _vp, _i64, _i32, _i64, _i32, _i32, _vp, _vp, _vp]),
 }
