@@ -143,56 +143,71 @@ __device__ __forceinline__ void neigh_setup(const LsimParams &p, const Tables &t
   __syncwarp();
 }
 
-// Forward window of one contribution given its samples V[k] (v[m] holds
-// V[32m + lane - 1]).  Interior windows (the whole window inside columns
-// [1, Nticks-2]) take the fast path: the boundary correction is the
-// leading sample U[-1] of the window and val[r] = U[r-2](1-f) + U[r-1] f.
-__device__ __forceinline__ void window_apply(const LsimParams &p, const float v[kChunks], int cb, float frac,
-                                             float corr, float *row, int lane) {
-  const int L = p.signal_length, NT = p.n_ticks;
+// Forward window update with a column-owner lane map: lane l handles the
+// window positions r with (cb + r) = l (mod 32), i.e. r = rl + 32j with
+// rl = (l - cb) mod 32, so each lane only ever touches its own columns.
+// Contributions therefore need no warp barrier between them and their
+// updates can be interleaved; the samples a block of lanes reads are still
+// 32 consecutive ticks.  U[j] is the window sample k = rl + 32j - 1: the
+// boundary correction at k = -1, V[k] for 0 <= k < L, 0 beyond, and
+//   val[r] = U(r-2) (1 - f) + U(r-1) f,
+// where U(r-2) comes from lane (l - 1) mod 32 (from the previous block for
+// the lane with rl = 0).
+
+__device__ __forceinline__ int owner_rl(int cb, int lane) { return (lane - cb) & (kWarp - 1); }
+
+// Window that crosses the edge of the waveform: value parts are kept only
+// in columns [2, Nticks-1], correction parts only in [1, Nticks-2].
+__device__ __noinline__ void window_apply_edge(const float U[kChunks], int cb, int rl, float frac, int L, int NT,
+                                               float *row, int lane) {
   const float f1 = 1.f - frac;
-  float carry = 0.f;
-  if (cb >= 1 && cb + L + 1 <= NT - 2) {
+  float sprev = 0.f;
 #pragma unroll
-    for (int m = 0; m < kChunks; ++m) {
-      float U = v[m];
-      if (m == 0 && lane == 0) U = corr;
-      float prev = __shfl_up_sync(0xffffffffu, U, 1);
-      if (lane == 0) prev = carry;
-      carry = __shfl_sync(0xffffffffu, U, kWarp - 1);
-      row[cb + m * kWarp + lane] += prev * f1 + U * frac;
-    }
-    return;
-  }
-#pragma unroll
-  for (int m = 0; m < kChunks; ++m) {
-    const int r = m * kWarp + lane;
-    const float Vk = v[m];
-    float prev = __shfl_up_sync(0xffffffffu, Vk, 1);
-    if (lane == 0) prev = carry;
-    carry = __shfl_sync(0xffffffffu, Vk, kWarp - 1);
+  for (int j = 0; j < kChunks; ++j) {
+    const float sh = __shfl_sync(0xffffffffu, U[j], (lane + kWarp - 1) & (kWarp - 1));
+    const float prev = rl == 0 ? sprev : sh;
+    sprev = sh;
+    const int r = rl + j * kWarp;
     const int col = cb + r;
-    if (r < L + 2) {
-      float val = 0.f;
-      if (col >= 2 && col <= NT - 1) val = prev * f1 + Vk * frac;
-      if (col >= 1 && col <= NT - 2) {
-        if (r == 0) val += corr * frac;
-        else if (r == 1) val += corr * f1;
-      }
-      if (col >= 1 && col <= NT - 1) row[col] += val;
-    }
+    if (r >= L + 2 || col < 1 || col > NT - 1) continue;
+    const bool vc = col <= NT - 2, vv = col >= 2;
+    float val;
+    if (r == 0) val = vc ? U[j] * frac : 0.f;
+    else if (r == 1) val = (vc ? prev * f1 : 0.f) + (vv ? U[j] * frac : 0.f);
+    else val = vv ? prev * f1 + U[j] * frac : 0.f;
+    row[col] += val;
   }
 }
 
-__device__ __forceinline__ void neigh_load(const LsimParams &p, const Tables &tab, int rowidx, float v[kChunks],
-                                           int lane) {
-  const int L = p.signal_length;
+__device__ __forceinline__ void window_apply(const float U[kChunks], int cb, int rl, float frac, int L, int NT,
+                                             float *row, int lane) {
+  if (cb >= 1 && cb + L + 1 <= NT - 2) {
+    // interior: all columns valid; positions past L + 1 add exact zeros
+    const float f1 = 1.f - frac;
+    float sprev = 0.f;
+#pragma unroll
+    for (int j = 0; j < kChunks; ++j) {
+      const float sh = __shfl_sync(0xffffffffu, U[j], (lane + kWarp - 1) & (kWarp - 1));
+      const float prev = rl == 0 ? sprev : sh;
+      sprev = sh;
+      row[cb + rl + j * kWarp] += prev * f1 + U[j] * frac;
+    }
+  } else {
+    window_apply_edge(U, cb, rl, frac, L, NT, row, lane);
+  }
+}
+
+// Template-0 window samples of a neighbour contribution, times n_e, with
+// the boundary correction as sample k = -1.
+__device__ __forceinline__ void neigh_samples(const Tables &tab, int rowidx, int rl, int L, float ne, float corr,
+                                              float U[kChunks]) {
   const float *src = tab.w0 + (size_t)(rowidx < 0 ? 0 : rowidx) * L;
 #pragma unroll
-  for (int m = 0; m < kChunks; ++m) {
-    const int k = m * kWarp + lane - 1;
-    v[m] = (rowidx >= 0 && k >= 0 && k < L) ? __ldg(src + k) : 0.f;
+  for (int j = 0; j < kChunks; ++j) {
+    const int k = rl + j * kWarp - 1;
+    U[j] = (rowidx >= 0 && k >= 0 && k < L) ? __ldg(src + k) * ne : 0.f;
   }
+  if (rl == 0) U[0] = corr;
 }
 
 __device__ __forceinline__ void scale(float v[kChunks], float a) {
@@ -203,47 +218,88 @@ __device__ __forceinline__ void scale(float v[kChunks], float a) {
 // Forward: all neighbour parts of the pixel, four contributions in flight.
 __device__ __forceinline__ void neigh_forward(const LsimParams &p, const Tables &tab, const Workspace &w,
                                               const ListSmem &ls, NBatch &nb, float *row, int lane) {
+  const int L = p.signal_length, NT = p.n_ticks;
   const int n_total = ls.pre_n[ls.n];
   for (int g0 = 0; g0 < n_total; g0 += kWarp) {
     neigh_setup<false>(p, tab, w, ls, nb, g0, n_total, lane);
     const int m = min(kWarp, n_total - g0);
     for (int j = 0; j < m; j += 4) {
-      float v0[kChunks], v1[kChunks], v2[kChunks], v3[kChunks];
+      float u0[kChunks], u1[kChunks], u2[kChunks], u3[kChunks];
       const int r0 = nb.row[j];
       const int r1 = j + 1 < m ? nb.row[j + 1] : -1;
       const int r2 = j + 2 < m ? nb.row[j + 2] : -1;
       const int r3 = j + 3 < m ? nb.row[j + 3] : -1;
-      neigh_load(p, tab, r0, v0, lane);
-      neigh_load(p, tab, r1, v1, lane);
-      neigh_load(p, tab, r2, v2, lane);
-      neigh_load(p, tab, r3, v3, lane);
-      if (r0 >= 0) {
-        scale(v0, nb.ne[j]);
-        window_apply(p, v0, nb.cb[j], nb.frac[j], nb.D[j] * nb.ne[j], row, lane);
-        __syncwarp();
-      }
-      if (r1 >= 0) {
-        scale(v1, nb.ne[j + 1]);
-        window_apply(p, v1, nb.cb[j + 1], nb.frac[j + 1], nb.D[j + 1] * nb.ne[j + 1], row, lane);
-        __syncwarp();
-      }
-      if (r2 >= 0) {
-        scale(v2, nb.ne[j + 2]);
-        window_apply(p, v2, nb.cb[j + 2], nb.frac[j + 2], nb.D[j + 2] * nb.ne[j + 2], row, lane);
-        __syncwarp();
-      }
-      if (r3 >= 0) {
-        scale(v3, nb.ne[j + 3]);
-        window_apply(p, v3, nb.cb[j + 3], nb.frac[j + 3], nb.D[j + 3] * nb.ne[j + 3], row, lane);
-        __syncwarp();
-      }
+      const int c0 = nb.cb[j], c1 = nb.cb[j + 1], c2 = nb.cb[j + 2], c3 = nb.cb[j + 3];
+      const int l0 = owner_rl(c0, lane), l1 = owner_rl(c1, lane), l2 = owner_rl(c2, lane), l3 = owner_rl(c3, lane);
+      neigh_samples(tab, r0, l0, L, nb.ne[j], nb.D[j] * nb.ne[j], u0);
+      neigh_samples(tab, r1, l1, L, nb.ne[j + 1], nb.D[j + 1] * nb.ne[j + 1], u1);
+      neigh_samples(tab, r2, l2, L, nb.ne[j + 2], nb.D[j + 2] * nb.ne[j + 2], u2);
+      neigh_samples(tab, r3, l3, L, nb.ne[j + 3], nb.D[j + 3] * nb.ne[j + 3], u3);
+      if (r0 >= 0) window_apply(u0, c0, l0, nb.frac[j], L, NT, row, lane);
+      if (r1 >= 0) window_apply(u1, c1, l1, nb.frac[j + 1], L, NT, row, lane);
+      if (r2 >= 0) window_apply(u2, c2, l2, nb.frac[j + 2], L, NT, row, lane);
+      if (r3 >= 0) window_apply(u3, c3, l3, nb.frac[j + 3], L, NT, row, lane);
     }
+    __syncwarp();
   }
 }
 
 struct Theta {
   float v[LSIM_NPARAM];
 };
+
+// Adjoint of one neighbour contribution (descriptor j of the batch) given
+// its template-0 samples v[c] = T0[32c + lane]: accumulates dL/dtheta.
+__device__ __forceinline__ void neigh_vjp_one(const NBatch &nb, int j, const float v[kChunks], int L, int NT,
+                                              float inv_ts, const float *grow, Theta &th, int lane) {
+  const int cb = nb.cb[j];
+  const float f = nb.frac[j], f1 = 1.f - f, ne = nb.ne[j];
+  float acc_ne = 0.f, acc_fr = 0.f;
+  if (cb >= 1 && cb + L + 1 <= NT - 2) {
+    // interior window: every column in range; samples past L are zero
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) {
+      const int k = c * kWarp + lane;
+      const float gA = grow[cb + k + 1], gB = grow[cb + k + 2];
+      acc_ne += (gA * f + gB * f1) * v[c];
+      acc_fr += v[c] * (gA - gB);
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) {
+      const int k = c * kWarp + lane;
+      if (k < L) {
+        const int ca = cb + k + 1, cbb = cb + k + 2;
+        const float gA = (ca >= 2 && ca <= NT - 1) ? grow[ca] : 0.f;
+        const float gB = (cbb >= 2 && cbb <= NT - 1) ? grow[cbb] : 0.f;
+        acc_ne += (gA * f + gB * f1) * v[c];
+        acc_fr += v[c] * (gA - gB);
+      }
+    }
+  }
+  if (lane == 0) {
+    const float gc0 = (cb >= 1 && cb <= NT - 2) ? grow[cb] : 0.f;
+    const float gc1 = (cb + 1 >= 1 && cb + 1 <= NT - 2) ? grow[cb + 1] : 0.f;
+    const float dcorr = gc0 * f + gc1 * f1;
+    acc_ne += dcorr * nb.D[j];
+    acc_fr += dcorr * nb.dl[j] + nb.D[j] * (gc0 - gc1);
+  }
+  const float dt = acc_fr * ne * inv_ts;
+  th.v[0] += acc_ne * nb.dne[0][j];
+  th.v[1] += acc_ne * nb.dne[1][j];
+  th.v[2] += acc_ne * nb.dne[2][j] + dt * nb.dt0[j];
+  th.v[3] += acc_ne * nb.dne[3][j];
+  th.v[7] += acc_ne * nb.dne[4][j];
+}
+
+__device__ __forceinline__ void neigh_rows(const Tables &tab, int rowidx, int L, float v[kChunks], int lane) {
+  const float *src = tab.w0 + (size_t)(rowidx < 0 ? 0 : rowidx) * L;
+#pragma unroll
+  for (int c = 0; c < kChunks; ++c) {
+    const int k = c * kWarp + lane;
+    v[c] = (rowidx >= 0 && k < L) ? __ldg(src + k) : 0.f;
+  }
+}
 
 // Adjoint: all neighbour parts, given the waveform cotangent grow[col].
 __device__ __forceinline__ void neigh_backward(const LsimParams &p, const Tables &tab, const Workspace &w,
@@ -258,51 +314,9 @@ __device__ __forceinline__ void neigh_backward(const LsimParams &p, const Tables
     for (int j = 0; j < m; ++j) {
       const int rowidx = nb.row[j];
       if (rowidx < 0) continue;
-      const int cb = nb.cb[j];
-      const float f = nb.frac[j], f1 = 1.f - f, ne = nb.ne[j];
       float v[kChunks];
-      const float *src = tab.w0 + (size_t)rowidx * L;
-#pragma unroll
-      for (int c = 0; c < kChunks; ++c) {
-        const int k = c * kWarp + lane;
-        v[c] = k < L ? __ldg(src + k) : 0.f;
-      }
-      float acc_ne = 0.f, acc_fr = 0.f;
-      if (cb >= 1 && cb + L + 1 <= NT - 2) {
-        // interior window: every column in range; samples past L are zero
-#pragma unroll
-        for (int c = 0; c < kChunks; ++c) {
-          const int k = c * kWarp + lane;
-          const float gA = grow[cb + k + 1], gB = grow[cb + k + 2];
-          acc_ne += (gA * f + gB * f1) * v[c];
-          acc_fr += v[c] * (gA - gB);
-        }
-      } else {
-#pragma unroll
-        for (int c = 0; c < kChunks; ++c) {
-          const int k = c * kWarp + lane;
-          if (k < L) {
-            const int ca = cb + k + 1, cbb = cb + k + 2;
-            const float gA = (ca >= 2 && ca <= NT - 1) ? grow[ca] : 0.f;
-            const float gB = (cbb >= 2 && cbb <= NT - 1) ? grow[cbb] : 0.f;
-            acc_ne += (gA * f + gB * f1) * v[c];
-            acc_fr += v[c] * (gA - gB);
-          }
-        }
-      }
-      if (lane == 0) {
-        const float gc0 = (cb >= 1 && cb <= NT - 2) ? grow[cb] : 0.f;
-        const float gc1 = (cb + 1 >= 1 && cb + 1 <= NT - 2) ? grow[cb + 1] : 0.f;
-        const float dcorr = gc0 * f + gc1 * f1;
-        acc_ne += dcorr * nb.D[j];
-        acc_fr += dcorr * nb.dl[j] + nb.D[j] * (gc0 - gc1);
-      }
-      const float dt = acc_fr * ne * inv_ts;
-      th.v[0] += acc_ne * nb.dne[0][j];
-      th.v[1] += acc_ne * nb.dne[1][j];
-      th.v[2] += acc_ne * nb.dne[2][j] + dt * nb.dt0[j];
-      th.v[3] += acc_ne * nb.dne[3][j];
-      th.v[7] += acc_ne * nb.dne[4][j];
+      neigh_rows(tab, rowidx, L, v, lane);
+      neigh_vjp_one(nb, j, v, L, NT, inv_ts, grow, th, lane);
     }
     __syncwarp();
   }
@@ -379,23 +393,25 @@ __device__ __forceinline__ bool main_setup(const LsimParams &p, const Tables &ta
 __device__ __forceinline__ void main_forward_one(const LsimParams &p, const Tables &tab, const MainHead &h,
                                                  const MainSmem &ms, float *row, int lane) {
   const int L = p.signal_length;
+  const int rl = owner_rl(h.cb, lane);
   float acc[kChunks];
 #pragma unroll
-  for (int m = 0; m < kChunks; ++m) acc[m] = 0.f;
+  for (int j = 0; j < kChunks; ++j) acc[j] = 0.f;
   for (int e = 0; e < h.n; ++e) {
     const float4 *src = tab.wmp + (size_t)ms.off[e] * L;
     const float W = ms.W[e];
 #pragma unroll
-    for (int m = 0; m < kChunks; ++m) {
-      const int k = m * kWarp + lane - 1;
+    for (int j = 0; j < kChunks; ++j) {
+      const int k = rl + j * kWarp - 1;
       if (k >= 0 && k < L) {
         const float4 t = __ldg(src + k);
-        acc[m] += W * ((t.y * h.qb + t.x * h.qa) + t.z * h.qc);
+        acc[j] += W * ((t.y * h.qb + t.x * h.qa) + t.z * h.qc);
       }
     }
   }
   scale(acc, h.ne);
-  window_apply(p, acc, h.cb, h.frac, h.corr, row, lane);
+  if (rl == 0) acc[0] = h.corr;
+  window_apply(acc, h.cb, rl, h.frac, L, p.n_ticks, row, lane);
   __syncwarp();
 }
 
