@@ -500,18 +500,39 @@ static_assert(sizeof(WarpSmem<true>) % 16 == 0, "per-warp shared memory must kee
 static_assert(offsetof(WarpSmem<false>, buf) == 0 && offsetof(WarpSmem<true>, buf) == 0, "row first");
 static_assert((kRowPad + 1) % 4 == 0 && kRowFloats % 4 == 0, "output column 1 of the row must be 16-byte aligned");
 
-// Walk the segments of the 3x3 slots; run fn on those with bins on the pixel.
+// Whether any of the kMaxTran bins around bin b (b - 2 .. b + 2) lies in
+// the pixel at offset d from the pixel of b (the test of axis_weights).
+__device__ __forceinline__ bool axis_reaches(int b, int nb, int d) {
+  const int pp = ifloordiv(b, nb);
+  return ifloordiv(b - kMaxTran / 2, nb) - pp <= d && d <= ifloordiv(b + kMaxTran / 2, nb) - pp;
+}
+
+// Walk the segments of the 3x3 slots; run fn on those with bins on the
+// pixel.  32 candidates are tested at once (charge and bin offsets), so
+// only segments that contribute reach the per-contribution setup.
 template <typename F>
-__device__ __forceinline__ void for_each_main(const Workspace &w, const ListSmem &ls, int lane, F &&fn) {
+__device__ __forceinline__ void for_each_main(const LsimParams &p, const Workspace &w, const ListSmem &ls, int lane,
+                                              F &&fn) {
+  const int nbp = p.nb_bins_per_pixel;
   for (int e = 0; e < ls.n; ++e) {
     const int dxy = ls.dxy[e];
     const int dx = (dxy & 0xff) - 16, dy = ((dxy >> 8) & 0xff) - 16;
     if (dx < -1 || dx > 1 || dy < -1 || dy > 1) continue;
     const int o = ls.off[e], c = ls.cnt[e];
     for (int j0 = 0; j0 < c; j0 += kWarp) {
-      const int mine = (j0 + lane < c) ? __ldg(w.seg_list + o + j0 + lane) : -1;
-      const int m = min(kWarp, c - j0);
-      for (int jj = 0; jj < m; ++jj) fn(__shfl_sync(0xffffffffu, mine, jj), dx, dy);
+      int mine = -1;
+      bool hit = false;
+      if (j0 + lane < c) {
+        mine = __ldg(w.seg_list + o + j0 + lane);
+        const SegFwd &f = w.segf[mine];
+        hit = __ldg(&f.ne) != 0.f && axis_reaches(__ldg(&f.bx), nbp, dx) && axis_reaches(__ldg(&f.by), nbp, dy);
+      }
+      unsigned bal = __ballot_sync(0xffffffffu, hit);
+      while (bal) {
+        const int jj = __ffs(bal) - 1;
+        bal &= bal - 1u;
+        fn(__shfl_sync(0xffffffffu, mine, jj), dx, dy);
+      }
     }
   }
 }
@@ -594,7 +615,7 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 3) k_lut_pixels(AccumArgs a
     build_list(a.g, a.w.cnt, a.w.off, slot, sm.list, lane);
     // ---- forward: neighbour parts, then main-bin parts
     neigh_forward(p, a.tab, a.w, sm.list, sm.nb, row, lane);
-    for_each_main(a.w, sm.list, lane, [&](int s, int dx, int dy) {
+    for_each_main(p, a.w, sm.list, lane, [&](int s, int dx, int dy) {
       MainHead h;
       if (main_setup<false>(p, a.tab, a.w, s, dx, dy, h, sm.ms, lane)) main_forward_one(p, a.tab, h, sm.ms, row, lane);
     });
@@ -652,7 +673,7 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 3) k_lut_pixels(AccumArgs a
 #pragma unroll
       for (int i = 0; i < LSIM_NPARAM; ++i) th.v[i] = 0.f;
       neigh_backward(p, a.tab, a.w, sm.list, sm.nb, row, th, lane);
-      for_each_main(a.w, sm.list, lane, [&](int s, int dx, int dy) {
+      for_each_main(p, a.w, sm.list, lane, [&](int s, int dx, int dy) {
         MainHead h;
         if (main_setup<true>(p, a.tab, a.w, s, dx, dy, h, sm.ms, lane))
           main_backward_one(p, a.tab, h, sm.ms, a.w.sega[s], row, th, lane);
