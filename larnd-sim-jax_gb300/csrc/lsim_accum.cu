@@ -27,6 +27,7 @@
 // fall on the pixel) take a per-contribution path over up to 5x5 grouped
 // LUT sub-positions.
 #include "lsim_internal.cuh"
+#include "lsim_bins.cuh"
 #include "lsim_fee.cuh"
 
 namespace lsim {
@@ -35,7 +36,6 @@ constexpr int kAccWarps = 4;
 constexpr int kRowPad = 3;            // row[col] at buf[kRowPad + col]: col 1 is 16-byte aligned
 constexpr int kRowFloats = 2052;      // >= kRowPad + n_ticks (2001), multiple of 4
 constexpr int kMaxList = 81;          // (2 * 4 + 1)^2 neighbourhood slots
-constexpr int kChunks = 5;            // ceil((L + 2) / 32) for L <= 158
 
 // Descriptors of one batch of 32 neighbour contributions (structure of arrays).
 struct NBatch {
@@ -53,41 +53,6 @@ struct ListSmem {
   int n;
 };
 
-
-// Sub-pixel LUT index of a bin, int(|b % nb - nb//2 + 0.5 - shift|)
-// (sim_jax.py:435, :443).
-__device__ __forceinline__ int lut_index(int b, int nb, int shift) {
-  return (int)fabsf(__fsub_rn(__fadd_rn((float)(imod(b, nb) - nb / 2), 0.5f), (float)shift));
-}
-
-// Weight (sum of 1-D bin integrals) per main LUT sub-position u in [0, 5)
-// for the bins of one axis that fall on the target pixel.
-__device__ __forceinline__ void axis_weights(const float e[kMaxTran], const float de[kMaxTran], int b, int nb,
-                                             int d, float W[kMainSub], float dW[kMainSub], unsigned *umask) {
-  const int pp = ifloordiv(b, nb);
-  unsigned um = 0;
-#pragma unroll
-  for (int u = 0; u < kMainSub; ++u) { W[u] = 0.f; dW[u] = 0.f; }
-#pragma unroll
-  for (int i = 0; i < kMaxTran; ++i) {
-    const int bi = b + i - kMaxTran / 2;
-    if (ifloordiv(bi, nb) - pp != d) continue;
-    const int u = lut_index(bi, nb, 0);
-#pragma unroll
-    for (int uu = 0; uu < kMainSub; ++uu)
-      if (uu == u) { W[uu] += e[i]; dW[uu] += de[i]; }
-    um |= 1u << u;
-  }
-  *umask = um;
-}
-
-__device__ __forceinline__ float cum_terms(const float *row, int cath, int Nt, int L, float frac, float *dlerp) {
-  const float v0 = __ldg(row + cath);
-  const float v1 = __ldg(row + min(cath + 1, Nt - 1));
-  const float vs = __ldg(row + Nt - L);
-  *dlerp = v0 - v1;
-  return vs - (v0 * (1.f - frac) + v1 * frac);
-}
 
 // ---------------------------------------------------------------- neighbour batches
 
@@ -322,158 +287,124 @@ __device__ __forceinline__ void neigh_backward(const LsimParams &p, const Tables
   }
 }
 
-// ---------------------------------------------------------------- main bins
+// ---------------------------------------------------------------- main-bin records
 
-// The current main-bin contribution: its distinct LUT sub-positions (u, v),
-// compacted by one lane each, with weight W = Xw[u] Yw[v] (summed 1-D bin
-// integrals of the bins on the pixel), dW/dsigma_T, and the boundary terms.
-struct MainSmem {
-  int off[kMainSub * kMainSub];     // (tidx*5 + u)*5 + v
-  float W[kMainSub * kMainSub], dW[kMainSub * kMainSub];
-  float D[kMainSub * kMainSub], dl[kMainSub * kMainSub];
-};
-
-struct MainHead {
-  float ne, frac, qa, qb, qc, corr;
-  int cb, n;
-};
-
-template <bool GRAD>
-__device__ __forceinline__ bool main_setup(const LsimParams &p, const Tables &tab, const Workspace &w, int s, int dx,
-                                           int dy, MainHead &h, MainSmem &ms, int lane) {
-  const SegFwd &f = w.segf[s];
-  h.ne = f.ne;
-  if (h.ne == 0.f) return false;
+// The main-bin records that land on this pixel: segments of the 3x3 slots
+// whose bins reach it (tested 32 candidates at a time).  Accepted records
+// are packed into the batch -- record index in nb.row, window origin,
+// sub-tick fraction, and for the adjoint d t0/d eField in nb.dt0 and the
+// record's d corr/d frac in nb.D -- and handed to flush(m) 32 at a time.
+template <bool GRAD, typename F>
+__device__ __forceinline__ void main_batches(const LsimParams &p, const Workspace &w, const ListSmem &ls, NBatch &nb,
+                                             int lane, F &&flush) {
   const int nbp = p.nb_bins_per_pixel;
-  float ex[kMaxTran], ey[kMaxTran], dex[kMaxTran], dey[kMaxTran];
-#pragma unroll
-  for (int i = 0; i < kMaxTran; ++i) {
-    ex[i] = f.ex[i];
-    ey[i] = f.ey[i];
-    dex[i] = GRAD ? w.sega[s].dex[i] : 0.f;
-    dey[i] = GRAD ? w.sega[s].dey[i] : 0.f;
-  }
-  float Xw[kMainSub], Yw[kMainSub], dXw[kMainSub], dYw[kMainSub];
-  unsigned um, vm;
-  axis_weights(ex, dex, f.bx, nbp, dx, Xw, dXw, &um);
-  axis_weights(ey, dey, f.by, nbp, dy, Yw, dYw, &vm);
-  if (!um || !vm) return false;
-  h.frac = f.frac; h.qa = f.qa; h.qb = f.qb; h.qc = f.qc;
-  const int cath = f.cath, tidx = f.tidx;
-  h.cb = p.lut_nt - p.signal_length - cath - 1;
-  // lane l < 25 owns sub-position (u, v) = (l / 5, l % 5)
-  const int u = lane / kMainSub, v = lane % kMainSub;
-  const bool mine = lane < kMainSub * kMainSub && ((um >> u) & 1u) && ((vm >> v) & 1u);
-  float xw = 0.f, yw = 0.f, dxw = 0.f, dyw = 0.f;
-#pragma unroll
-  for (int q = 0; q < kMainSub; ++q) {
-    if (q == u) { xw = Xw[q]; dxw = dXw[q]; }
-    if (q == v) { yw = Yw[q]; dyw = dYw[q]; }
-  }
-  const unsigned bal = __ballot_sync(0xffffffffu, mine);
-  float wd = 0.f;
-  if (mine) {
-    const int pos = __popc(bal & ((1u << lane) - 1u));
-    const int off = (tidx * kMainSub + u) * kMainSub + v;
-    float dl;
-    const float D = cum_terms(tab.cm + (size_t)off * p.lut_nt, cath, p.lut_nt, p.signal_length, h.frac, &dl);
-    ms.off[pos] = off;
-    ms.W[pos] = xw * yw;
-    ms.dW[pos] = dxw * yw + xw * dyw;
-    ms.D[pos] = D;
-    ms.dl[pos] = dl;
-    wd = (xw * yw) * D;
-  }
-  h.corr = warp_sum(wd) * h.ne;
-  h.n = __popc(bal);
-  __syncwarp();
-  return true;
-}
-
-__device__ __forceinline__ void main_forward_one(const LsimParams &p, const Tables &tab, const MainHead &h,
-                                                 const MainSmem &ms, float *row, int lane) {
-  const int L = p.signal_length;
-  const int rl = owner_rl(h.cb, lane);
-  float acc[kChunks];
-#pragma unroll
-  for (int j = 0; j < kChunks; ++j) acc[j] = 0.f;
-  for (int e = 0; e < h.n; ++e) {
-    const float4 *src = tab.wmp + (size_t)ms.off[e] * L;
-    const float W = ms.W[e];
-#pragma unroll
-    for (int j = 0; j < kChunks; ++j) {
-      const int k = rl + j * kWarp - 1;
-      if (k >= 0 && k < L) {
-        const float4 t = __ldg(src + k);
-        acc[j] += W * ((t.y * h.qb + t.x * h.qa) + t.z * h.qc);
+  int m = 0;
+  for (int e = 0; e < ls.n; ++e) {
+    const int dxy = ls.dxy[e];
+    const int dx = (dxy & 0xff) - 16, dy = ((dxy >> 8) & 0xff) - 16;
+    if (dx < -1 || dx > 1 || dy < -1 || dy > 1) continue;
+    const int o = ls.off[e], c = ls.cnt[e];
+    for (int j0 = 0; j0 < c; j0 += kWarp) {
+      int s = 0, slot = 0;
+      bool hit = false;
+      if (j0 + lane < c) {
+        s = __ldg(w.seg_list + o + j0 + lane);
+        const SegFwd &f = w.segf[s];
+        int lx, hx, ly, hy;
+        axis_range(__ldg(&f.bx), nbp, &lx, &hx);
+        axis_range(__ldg(&f.by), nbp, &ly, &hy);
+        hit = __ldg(&f.ne) != 0.f && lx <= dx && dx <= hx && ly <= dy && dy <= hy;
+        slot = (dx - lx) * 2 + (dy - ly);
       }
+      const unsigned bal = __ballot_sync(0xffffffffu, hit);
+      const int nh = __popc(bal);
+      if (m + nh > kWarp) {
+        flush(m);
+        m = 0;
+      }
+      if (hit) {
+        const int pos = m + __popc(bal & ((1u << lane) - 1u));
+        const SegFwd &f = w.segf[s];
+        const int rec = s * kRecPerSeg + slot;
+        nb.row[pos] = rec;
+        nb.cb[pos] = p.lut_nt - p.signal_length - __ldg(&f.cath) - 1;
+        nb.frac[pos] = __ldg(&f.frac);
+        if (GRAD) {
+          nb.dt0[pos] = __ldg(&w.sega[s].dt0);
+          nb.D[pos] = w.mrec[(size_t)rec * kRecFloats + kRecDl];
+        }
+      }
+      m += nh;
+      __syncwarp();
     }
   }
-  scale(acc, h.ne);
-  if (rl == 0) acc[0] = h.corr;
-  window_apply(acc, h.cb, rl, h.frac, L, p.n_ticks, row, lane);
-  __syncwarp();
+  if (m) flush(m);
 }
 
-__device__ __forceinline__ void main_backward_one(const LsimParams &p, const Tables &tab, const MainHead &h,
-                                                  const MainSmem &ms, const SegAdj &a, const float *grow, Theta &th,
-                                                  int lane) {
+// Forward: add m batched records (window samples k = -1 .. 158 stored at
+// rec[k + 1], zero past L), four in flight.
+__device__ __forceinline__ void main_rec_forward(const LsimParams &p, const float *mrec, const NBatch &nb, int m,
+                                                 float *row, int lane) {
   const int L = p.signal_length, NT = p.n_ticks;
-  const float f = h.frac, f1 = 1.f - h.frac;
-  const int cb = h.cb;
-  float dV[kChunks], dG[kChunks];
+  __syncwarp();
+  for (int j = 0; j < m; j += 4) {
+    float u[4][kChunks];
+    int cb[4], rl[4];
 #pragma unroll
-  for (int m = 0; m < kChunks; ++m) {
-    const int k = m * kWarp + lane;
-    const int ca = cb + k + 1, cbb = cb + k + 2;
-    const float gA = (k < L && ca >= 2 && ca <= NT - 1) ? grow[ca] : 0.f;
-    const float gB = (k < L && cbb >= 2 && cbb <= NT - 1) ? grow[cbb] : 0.f;
-    dV[m] = gA * f + gB * f1;
-    dG[m] = gA - gB;
+    for (int q = 0; q < 4; ++q) {
+      const bool ok = j + q < m;
+      cb[q] = nb.cb[j + q];
+      rl[q] = owner_rl(cb[q], lane);
+      const float *src = mrec + (size_t)(ok ? nb.row[j + q] : 0) * kRecFloats + rl[q];
+#pragma unroll
+      for (int c = 0; c < kChunks; ++c) u[q][c] = ok ? src[c * kWarp] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (j + q < m) window_apply(u[q], cb[q], rl[q], nb.frac[j + q], L, NT, row, lane);
   }
-  float acc_ne = 0.f, acc_sig = 0.f, acc_a = 0.f, acc_b = 0.f, acc_c = 0.f, acc_fr = 0.f;
-  for (int e = 0; e < h.n; ++e) {
-    const float4 *src = tab.wmp + (size_t)ms.off[e] * L;
-    const float W = ms.W[e], dW = ms.dW[e];
+  __syncwarp();
+}
+
+// Adjoint of m batched records given the waveform cotangent grow[col]:
+// each record is replaced by the cotangent of its samples (rec[0]: the
+// boundary correction, rec[1 + k]: V[k]); the sub-tick-fraction part goes
+// straight to dL/d eField through d t0/d eField.
+__device__ __forceinline__ void main_rec_backward(const LsimParams &p, float *mrec, const NBatch &nb, int m,
+                                                  const float *grow, Theta &th, int lane) {
+  const int L = p.signal_length, NT = p.n_ticks;
+  const float inv_ts = 1.f / p.t_sampling;
+  __syncwarp();
+  for (int j = 0; j < m; ++j) {
+    float *rec = mrec + (size_t)nb.row[j] * kRecFloats;
+    const int cb = nb.cb[j];
+    const float f = nb.frac[j], f1 = 1.f - f;
+    const bool interior = cb >= 1 && cb + L + 1 <= NT - 2;
+    float dfr = 0.f, dcorr = 0.f;
 #pragma unroll
-    for (int m = 0; m < kChunks; ++m) {
-      const int k = m * kWarp + lane;
-      if (k < L) {
-        const float4 t = __ldg(src + k);
-        const float B = (t.y * h.qb + t.x * h.qa) + t.z * h.qc;
-        const float dVB = dV[m] * B;
-        acc_ne += W * dVB;
-        acc_sig += dW * dVB;
-        const float dVW = dV[m] * W;
-        acc_a += dVW * t.x;
-        acc_b += dVW * t.y;
-        acc_c += dVW * t.z;
-        acc_fr += (W * B) * dG[m];
+    for (int c = 0; c < kChunks; ++c) {
+      const int idx = lane + c * kWarp;     // sample idx - 1 lands on columns cb + idx (x frac), cb + idx + 1
+      if (idx <= L) {
+        const float u = rec[idx];
+        const int c1 = cb + idx;
+        float gA, gB;
+        if (interior) {
+          gA = grow[c1];
+          gB = grow[c1 + 1];
+        } else {
+          const int lo = idx == 0 ? 1 : 2, hi = idx == 0 ? NT - 2 : NT - 1;
+          gA = (c1 >= lo && c1 <= hi) ? grow[c1] : 0.f;
+          gB = (c1 + 1 >= lo && c1 + 1 <= hi) ? grow[c1 + 1] : 0.f;
+        }
+        const float du = gA * f + gB * f1;
+        rec[idx] = du;
+        dfr += u * (gA - gB);
+        if (idx == 0) dcorr = du;
       }
     }
+    if (lane == 0) dfr += dcorr * nb.D[j];
+    th.v[2] += dfr * inv_ts * nb.dt0[j];
   }
-  // boundary corrections: lane e owns sub-position entry e
-  if (lane < h.n) {
-    const float gc0 = (cb >= 1 && cb <= NT - 2) ? grow[cb] : 0.f;
-    const float gc1 = (cb + 1 >= 1 && cb + 1 <= NT - 2) ? grow[cb + 1] : 0.f;
-    const float dcorr = gc0 * f + gc1 * f1;
-    const float W = ms.W[lane], D = ms.D[lane];
-    acc_ne += dcorr * W * D;
-    acc_sig += dcorr * ms.dW[lane] * D;
-    acc_fr += W * (dcorr * ms.dl[lane] + D * (gc0 - gc1));
-  }
-  // q_uv = ne * W: all terms but acc_ne carry a factor ne
-  const float ne = h.ne;
-  const float sig = acc_sig * ne;
-  const float lsum = (acc_a * a.dqa + acc_b * a.dqb + acc_c * a.dqc) * ne;
-  const float dt = acc_fr * ne / p.t_sampling;
-  th.v[0] += acc_ne * a.dne[0];
-  th.v[1] += acc_ne * a.dne[1];
-  th.v[2] += acc_ne * a.dne[2] + sig * a.dsig[0] + lsum * a.dld[0] + dt * a.dt0;
-  th.v[3] += acc_ne * a.dne[3];
-  th.v[5] += lsum * a.dld[1];
-  th.v[6] += sig * a.dsig[1];
-  th.v[7] += acc_ne * a.dne[4];
   __syncwarp();
 }
 
@@ -484,14 +415,12 @@ struct __align__(16) WarpSmem {
   float buf[kRowFloats];
   ListSmem list;
   NBatch nb;
-  MainSmem ms;
 };
 template <>
 struct __align__(16) WarpSmem<true> {
   float buf[kRowFloats];
   ListSmem list;
   NBatch nb;
-  MainSmem ms;
   float gint[LSIM_MAX_HITS];
   FeeState fee;
 };
@@ -500,66 +429,30 @@ static_assert(sizeof(WarpSmem<true>) % 16 == 0, "per-warp shared memory must kee
 static_assert(offsetof(WarpSmem<false>, buf) == 0 && offsetof(WarpSmem<true>, buf) == 0, "row first");
 static_assert((kRowPad + 1) % 4 == 0 && kRowFloats % 4 == 0, "output column 1 of the row must be 16-byte aligned");
 
-// Whether any of the kMaxTran bins around bin b (b - 2 .. b + 2) lies in
-// the pixel at offset d from the pixel of b (the test of axis_weights).
-__device__ __forceinline__ bool axis_reaches(int b, int nb, int d) {
-  const int pp = ifloordiv(b, nb);
-  return ifloordiv(b - kMaxTran / 2, nb) - pp <= d && d <= ifloordiv(b + kMaxTran / 2, nb) - pp;
-}
-
-// Walk the segments of the 3x3 slots; run fn on those with bins on the
-// pixel.  32 candidates are tested at once (charge and bin offsets), so
-// only segments that contribute reach the per-contribution setup.
-template <typename F>
-__device__ __forceinline__ void for_each_main(const LsimParams &p, const Workspace &w, const ListSmem &ls, int lane,
-                                              F &&fn) {
-  const int nbp = p.nb_bins_per_pixel;
-  for (int e = 0; e < ls.n; ++e) {
-    const int dxy = ls.dxy[e];
-    const int dx = (dxy & 0xff) - 16, dy = ((dxy >> 8) & 0xff) - 16;
-    if (dx < -1 || dx > 1 || dy < -1 || dy > 1) continue;
-    const int o = ls.off[e], c = ls.cnt[e];
-    for (int j0 = 0; j0 < c; j0 += kWarp) {
-      int mine = -1;
-      bool hit = false;
-      if (j0 + lane < c) {
-        mine = __ldg(w.seg_list + o + j0 + lane);
-        const SegFwd &f = w.segf[mine];
-        hit = __ldg(&f.ne) != 0.f && axis_reaches(__ldg(&f.bx), nbp, dx) && axis_reaches(__ldg(&f.by), nbp, dy);
-      }
-      unsigned bal = __ballot_sync(0xffffffffu, hit);
-      while (bal) {
-        const int jj = __ffs(bal) - 1;
-        bal &= bal - 1u;
-        fn(__shfl_sync(0xffffffffu, mine, jj), dx, dy);
-      }
-    }
-  }
-}
-
 // ---------------------------------------------------------------- per pixel
 
-// Neighbourhood slot list of a pixel (compacted, fixed order) with the
-// prefix count of neighbour contributions.
+// Neighbourhood slot list of a pixel (compacted, fixed order) over the
+// (2h+1)^2 slots around it, with the prefix count of neighbour
+// contributions (slots within the neighbour radius n, centre excluded).
 __device__ __forceinline__ void build_list(const Grid &g, const int32_t *__restrict__ cnt,
                                            const int32_t *__restrict__ off, int64_t slot, ListSmem &ls, int lane) {
-  const int D = 2 * g.n + 1;
+  const int D = 2 * g.h + 1;
   int base = 0, nbase = 0;
   for (int i0 = 0; i0 < D * D; i0 += kWarp) {
     const int idx = i0 + lane;
     int c = 0, o = 0, dxy = 0;
-    bool centre = false;
+    bool neigh = false;
     if (idx < D * D) {
-      const int dx = idx / D - g.n, dy = idx % D - g.n;
+      const int dx = idx / D - g.h, dy = idx % D - g.h;
       const int64_t q = slot - (int64_t)dy * g.nxe - dx;
       c = __ldg(cnt + q);
       if (c > 0) o = __ldg(off + q);
       dxy = (dx + 16) | ((dy + 16) << 8);
-      centre = (dx == 0 && dy == 0);
+      neigh = !(dx == 0 && dy == 0) && abs(dx) <= g.n && abs(dy) <= g.n;
     }
     const bool has = c > 0;
     const unsigned bal = __ballot_sync(0xffffffffu, has);
-    const int nc = (has && !centre) ? c : 0;
+    const int nc = (has && neigh) ? c : 0;
     int incl = nc;   // inclusive scan of neighbour counts over the compacted entries
     for (int o2 = 1; o2 < kWarp; o2 <<= 1) {
       const int y = __shfl_up_sync(0xffffffffu, incl, o2);
@@ -587,7 +480,7 @@ __device__ __forceinline__ int32_t slot_pid(const LsimParams &p, const Grid &g, 
   const int64_t rem = slot - ev * g.event_stride;
   const int plane = (int)(rem / g.plane_stride);
   const int64_t inplane = rem % g.plane_stride;
-  const int py = (int)(inplane / g.nxe) - g.n, px = (int)(inplane % g.nxe) - g.n;
+  const int py = (int)(inplane / g.nxe) - g.h, px = (int)(inplane % g.nxe) - g.h;
   return pixel2id(p, px, py, plane, (int)ev - 1);
 }
 
@@ -615,10 +508,8 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 3) k_lut_pixels(AccumArgs a
     build_list(a.g, a.w.cnt, a.w.off, slot, sm.list, lane);
     // ---- forward: neighbour parts, then main-bin parts
     neigh_forward(p, a.tab, a.w, sm.list, sm.nb, row, lane);
-    for_each_main(p, a.w, sm.list, lane, [&](int s, int dx, int dy) {
-      MainHead h;
-      if (main_setup<false>(p, a.tab, a.w, s, dx, dy, h, sm.ms, lane)) main_forward_one(p, a.tab, h, sm.ms, row, lane);
-    });
+    main_batches<false>(p, a.w, sm.list, sm.nb, lane,
+                        [&](int m) { main_rec_forward(p, a.w.mrec, sm.nb, m, row, lane); });
     __syncwarp();
     if (MODE == kModeWfs) {
       float4 *dst = reinterpret_cast<float4 *>(a.wfs + (a.row_offset + r) * (int64_t)T);
@@ -673,11 +564,8 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 3) k_lut_pixels(AccumArgs a
 #pragma unroll
       for (int i = 0; i < LSIM_NPARAM; ++i) th.v[i] = 0.f;
       neigh_backward(p, a.tab, a.w, sm.list, sm.nb, row, th, lane);
-      for_each_main(p, a.w, sm.list, lane, [&](int s, int dx, int dy) {
-        MainHead h;
-        if (main_setup<true>(p, a.tab, a.w, s, dx, dy, h, sm.ms, lane))
-          main_backward_one(p, a.tab, h, sm.ms, a.w.sega[s], row, th, lane);
-      });
+      main_batches<true>(p, a.w, sm.list, sm.nb, lane,
+                         [&](int m) { main_rec_backward(p, a.w.mrec, sm.nb, m, row, th, lane); });
       // per-pixel record [loss, dL/dtheta]
 #pragma unroll
       for (int i = 0; i < LSIM_NPARAM; ++i) th.v[i] = warp_sum(th.v[i]);
@@ -696,15 +584,19 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 3) k_lut_pixels(AccumArgs a
 
 constexpr int kRedThreads = 256;
 constexpr int kPixBlocks = 1024;     // reduction blocks over pixel records
+constexpr int kMainBlocks = 256;     // reduction blocks over main-bin adjoint warps
 constexpr int kTgtBlocks = 256;      // reduction blocks over target-only rows
+static_assert(kPixBlocks + kMainBlocks + kTgtBlocks <= kRedSlots, "reduction partials");
 
-// Fixed-order float64 sum of the per-pixel records: block b reduces a
-// contiguous chunk; the chunking depends only on n_valid.
-__global__ void k_reduce_pixels(const float *__restrict__ pix, const LsimCounts *counts, double *partials) {
+// Fixed-order float64 sum of per-pixel (or per-warp) records [loss, 8
+// gradient terms]: block b reduces a contiguous chunk; the chunking depends
+// only on the record count (n_fixed, or the valid-pixel count when < 0).
+__global__ void k_reduce_records(const float *__restrict__ pix, int64_t n_fixed, const LsimCounts *counts,
+                                 double *partials) {
   __shared__ double sh[kRedThreads];
-  const int n = counts->n_valid;
-  const int64_t chunk = ((int64_t)n + gridDim.x - 1) / gridDim.x;
-  const int64_t lo = blockIdx.x * chunk, hi = min((int64_t)n, lo + chunk);
+  const int64_t n = n_fixed >= 0 ? n_fixed : counts->n_valid;
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
   for (int q = 0; q <= LSIM_NPARAM; ++q) {
     double s = 0.0;
     for (int64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) s += (double)pix[i * kPixRec + q];
@@ -752,12 +644,12 @@ __global__ void k_target_only(AccumArgs a, double *partials) {
   if (threadIdx.x == 0) partials[(size_t)blockIdx.x * 16] = sh[0];
 }
 
-__global__ void k_grad_finalize(const double *pix_partials, int n_pix_blocks, const double *tgt_partials,
+__global__ void k_grad_finalize(const double *partials, int n_rec_blocks, const double *tgt_partials,
                                 int n_tgt_blocks, float *loss_out, float *grad_out) {
   const int q = threadIdx.x;   // 0: loss, 1..8: gradient
   if (q > LSIM_NPARAM) return;
   double s = 0.0;
-  for (int b = 0; b < n_pix_blocks; ++b) s += pix_partials[(size_t)b * 16 + q];
+  for (int b = 0; b < n_rec_blocks; ++b) s += partials[(size_t)b * 16 + q];
   if (q == 0) {
     for (int b = 0; b < n_tgt_blocks; ++b) s += tgt_partials[(size_t)b * 16];
     if (loss_out) loss_out[0] = (float)s;
@@ -805,24 +697,31 @@ int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st) {
   const int need = a.p.nb_bins_per_pixel * a.p.n_neighbors + a.p.nb_bins_per_pixel / 2;
   if (a.p.lut_nx < need || a.p.lut_ny < need || a.p.lut_nx < kMainSub || a.p.lut_ny < kMainSub)
     return LSIM_ERR_UNSUPPORTED;
+  if (a.n_rows > 0x7fffffff / kRecPerSeg) return LSIM_ERR_UNSUPPORTED;   // record indices are int32
+  int rc = run_main_records(a, st);
+  if (rc != LSIM_OK) return rc;
   switch (mode) {
     case kModeWfs: return launch_mode<kModeWfs>(a, st);
     case kModeAdc: return launch_mode<kModeAdc>(a, st);
-    case kModeGrad: return launch_mode<kModeGrad>(a, st);
+    case kModeGrad:
+      rc = launch_mode<kModeGrad>(a, st);
+      return rc != LSIM_OK ? rc : run_main_adjoint(a, st);
   }
   return LSIM_ERR_INVALID;
 }
 
 int run_grad_finalize(const AccumArgs &a, float *loss_out, float *grad_out, cudaStream_t st) {
-  double *pix_partials = a.w.red_partials;
-  double *tgt_partials = a.w.red_partials + (size_t)kPixBlocks * 16;
-  k_reduce_pixels<<<kPixBlocks, kRedThreads, 0, st>>>(a.w.pix_out, a.w.counts, pix_partials);
+  double *rec_partials = a.w.red_partials;
+  double *tgt_partials = a.w.red_partials + (size_t)(kPixBlocks + kMainBlocks) * 16;
+  k_reduce_records<<<kPixBlocks, kRedThreads, 0, st>>>(a.w.pix_out, -1, a.w.counts, rec_partials);
+  k_reduce_records<<<kMainBlocks, kRedThreads, 0, st>>>(a.w.main_out, kMainWarps, a.w.counts,
+                                                        rec_partials + (size_t)kPixBlocks * 16);
   int tb = 0;
   if (!a.g_adc && a.n_tgt > 0) {
     tb = kTgtBlocks;
     k_target_only<<<tb, kRedThreads, 0, st>>>(a, tgt_partials);
   }
-  k_grad_finalize<<<1, 32, 0, st>>>(pix_partials, kPixBlocks, tgt_partials, tb, loss_out, grad_out);
+  k_grad_finalize<<<1, 32, 0, st>>>(rec_partials, kPixBlocks + kMainBlocks, tgt_partials, tb, loss_out, grad_out);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 

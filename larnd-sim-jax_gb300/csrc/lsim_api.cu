@@ -164,6 +164,7 @@ static AccumArgs make_args(const LsimParams *p, const void *tables, const void *
   if (tables) a.tab = carve_tables(tables, *p);
   a.w = carve_workspace(const_cast<void *>(ws), *p, n_rows, n_events);
   a.g = make_grid(*p, n_events);
+  a.n_rows = n_rows;
   return a;
 }
 

@@ -61,20 +61,34 @@ struct __align__(16) SegPar {
 // --------------------------------------------------------------- layout
 
 struct Grid {
-  int nxe, nye, ntpc, n;       // extended pixel grid per (event, plane)
+  int nxe, nye, ntpc;          // extended pixel grid per (event, plane)
+  int n;                       // neighbour radius (number_pix_neighbors)
+  int h;                       // halo = max(n, 1): main bins reach the 3x3 pixels around a segment's pixel
   int64_t plane_stride, event_stride, G;
 };
 
 __host__ __device__ inline Grid make_grid(const LsimParams &p, int32_t n_events) {
   Grid g;
   g.n = p.n_neighbors;
-  g.nxe = p.n_pixels_x + 2 * g.n;
-  g.nye = p.n_pixels_y + 2 * g.n;
+  g.h = g.n > 1 ? g.n : 1;
+  g.nxe = p.n_pixels_x + 2 * g.h;
+  g.nye = p.n_pixels_y + 2 * g.h;
   g.ntpc = p.n_tpc;
   g.plane_stride = (int64_t)g.nxe * g.nye;
   g.event_stride = g.plane_stride * g.ntpc;
   g.G = g.event_stride * (int64_t)(n_events + 1);   // events -1 .. n_events-1
   return g;
+}
+
+// Whether grid slot t is a simulated pixel: it holds segments, lies inside
+// the detector (not in the halo) and belongs to an event >= 0.
+__device__ __forceinline__ bool slot_is_pixel(const Grid &g, const int32_t *cnt, int64_t t) {
+  if (t < 0 || t >= g.G || cnt[t] <= 0) return false;
+  const int64_t ev = t / g.event_stride;
+  if (ev == 0) return false;
+  const int64_t inplane = (t - ev * g.event_stride) % g.plane_stride;
+  const int pye = (int)(inplane / g.nxe), pxe = (int)(inplane % g.nxe);
+  return pxe >= g.h && pxe < g.nxe - g.h && pye >= g.h && pye < g.nye - g.h;
 }
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -91,11 +105,16 @@ struct Workspace {
   int32_t *scan_blocks;     // 3 ints per scan block (+1 block)
   float *pix_out;           // per valid pixel: [loss, 8 gradient terms] (kPixRec floats)
   double *red_partials;     // fixed-order reduction partials (kRedSlots * 16 doubles)
+  float *mrec;              // main-bin records: kMainRecPerSeg per segment, kMainRecFloats each
+  float *main_out;          // per main-adjoint warp: [0, 8 gradient terms] (kPixRec floats)
   size_t bytes;
 };
 
 constexpr int kPixRec = 12;      // floats per per-pixel record (loss + 8 grads, padded)
-constexpr int kRedSlots = 2048;  // reduction blocks (pixels + target-only)
+constexpr int kRedSlots = 4096;  // reduction blocks (pixels + main-bin warps + target-only)
+constexpr int kMainWarps = 8192; // warps of the segment-major main-bin kernels
+constexpr int kMainRecPerSeg = 4;      // a segment's main bins cover at most 2 x 2 pixels
+constexpr int kMainRecFloats = 164;    // window of 160 samples + d(corr)/d(frac), padded to 16 bytes
 
 inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows, int32_t n_events) {
   Grid g = make_grid(p, n_events);
@@ -117,6 +136,8 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   size_t o_scan = take(3 * 4 * (size_t)nscan);
   size_t o_pix = take(4 * (size_t)kPixRec * (size_t)n_rows);
   size_t o_red = take(8 * (size_t)kRedSlots * 16);
+  size_t o_mrec = take(4 * (size_t)kMainRecFloats * kMainRecPerSeg * (size_t)n_rows);
+  size_t o_mout = take(4 * (size_t)kPixRec * kMainWarps);
   Workspace w;
   char *b = (char *)base;
   w.counts = (LsimCounts *)(b + o_counts);
@@ -134,6 +155,8 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   w.scan_blocks = (int32_t *)(b + o_scan);
   w.pix_out = (float *)(b + o_pix);
   w.red_partials = (double *)(b + o_red);
+  w.mrec = (float *)(b + o_mrec);
+  w.main_out = (float *)(b + o_mout);
   w.bytes = off;
   return w;
 }

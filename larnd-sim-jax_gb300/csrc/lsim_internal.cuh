@@ -15,6 +15,7 @@ int run_fill_unique(const LsimParams &p, const Workspace &w, const Grid &g, int6
 enum AccumMode { kModeWfs = 0, kModeAdc = 1, kModeGrad = 2 };
 struct AccumArgs {
   LsimParams p;
+  int64_t n_rows;           // segments (rows of the track table)
   Tables tab;
   Workspace w;
   Grid g;
@@ -30,6 +31,10 @@ struct AccumArgs {
 };
 int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st);
 int run_grad_finalize(const AccumArgs &a, float *loss_out, float *grad_out, cudaStream_t st);
+
+// lsim_main.cu: segment-major main-bin records and their adjoint
+int run_main_records(const AccumArgs &a, cudaStream_t st);
+int run_main_adjoint(const AccumArgs &a, cudaStream_t st);
 
 int run_param_accum(const LsimParams &p, const Workspace &w, const Grid &g, int32_t n_valid, int64_t row_offset,
                     float *wfs, cudaStream_t st);

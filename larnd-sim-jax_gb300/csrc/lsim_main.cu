@@ -1,0 +1,242 @@
+// Main-bin parts of LUT mode, segment-major.
+//
+// A segment's 5 x 5 transverse-diffusion bins cover at most 2 x 2 pixels.
+// For each covered pixel the window it adds is
+//   V[k] = n_e * sum over the bins (i, j) on that pixel of
+//          ex_i ey_j * (a T_{t-1} + b T_t + c T_{t+1})[cx_i, cy_j, Nt - L + k]
+// (main_vals_2d, sim_jax.py:186-192) with the quadratic long-diffusion
+// interpolation weights (a, b, c) (sim_jax.py:162-168) and the
+// cumulative-sum boundary term (sim_jax.py:237-241).  Bins of one pixel that share a LUT sub-position
+// (u, v) are grouped, W_uv = sum ex_i * sum ey_j, so each window reads at
+// most 25 LUT rows.
+//
+// k_main_records computes V and the boundary term once per (segment,
+// pixel) and stores them as a record; the pixel-major accumulation adds the
+// record like a neighbour part.  After the pixel-major adjoint has replaced
+// the record by its cotangent, k_main_adjoint projects it back onto n_e,
+// sigma_T and (a, b, c) and accumulates dL/dtheta per warp.  One warp owns
+// one segment at a time; warps own fixed contiguous segment ranges, so the
+// per-warp gradient records and their reduction order are fixed.
+#include "lsim_internal.cuh"
+#include "lsim_bins.cuh"
+#include "lsim_fee.cuh"
+
+namespace lsim {
+
+constexpr int kMainBlockWarps = 4;
+
+// Grouped LUT sub-positions of one (segment, pixel) pair: row offset
+// (tidx*5 + u)*5 + v into the window tables, W, dW/dsigma_T, the
+// cumulative-sum term D and dD/dfrac.
+struct MainSmem {
+  int off[kMainSub * kMainSub];
+  float W[kMainSub * kMainSub], dW[kMainSub * kMainSub];
+  float D[kMainSub * kMainSub], dl[kMainSub * kMainSub];
+};
+
+// Lane l < 25 owns sub-position (u, v) = (l / 5, l % 5); the owners of
+// sub-positions with bins on the pixel are compacted in (u, v) order.
+// Returns the entry count; *wd and *wdl are sum W D and sum W dD/dfrac.
+template <bool GRAD>
+__device__ __forceinline__ int main_entries(const LsimParams &p, const Tables &tab, const SegFwd &f,
+                                            const SegAdj *a, int dx, int dy, MainSmem &ms, float *wd, float *wdl,
+                                            int lane) {
+  const int nbp = p.nb_bins_per_pixel;
+  float ex[kMaxTran], ey[kMaxTran], dex[kMaxTran], dey[kMaxTran];
+#pragma unroll
+  for (int i = 0; i < kMaxTran; ++i) {
+    ex[i] = f.ex[i];
+    ey[i] = f.ey[i];
+    dex[i] = GRAD ? a->dex[i] : 0.f;
+    dey[i] = GRAD ? a->dey[i] : 0.f;
+  }
+  float Xw[kMainSub], Yw[kMainSub], dXw[kMainSub], dYw[kMainSub];
+  unsigned um, vm;
+  axis_weights(ex, dex, f.bx, nbp, dx, Xw, dXw, &um);
+  axis_weights(ey, dey, f.by, nbp, dy, Yw, dYw, &vm);
+  const int u = lane / kMainSub, v = lane % kMainSub;
+  const bool mine = lane < kMainSub * kMainSub && ((um >> u) & 1u) && ((vm >> v) & 1u);
+  float xw = 0.f, yw = 0.f, dxw = 0.f, dyw = 0.f;
+#pragma unroll
+  for (int q = 0; q < kMainSub; ++q) {
+    if (q == u) { xw = Xw[q]; dxw = dXw[q]; }
+    if (q == v) { yw = Yw[q]; dyw = dYw[q]; }
+  }
+  const unsigned bal = __ballot_sync(0xffffffffu, mine);
+  float s_wd = 0.f, s_wdl = 0.f;
+  if (mine) {
+    const int pos = __popc(bal & ((1u << lane) - 1u));
+    const int off = (f.tidx * kMainSub + u) * kMainSub + v;
+    float dl;
+    const float D = cum_terms(tab.cm + (size_t)off * p.lut_nt, f.cath, p.lut_nt, p.signal_length, f.frac, &dl);
+    const float W = xw * yw;
+    ms.off[pos] = off;
+    ms.W[pos] = W;
+    ms.dW[pos] = dxw * yw + xw * dyw;
+    ms.D[pos] = D;
+    ms.dl[pos] = dl;
+    s_wd = W * D;
+    s_wdl = W * dl;
+  }
+  *wd = warp_sum(s_wd);
+  *wdl = warp_sum(s_wdl);
+  __syncwarp();
+  return __popc(bal);
+}
+
+__device__ __forceinline__ void warp_range(int64_t n_rows, int64_t *s0, int64_t *s1) {
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int64_t nw = (int64_t)gridDim.x * blockDim.x / kWarp;
+  const int64_t chunk = (n_rows + nw - 1) / nw;
+  *s0 = gw * chunk;
+  *s1 = min(n_rows, *s0 + chunk);
+}
+
+__global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_records(LsimParams p, Tables tab, Workspace w, Grid g,
+                                                                           int64_t n_rows) {
+  __shared__ MainSmem sms[kMainBlockWarps];
+  const int lane = threadIdx.x % kWarp;
+  MainSmem &ms = sms[threadIdx.x / kWarp];
+  const int L = p.signal_length, nbp = p.nb_bins_per_pixel;
+  int64_t s0, s1;
+  warp_range(n_rows, &s0, &s1);
+  for (int64_t s = s0; s < s1; ++s) {
+    const SegFwd &f = w.segf[s];
+    const float ne = f.ne;
+    const int32_t key = w.key[s];
+    if (ne == 0.f || key < 0) continue;
+    const float qa = f.qa, qb = f.qb, qc = f.qc;
+    int lx, hx, ly, hy;
+    axis_range(f.bx, nbp, &lx, &hx);
+    axis_range(f.by, nbp, &ly, &hy);
+    for (int dx = lx; dx <= hx; ++dx)
+      for (int dy = ly; dy <= hy; ++dy) {
+        // records of pixels that are not simulated are never read (the
+        // reference drops main bins outside unique_pixels, sim_jax.py:152-154)
+        if (!slot_is_pixel(g, w.cnt, (int64_t)key + (int64_t)dy * g.nxe + dx)) continue;
+        float wd, wdl;
+        const int n = main_entries<false>(p, tab, f, nullptr, dx, dy, ms, &wd, &wdl, lane);
+        float acc[kChunks];
+#pragma unroll
+        for (int j = 0; j < kChunks; ++j) acc[j] = 0.f;
+        for (int e = 0; e < n; ++e) {
+          const float4 *src = tab.wmp + (size_t)ms.off[e] * L;   // record index idx holds sample idx - 1
+          const float W = ms.W[e];
+#pragma unroll
+          for (int j = 0; j < kChunks; ++j) {
+            const int idx = lane + j * kWarp;
+            if (idx >= 1 && idx <= L) {
+              const float4 t = __ldg(src + idx - 1);
+              acc[j] += W * ((t.y * qb + t.x * qa) + t.z * qc);
+            }
+          }
+        }
+        float *rec = w.mrec + ((size_t)s * kRecPerSeg + (dx - lx) * 2 + (dy - ly)) * kRecFloats;
+#pragma unroll
+        for (int j = 0; j < kChunks; ++j) {
+          const int idx = lane + j * kWarp;
+          rec[idx] = idx == 0 ? wd * ne : (idx <= L ? acc[j] * ne : 0.f);
+        }
+        if (lane == 0) rec[kRecDl] = wdl * ne;
+        __syncwarp();
+      }
+  }
+}
+
+__global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_adjoint(LsimParams p, Tables tab, Workspace w, Grid g,
+                                                                           int64_t n_rows) {
+  __shared__ MainSmem sms[kMainBlockWarps];
+  const int lane = threadIdx.x % kWarp;
+  MainSmem &ms = sms[threadIdx.x / kWarp];
+  const int L = p.signal_length, nbp = p.nb_bins_per_pixel;
+  float th[LSIM_NPARAM];
+#pragma unroll
+  for (int i = 0; i < LSIM_NPARAM; ++i) th[i] = 0.f;
+  int64_t s0, s1;
+  warp_range(n_rows, &s0, &s1);
+  for (int64_t s = s0; s < s1; ++s) {
+    const SegFwd &f = w.segf[s];
+    const float ne = f.ne;
+    const int32_t key = w.key[s];
+    if (ne == 0.f || key < 0) continue;
+    const SegAdj &a = w.sega[s];
+    const float qa = f.qa, qb = f.qb, qc = f.qc;
+    float acc_ne = 0.f, acc_sig = 0.f, acc_a = 0.f, acc_b = 0.f, acc_c = 0.f;
+    int lx, hx, ly, hy;
+    axis_range(f.bx, nbp, &lx, &hx);
+    axis_range(f.by, nbp, &ly, &hy);
+    for (int dx = lx; dx <= hx; ++dx)
+      for (int dy = ly; dy <= hy; ++dy) {
+        // records of pixels that are not simulated are never read (the
+        // reference drops main bins outside unique_pixels, sim_jax.py:152-154)
+        if (!slot_is_pixel(g, w.cnt, (int64_t)key + (int64_t)dy * g.nxe + dx)) continue;
+        float wd, wdl;
+        const int n = main_entries<true>(p, tab, f, &a, dx, dy, ms, &wd, &wdl, lane);
+        const float *rec = w.mrec + ((size_t)s * kRecPerSeg + (dx - lx) * 2 + (dy - ly)) * kRecFloats;
+        float d[kChunks];
+#pragma unroll
+        for (int j = 0; j < kChunks; ++j) {
+          const int idx = lane + j * kWarp;
+          d[j] = (idx >= 1 && idx <= L) ? rec[idx] : 0.f;
+        }
+        const float dcorr = rec[0];
+        for (int e = 0; e < n; ++e) {
+          const float4 *src = tab.wmp + (size_t)ms.off[e] * L;
+          const float W = ms.W[e], dW = ms.dW[e];
+#pragma unroll
+          for (int j = 0; j < kChunks; ++j) {
+            const int idx = lane + j * kWarp;
+            if (idx >= 1 && idx <= L) {
+              const float4 t = __ldg(src + idx - 1);
+              const float B = (t.y * qb + t.x * qa) + t.z * qc;
+              const float dVB = d[j] * B;
+              acc_ne += W * dVB;
+              acc_sig += dW * dVB;
+              const float dVW = d[j] * W;
+              acc_a += dVW * t.x;
+              acc_b += dVW * t.y;
+              acc_c += dVW * t.z;
+            }
+          }
+        }
+        if (lane < n) {
+          acc_ne += dcorr * ms.W[lane] * ms.D[lane];
+          acc_sig += dcorr * ms.dW[lane] * ms.D[lane];
+        }
+        __syncwarp();
+      }
+    // V and the boundary term carry n_e * W(sigma_T) * (a, b, c)(longdiff)
+    const float sig = acc_sig * ne;
+    const float lsum = (acc_a * a.dqa + acc_b * a.dqb + acc_c * a.dqc) * ne;
+    th[0] += acc_ne * a.dne[0];
+    th[1] += acc_ne * a.dne[1];
+    th[2] += acc_ne * a.dne[2] + sig * a.dsig[0] + lsum * a.dld[0];
+    th[3] += acc_ne * a.dne[3];
+    th[5] += lsum * a.dld[1];
+    th[6] += sig * a.dsig[1];
+    th[7] += acc_ne * a.dne[4];
+  }
+#pragma unroll
+  for (int i = 0; i < LSIM_NPARAM; ++i) th[i] = warp_sum(th[i]);
+  if (lane == 0) {
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    float *dst = w.main_out + gw * kPixRec;
+    dst[0] = 0.f;
+#pragma unroll
+    for (int i = 0; i < LSIM_NPARAM; ++i) dst[1 + i] = th[i];
+  }
+}
+
+int run_main_records(const AccumArgs &a, cudaStream_t st) {
+  if (a.n_rows <= 0) return LSIM_OK;
+  k_main_records<<<kMainWarps / kMainBlockWarps, kMainBlockWarps * kWarp, 0, st>>>(a.p, a.tab, a.w, a.g, a.n_rows);
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
+int run_main_adjoint(const AccumArgs &a, cudaStream_t st) {
+  // every warp writes its record, also when it owns no segment
+  k_main_adjoint<<<kMainWarps / kMainBlockWarps, kMainBlockWarps * kWarp, 0, st>>>(a.p, a.tab, a.w, a.g, a.n_rows);
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
+}  // namespace lsim

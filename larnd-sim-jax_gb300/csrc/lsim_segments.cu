@@ -217,12 +217,12 @@ __global__ void k_segments_lut(LsimParams p, LsimFieldMap f, const float *__rest
   w.pid[s] = pid;
   if (pid == -1) atomicExch(&w.counts->any_m1, 1);
   int32_t key = -1;
-  const int n = g.n;
+  const int h = g.h;
   if (t.event >= 0) {
-    if (ppx >= -n && ppx < p.n_pixels_x + n && ppy >= -n && ppy < p.n_pixels_y + n)
-      key = (int32_t)((t.event + 1) * g.event_stride + plane * g.plane_stride + (int64_t)(ppy + n) * g.nxe + (ppx + n));
+    if (ppx >= -h && ppx < p.n_pixels_x + h && ppy >= -h && ppy < p.n_pixels_y + h)
+      key = (int32_t)((t.event + 1) * g.event_stride + plane * g.plane_stride + (int64_t)(ppy + h) * g.nxe + (ppx + h));
   } else if (pid != -1) {
-    key = (int32_t)(plane * g.plane_stride + (int64_t)(ppy + n) * g.nxe + (ppx + n));
+    key = (int32_t)(plane * g.plane_stride + (int64_t)(ppy + h) * g.nxe + (ppx + h));
   }
   w.key[s] = key;
   if (key >= 0) atomicAdd(&w.cnt[key], 1);
@@ -287,7 +287,8 @@ __global__ void k_segments_param(LsimParams p, LsimFieldMap f, const float *__re
   if (pid == -1) atomicExch(&w.counts->any_m1, 1);
   int32_t key = -1;
   if (pid != -1)
-    key = (int32_t)((t.event + 1) * g.event_stride + plane * g.plane_stride + (int64_t)py * g.nxe + px);
+    key = (int32_t)((t.event + 1) * g.event_stride + plane * g.plane_stride + (int64_t)(py + g.h) * g.nxe +
+                    (px + g.h));
   w.key[s] = key;
   if (key >= 0) atomicAdd(&w.cnt[key], 1);
 }
@@ -301,7 +302,7 @@ __device__ __forceinline__ void slot_flags(const Grid &g, int64_t slot, int c, i
   int64_t rem = slot - ev * g.event_stride;
   int64_t inplane = rem % g.plane_stride;
   int pye = (int)(inplane / g.nxe), pxe = (int)(inplane % g.nxe);
-  bool interior = pxe >= g.n && pxe < g.nxe - g.n && pye >= g.n && pye < g.nye - g.n;
+  bool interior = pxe >= g.h && pxe < g.nxe - g.h && pye >= g.h && pye < g.nye - g.h;
   if (!interior) return;
   if (ev == 0) *fe = 1; else *fv = 1;
 }
@@ -465,7 +466,7 @@ __global__ void k_fill_unique(LsimParams p, Grid g, const int32_t *__restrict__ 
     int64_t rem = slot - ev * g.event_stride;
     int plane = (int)(rem / g.plane_stride);
     int64_t inplane = rem % g.plane_stride;
-    int py = (int)(inplane / g.nxe) - g.n, px = (int)(inplane % g.nxe) - g.n;
+    int py = (int)(inplane / g.nxe) - g.h, px = (int)(inplane % g.nxe) - g.h;
     pid = pixel2id(p, px, py, plane, (int)ev - 1);
   }
   unique_pixels[r] = pid;

@@ -118,6 +118,19 @@ def test_empty_and_single_segment(cuda, small_lut):
     assert np.array_equal(u, uo) and w.shape == wo.shape
 
 
+def test_no_neighbours_main_bins_spill(cuda):
+    """number_pix_neighbors = 0: no neighbour parts, but a segment's main
+    bins still land on the adjacent simulated pixels (dense shower)."""
+    from larndsim_gb300 import workloads
+    from oracle import reference_np as R
+    p = small_params(n_neighbors=0)
+    tmpl = R.load_lut_templates(workloads.synthetic_response(seed=0, nx=5, ny=5), p)
+    tracks, fields = workloads.shower_event(seed=8, n_segments=600)
+    w, u, wo, uo = _run(p, tmpl, tracks, fields)
+    assert (u >= 0).sum() > 100
+    assert compare_wfs(w, u, wo, uo) < WFS_RTOL
+
+
 def test_recombination_models(cuda, small_lut):
     from larndsim_gb300 import consts, workloads
     p, tmpl = small_lut
