@@ -121,11 +121,23 @@ __device__ __forceinline__ void neigh_setup(const LsimParams &p, const Tables &t
 
 __device__ __forceinline__ int owner_rl(int cb, int lane) { return (lane - cb) & (kWarp - 1); }
 
+// A window is interior when all its columns are valid waveform columns and
+// all kWinSamples padded positions (cb .. cb + kWinSamples) stay inside the
+// row buffer; interior passes skip the per-column tests (padded positions
+// past L + 1 add or meet exact zeros).
+__device__ __forceinline__ bool window_interior(int cb, int L, int NT) {
+  return cb >= 1 && cb + L + 1 <= NT - 2 && cb + kWinSamples + 1 <= kRowFloats - kRowPad;
+}
+
+// The window update with weights a = s (1 - frac), b = s frac (s = n_e for
+// neighbour parts, whose samples are the raw template values and the
+// boundary term per electron; s = 1 for main-bin records, stored scaled):
+//   val[r] = U(r-2) a + U(r-1) b.
+
 // Window that crosses the edge of the waveform: value parts are kept only
 // in columns [2, Nticks-1], correction parts only in [1, Nticks-2].
-__device__ __noinline__ void window_apply_edge(const float U[kChunks], int cb, int rl, float frac, int L, int NT,
-                                               float *row, int lane) {
-  const float f1 = 1.f - frac;
+__device__ __noinline__ void window_apply_edge(const float U[kChunks], int cb, int rl, float a, float b, int L,
+                                               int NT, float *row, int lane) {
   float sprev = 0.f;
 #pragma unroll
   for (int j = 0; j < kChunks; ++j) {
@@ -137,47 +149,38 @@ __device__ __noinline__ void window_apply_edge(const float U[kChunks], int cb, i
     if (r >= L + 2 || col < 1 || col > NT - 1) continue;
     const bool vc = col <= NT - 2, vv = col >= 2;
     float val;
-    if (r == 0) val = vc ? U[j] * frac : 0.f;
-    else if (r == 1) val = (vc ? prev * f1 : 0.f) + (vv ? U[j] * frac : 0.f);
-    else val = vv ? prev * f1 + U[j] * frac : 0.f;
+    if (r == 0) val = vc ? U[j] * b : 0.f;
+    else if (r == 1) val = (vc ? prev * a : 0.f) + (vv ? U[j] * b : 0.f);
+    else val = vv ? prev * a + U[j] * b : 0.f;
     row[col] += val;
   }
 }
 
-__device__ __forceinline__ void window_apply(const float U[kChunks], int cb, int rl, float frac, int L, int NT,
+__device__ __forceinline__ void window_apply(const float U[kChunks], int cb, int rl, float a, float b, int L, int NT,
                                              float *row, int lane) {
-  if (cb >= 1 && cb + L + 1 <= NT - 2) {
+  if (window_interior(cb, L, NT)) {
     // interior: all columns valid; positions past L + 1 add exact zeros
-    const float f1 = 1.f - frac;
     float sprev = 0.f;
 #pragma unroll
     for (int j = 0; j < kChunks; ++j) {
       const float sh = __shfl_sync(0xffffffffu, U[j], (lane + kWarp - 1) & (kWarp - 1));
       const float prev = rl == 0 ? sprev : sh;
       sprev = sh;
-      row[cb + rl + j * kWarp] += prev * f1 + U[j] * frac;
+      float &x = row[cb + rl + j * kWarp];
+      x = fmaf(U[j], b, fmaf(prev, a, x));
     }
   } else {
-    window_apply_edge(U, cb, rl, frac, L, NT, row, lane);
+    window_apply_edge(U, cb, rl, a, b, L, NT, row, lane);
   }
 }
 
-// Template-0 window samples of a neighbour contribution, times n_e, with
-// the boundary correction as sample k = -1.
-__device__ __forceinline__ void neigh_samples(const Tables &tab, int rowidx, int rl, int L, float ne, float corr,
-                                              float U[kChunks]) {
-  const float *src = tab.w0 + (size_t)(rowidx < 0 ? 0 : rowidx) * L;
+// Template-0 window samples of a neighbour contribution (per electron),
+// with the boundary term D as sample k = -1 (padded table: idx = k + 1).
+__device__ __forceinline__ void neigh_samples(const Tables &tab, int rowidx, int rl, float D, float U[kChunks]) {
+  const float *src = tab.w0 + (size_t)(rowidx < 0 ? 0 : rowidx) * kWinSamples + rl;
 #pragma unroll
-  for (int j = 0; j < kChunks; ++j) {
-    const int k = rl + j * kWarp - 1;
-    U[j] = (rowidx >= 0 && k >= 0 && k < L) ? __ldg(src + k) * ne : 0.f;
-  }
-  if (rl == 0) U[0] = corr;
-}
-
-__device__ __forceinline__ void scale(float v[kChunks], float a) {
-#pragma unroll
-  for (int m = 0; m < kChunks; ++m) v[m] *= a;
+  for (int j = 0; j < kChunks; ++j) U[j] = __ldg(src + j * kWarp);
+  if (rl == 0) U[0] = D;
 }
 
 // Forward: all neighbour parts of the pixel, four contributions in flight.
@@ -196,14 +199,20 @@ __device__ __forceinline__ void neigh_forward(const LsimParams &p, const Tables 
       const int r3 = j + 3 < m ? nb.row[j + 3] : -1;
       const int c0 = nb.cb[j], c1 = nb.cb[j + 1], c2 = nb.cb[j + 2], c3 = nb.cb[j + 3];
       const int l0 = owner_rl(c0, lane), l1 = owner_rl(c1, lane), l2 = owner_rl(c2, lane), l3 = owner_rl(c3, lane);
-      neigh_samples(tab, r0, l0, L, nb.ne[j], nb.D[j] * nb.ne[j], u0);
-      neigh_samples(tab, r1, l1, L, nb.ne[j + 1], nb.D[j + 1] * nb.ne[j + 1], u1);
-      neigh_samples(tab, r2, l2, L, nb.ne[j + 2], nb.D[j + 2] * nb.ne[j + 2], u2);
-      neigh_samples(tab, r3, l3, L, nb.ne[j + 3], nb.D[j + 3] * nb.ne[j + 3], u3);
-      if (r0 >= 0) window_apply(u0, c0, l0, nb.frac[j], L, NT, row, lane);
-      if (r1 >= 0) window_apply(u1, c1, l1, nb.frac[j + 1], L, NT, row, lane);
-      if (r2 >= 0) window_apply(u2, c2, l2, nb.frac[j + 2], L, NT, row, lane);
-      if (r3 >= 0) window_apply(u3, c3, l3, nb.frac[j + 3], L, NT, row, lane);
+      neigh_samples(tab, r0, l0, nb.D[j], u0);
+      neigh_samples(tab, r1, l1, nb.D[j + 1], u1);
+      neigh_samples(tab, r2, l2, nb.D[j + 2], u2);
+      neigh_samples(tab, r3, l3, nb.D[j + 3], u3);
+#define LSIM_NEIGH_APPLY(r, u, c, l, q)                                                                     \
+  if (r >= 0) {                                                                                          \
+    const float ne = nb.ne[j + q], f = nb.frac[j + q];                                                   \
+    window_apply(u, c, l, ne * (1.f - f), ne * f, L, NT, row, lane);                                     \
+  }
+      LSIM_NEIGH_APPLY(r0, u0, c0, l0, 0)
+      LSIM_NEIGH_APPLY(r1, u1, c1, l1, 1)
+      LSIM_NEIGH_APPLY(r2, u2, c2, l2, 2)
+      LSIM_NEIGH_APPLY(r3, u3, c3, l3, 3)
+#undef LSIM_NEIGH_APPLY
     }
     __syncwarp();
   }
@@ -214,40 +223,46 @@ struct Theta {
 };
 
 // Adjoint of one neighbour contribution (descriptor j of the batch) given
-// its template-0 samples v[c] = T0[32c + lane]: accumulates dL/dtheta.
+// its padded template-0 samples v[c] = w0[row][32c + lane] (sample
+// idx - 1 of the window, idx = 32c + lane): sample k lands on columns
+// cb + k + 1 (x frac) and cb + k + 2 (x (1 - frac)); lane 0's idx = 0 is the
+// boundary correction D * n_e (table value 0).  Accumulates dL/dtheta.
 __device__ __forceinline__ void neigh_vjp_one(const NBatch &nb, int j, const float v[kChunks], int L, int NT,
                                               float inv_ts, const float *grow, Theta &th, int lane) {
   const int cb = nb.cb[j];
   const float f = nb.frac[j], f1 = 1.f - f, ne = nb.ne[j];
-  float acc_ne = 0.f, acc_fr = 0.f;
-  if (cb >= 1 && cb + L + 1 <= NT - 2) {
-    // interior window: every column in range; samples past L are zero
+  float sA = 0.f, sB = 0.f, gA0 = 0.f, gB0 = 0.f;   // sum v gA, sum v gB
+  if (window_interior(cb, L, NT)) {
+    // interior window: every column in range (columns past cb + L + 1 hold
+    // zeros of the row padding and meet zero samples)
 #pragma unroll
     for (int c = 0; c < kChunks; ++c) {
-      const int k = c * kWarp + lane;
-      const float gA = grow[cb + k + 1], gB = grow[cb + k + 2];
-      acc_ne += (gA * f + gB * f1) * v[c];
-      acc_fr += v[c] * (gA - gB);
+      const int c1 = cb + c * kWarp + lane;
+      const float gA = grow[c1], gB = grow[c1 + 1];
+      sA = fmaf(v[c], gA, sA);
+      sB = fmaf(v[c], gB, sB);
+      if (c == 0) { gA0 = gA; gB0 = gB; }
     }
   } else {
 #pragma unroll
     for (int c = 0; c < kChunks; ++c) {
-      const int k = c * kWarp + lane;
-      if (k < L) {
-        const int ca = cb + k + 1, cbb = cb + k + 2;
-        const float gA = (ca >= 2 && ca <= NT - 1) ? grow[ca] : 0.f;
-        const float gB = (cbb >= 2 && cbb <= NT - 1) ? grow[cbb] : 0.f;
-        acc_ne += (gA * f + gB * f1) * v[c];
-        acc_fr += v[c] * (gA - gB);
+      const int idx = c * kWarp + lane;
+      if (idx <= L) {
+        const int c1 = cb + idx;
+        const int lo = idx == 0 ? 1 : 2, hi = idx == 0 ? NT - 2 : NT - 1;
+        const float gA = (c1 >= lo && c1 <= hi) ? grow[c1] : 0.f;
+        const float gB = (c1 + 1 >= lo && c1 + 1 <= hi) ? grow[c1 + 1] : 0.f;
+        sA = fmaf(v[c], gA, sA);
+        sB = fmaf(v[c], gB, sB);
+        if (c == 0) { gA0 = gA; gB0 = gB; }
       }
     }
   }
+  float acc_ne = sA * f + sB * f1, acc_fr = sA - sB;
   if (lane == 0) {
-    const float gc0 = (cb >= 1 && cb <= NT - 2) ? grow[cb] : 0.f;
-    const float gc1 = (cb + 1 >= 1 && cb + 1 <= NT - 2) ? grow[cb + 1] : 0.f;
-    const float dcorr = gc0 * f + gc1 * f1;
+    const float dcorr = gA0 * f + gB0 * f1;
     acc_ne += dcorr * nb.D[j];
-    acc_fr += dcorr * nb.dl[j] + nb.D[j] * (gc0 - gc1);
+    acc_fr += dcorr * nb.dl[j] + nb.D[j] * (gA0 - gB0);
   }
   const float dt = acc_fr * ne * inv_ts;
   th.v[0] += acc_ne * nb.dne[0][j];
@@ -257,13 +272,10 @@ __device__ __forceinline__ void neigh_vjp_one(const NBatch &nb, int j, const flo
   th.v[7] += acc_ne * nb.dne[4][j];
 }
 
-__device__ __forceinline__ void neigh_rows(const Tables &tab, int rowidx, int L, float v[kChunks], int lane) {
-  const float *src = tab.w0 + (size_t)(rowidx < 0 ? 0 : rowidx) * L;
+__device__ __forceinline__ void neigh_rows(const Tables &tab, int rowidx, float v[kChunks], int lane) {
+  const float *src = tab.w0 + (size_t)rowidx * kWinSamples + lane;
 #pragma unroll
-  for (int c = 0; c < kChunks; ++c) {
-    const int k = c * kWarp + lane;
-    v[c] = (rowidx >= 0 && k < L) ? __ldg(src + k) : 0.f;
-  }
+  for (int c = 0; c < kChunks; ++c) v[c] = __ldg(src + c * kWarp);
 }
 
 // Adjoint: all neighbour parts, given the waveform cotangent grow[col].
@@ -280,7 +292,7 @@ __device__ __forceinline__ void neigh_backward(const LsimParams &p, const Tables
       const int rowidx = nb.row[j];
       if (rowidx < 0) continue;
       float v[kChunks];
-      neigh_rows(tab, rowidx, L, v, lane);
+      neigh_rows(tab, rowidx, v, lane);
       neigh_vjp_one(nb, j, v, L, NT, inv_ts, grow, th, lane);
     }
     __syncwarp();
@@ -361,7 +373,7 @@ __device__ __forceinline__ void main_rec_forward(const LsimParams &p, const floa
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q)
-      if (j + q < m) window_apply(u[q], cb[q], rl[q], nb.frac[j + q], L, NT, row, lane);
+      if (j + q < m) window_apply(u[q], cb[q], rl[q], 1.f - nb.frac[j + q], nb.frac[j + q], L, NT, row, lane);
   }
   __syncwarp();
 }
@@ -379,7 +391,7 @@ __device__ __forceinline__ void main_rec_backward(const LsimParams &p, float *mr
     float *rec = mrec + (size_t)nb.row[j] * kRecFloats;
     const int cb = nb.cb[j];
     const float f = nb.frac[j], f1 = 1.f - f;
-    const bool interior = cb >= 1 && cb + L + 1 <= NT - 2;
+    const bool interior = window_interior(cb, L, NT);
     float dfr = 0.f, dcorr = 0.f;
 #pragma unroll
     for (int c = 0; c < kChunks; ++c) {
@@ -408,8 +420,8 @@ __device__ __forceinline__ void main_rec_backward(const LsimParams &p, float *mr
   __syncwarp();
 }
 
-// Per-warp shared memory.  Warps index an array of these and access the
-// row with float4, so the size must keep every element 16-byte aligned.
+// Per-warp shared memory.  Each warp's block starts on a 16-byte boundary
+// (the row is accessed with float4), so the size stays a 16-byte multiple.
 template <bool GRAD>
 struct __align__(16) WarpSmem {
   float buf[kRowFloats];
@@ -489,7 +501,12 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 3) k_lut_pixels(AccumArgs a
   constexpr bool GRAD = (MODE == kModeGrad);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x % kWarp, wid = threadIdx.x / kWarp;
-  WarpSmem<GRAD> &sm = reinterpret_cast<WarpSmem<GRAD> *>(smem_raw)[wid];
+  unsigned char *wbase = smem_raw + (size_t)wid * a.warp_smem;
+  WarpSmem<GRAD> &sm = *reinterpret_cast<WarpSmem<GRAD> *>(wbase);
+  if constexpr (GRAD) {
+    if (lane == 0) sm.fee.mask = reinterpret_cast<uint32_t *>(wbase + sizeof(WarpSmem<true>));
+    __syncwarp();
+  }
   const LsimParams &p = a.p;
   float *row = sm.buf + kRowPad;
   const int NT = p.n_ticks;
@@ -661,9 +678,19 @@ __global__ void k_grad_finalize(const double *partials, int n_rec_blocks, const 
 // ---------------------------------------------------------------- launch
 
 // Persistent grid: every SM filled to its occupancy limit.
+// Per-warp shared memory: the WarpSmem block, then (adjoint mode) the
+// per-hit reset masks of the front end, max_adc_values x kMaskWords words.
 template <int MODE>
-static int grid_blocks(int *blocks, size_t *smem_out) {
-  const size_t smem = sizeof(WarpSmem<MODE == kModeGrad>) * kAccWarps;
+static size_t warp_smem_bytes(const LsimParams &p) {
+  size_t b = sizeof(WarpSmem<MODE == kModeGrad>);
+  if (MODE == kModeGrad) b += sizeof(uint32_t) * kMaskWords * (size_t)p.max_adc_values;
+  return (b + 15) & ~size_t(15);
+}
+
+// Persistent grid: every SM filled to its occupancy limit.
+template <int MODE>
+static int grid_blocks(const LsimParams &p, int *blocks, size_t *smem_out) {
+  const size_t smem = warp_smem_bytes<MODE>(p) * kAccWarps;
   if (cudaFuncSetAttribute(k_lut_pixels<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return LSIM_ERR_CUDA;
@@ -678,11 +705,13 @@ static int grid_blocks(int *blocks, size_t *smem_out) {
 }
 
 template <int MODE>
-static int launch_mode(const AccumArgs &a, cudaStream_t st) {
+static int launch_mode(const AccumArgs &a0, cudaStream_t st) {
   int blocks = 0;
   size_t smem = 0;
-  int rc = grid_blocks<MODE>(&blocks, &smem);
+  int rc = grid_blocks<MODE>(a0.p, &blocks, &smem);
   if (rc != LSIM_OK) return rc;
+  AccumArgs a = a0;
+  a.warp_smem = (int)warp_smem_bytes<MODE>(a0.p);
   if (cudaMemsetAsync(&a.w.counts->work, 0, sizeof(int32_t), st) != cudaSuccess) return LSIM_ERR_CUDA;
   k_lut_pixels<MODE><<<blocks, kAccWarps * kWarp, smem, st>>>(a);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;

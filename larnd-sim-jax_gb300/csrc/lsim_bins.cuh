@@ -7,7 +7,7 @@
 
 namespace lsim {
 
-constexpr int kChunks = 5;            // ceil((L + 2) / 32) window chunks per lane, L <= 158
+constexpr int kChunks = kWinSamples / kWarp;   // window chunks per lane
 
 // Main-bin record of one (segment, pixel whose main bins it covers) pair:
 //   rec[0]        boundary correction  n_e * sum_uv W_uv D_uv
@@ -17,7 +17,7 @@ constexpr int kChunks = 5;            // ceil((L + 2) / 32) window chunks per la
 // The adjoint pass overwrites rec[0 .. L] with the cotangents of the same
 // quantities.  A segment's bins cover at most 2 x 2 pixels, so each segment
 // owns 4 consecutive records, indexed by its pixel offsets.
-constexpr int kRecDl = kChunks * kWarp;      // 160
+constexpr int kRecDl = kWinSamples;          // 160
 constexpr int kRecFloats = kMainRecFloats;   // 164 floats = 656 bytes
 constexpr int kRecPerSeg = kMainRecPerSeg;
 static_assert(kRecFloats >= kRecDl + 1 && kRecFloats % 4 == 0, "main-bin record layout");

@@ -16,6 +16,7 @@ constexpr int kWarp = 32;
 constexpr int kMaxNeigh = 8;             // number_pix_neighbors supported: 0..8
 constexpr int kMaxTran = 5;              // nb_tran_diff_bins supported: 5
 constexpr int kMainSub = 5;              // main-bin LUT sub-positions (nb_bins_per_pixel / 2)
+constexpr int kWinSamples = 160;         // padded window samples k = -1 .. 158 (signal_length <= 158)
 constexpr int kScanTile = 2048;          // slots per scan block
 constexpr int kScanThreads = 256;
 
@@ -165,7 +166,7 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
 struct Tables {
   const float4 *wmp;   // [T][5][5][L] : (T[i-1], T[i], T[i+1], 0) windows, i in [1, T-2]
   const float *cm;     // [T][5][5][Nt] cumulative sums of the main sub-positions
-  const float *w0;     // [nx][ny][L] template-0 windows
+  const float *w0;     // [nx][ny][kWinSamples] template-0 windows: 0, T0[Nt-L .. Nt-1], zeros
   const float *c0;     // [nx][ny][Nt] template-0 cumulative sums
 };
 
@@ -175,7 +176,7 @@ inline size_t tables_layout(const LsimParams &p, size_t *o_wmp, size_t *o_cm, si
   size_t off = 0;
   *o_wmp = off; off += align256(sizeof(float4) * T * m * L);
   *o_cm = off;  off += align256(sizeof(float) * T * m * Nt);
-  *o_w0 = off;  off += align256(sizeof(float) * nx * ny * L);
+  *o_w0 = off;  off += align256(sizeof(float) * nx * ny * kWinSamples);
   *o_c0 = off;  off += align256(sizeof(float) * nx * ny * Nt);
   return off;
 }

@@ -22,7 +22,7 @@ struct FeeState {
   int e2[LSIM_MAX_HITS];       // reset index
   int cond[LSIM_MAX_HITS];     // 1 = rejected (adc forced to 0)
   float raw[LSIM_MAX_HITS];    // integrated charge before digitisation
-  uint32_t mask[LSIM_MAX_HITS][kMaskWords];  // (C - R >= 0) per tick, per hit
+  uint32_t *mask;              // [max_adc_values][kMaskWords]: (C - R >= 0) per tick, per hit
 };
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -123,7 +123,7 @@ __device__ __forceinline__ void fee_forward(const LsimParams &p, float *C, int T
       }
       if (st) {
         unsigned bal = __ballot_sync(0xffffffffu, keep);
-        if (lane == 0) st->mask[h][m] = bal;
+        if (lane == 0) st->mask[h * kMaskWords + m] = bal;
       }
     }
     __syncwarp();
@@ -174,7 +174,7 @@ __device__ __forceinline__ void fee_backward(const LsimParams &p, float *G, int 
     for (int m = 0; m < nwords; ++m) {
       int i = m * kWarp + lane;
       if (i < T) {
-        bool bit = (st->mask[h][m] >> lane) & 1u;
+        bool bit = (st->mask[h * kMaskWords + m] >> lane) & 1u;
         float g = G[i];
         if (bit) S += g; else G[i] = 0.f;
       }

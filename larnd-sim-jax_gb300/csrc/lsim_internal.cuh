@@ -28,6 +28,7 @@ struct AccumArgs {
   const int32_t *tgt_pids;  // target pixels for the SSE loss (grad mode, when g_adc is null)
   const float *tgt_adc;
   int64_t n_tgt;
+  int warp_smem;            // shared-memory bytes per warp of the pixel kernel (set at launch)
 };
 int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st);
 int run_grad_finalize(const AccumArgs &a, float *loss_out, float *grad_out, cudaStream_t st);

@@ -93,13 +93,16 @@ __global__ void k_prep_wmp(LsimParams p, const float *__restrict__ tmpl, float4 
 }
 
 // Template-0 windows over the full LUT.
+// Template-0 windows padded to kWinSamples: w0[row][idx] is sample idx - 1
+// of the window (0 at idx = 0 and past the signal length), so the window
+// passes read whole 32-sample chunks without bounds tests.
 __global__ void k_prep_w0(LsimParams p, const float *__restrict__ tmpl, float *__restrict__ w0) {
   const int L = p.signal_length, Nt = p.lut_nt;
-  const int64_t total = (int64_t)p.lut_nx * p.lut_ny * L;
+  const int64_t total = (int64_t)p.lut_nx * p.lut_ny * kWinSamples;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(i % L);
-    const int64_t row = i / L;
-    w0[i] = tmpl[(size_t)row * Nt + (Nt - L) + k];
+    const int idx = (int)(i % kWinSamples);
+    const int64_t row = i / kWinSamples;
+    w0[i] = (idx >= 1 && idx <= L) ? tmpl[(size_t)row * Nt + (Nt - L) + idx - 1] : 0.f;
   }
 }
 
@@ -128,7 +131,8 @@ __global__ void k_prep_cum(LsimParams p, const float *__restrict__ tmpl, float *
 }
 
 int run_prepare_tables(const LsimParams &p, const float *templates, void *tables, cudaStream_t st) {
-  if (p.lut_nx < kMainSub || p.lut_ny < kMainSub || p.signal_length > p.lut_nt || p.n_templates < 3)
+  if (p.lut_nx < kMainSub || p.lut_ny < kMainSub || p.signal_length > p.lut_nt || p.n_templates < 3 ||
+      p.signal_length + 2 > kWinSamples)
     return LSIM_ERR_UNSUPPORTED;
   size_t a, b, c, d;
   tables_layout(p, &a, &b, &c, &d);
