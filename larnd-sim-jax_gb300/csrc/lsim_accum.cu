@@ -497,7 +497,7 @@ __device__ __forceinline__ int32_t slot_pid(const LsimParams &p, const Grid &g, 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kAccWarps * kWarp, 3) k_lut_pixels(AccumArgs a) {
+__global__ void __launch_bounds__(kAccWarps * kWarp, 4) k_lut_pixels(AccumArgs a) {
   constexpr bool GRAD = (MODE == kModeGrad);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x % kWarp, wid = threadIdx.x / kWarp;

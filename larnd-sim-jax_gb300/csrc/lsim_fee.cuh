@@ -14,7 +14,8 @@
 
 namespace lsim {
 
-constexpr int kMaskWords = 64;   // bits per hit for T <= 2048
+constexpr int kMaskWords = 64;   // words per hit: 2 per lane, bit 4m + q for tick 128m + 4 lane + q (T <= 2048)
+constexpr int kFeePass = 4 * kWarp;   // ticks per warp pass: lane l holds ticks 4l .. 4l + 3
 
 struct FeeState {
   int n_done;                  // hits evaluated before the early exit (the rest are empty)
@@ -22,7 +23,7 @@ struct FeeState {
   int e2[LSIM_MAX_HITS];       // reset index
   int cond[LSIM_MAX_HITS];     // 1 = rejected (adc forced to 0)
   float raw[LSIM_MAX_HITS];    // integrated charge before digitisation
-  uint32_t *mask;              // [max_adc_values][kMaskWords]: (C - R >= 0) per tick, per hit
+  uint32_t *mask;              // [max_adc_values][kMaskWords]: (C - R >= 0) per tick, per hit, lane-private
 };
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -71,7 +72,10 @@ __device__ __forceinline__ void warp_cumsum_charge(float *X, int T, float ts, in
 
 // Forward self-trigger on C (in place).  normals: per-pixel standard
 // normals [1 + 3H] or null (noise off).  Writes adc (digitized) and tick
-// per hit through lane 0; fills st when non-null.
+// per hit through lane 0; fills st when non-null.  C must be 16-byte
+// aligned with room for whole 4-tick groups (T rounded up to 4).
+//
+// Lane l works on ticks 128m + 4l .. 128m + 4l + 3 of pass m (one float4).
 //
 // early_exit (noise off, threshold > 0): once a rejected hit leaves C all
 // zero, every later hit is provably empty (no crossing of a positive
@@ -83,19 +87,26 @@ __device__ __forceinline__ void fee_forward(const LsimParams &p, float *C, int T
   const float thr = p.threshold;
   const int H = p.max_adc_values;
   float base = normals ? normals[0] * p.reset_noise : 0.f;
-  const int nwords = (T + kWarp - 1) / kWarp;
+  float4 *C4 = reinterpret_cast<float4 *>(C);
   for (int h = 0; h < H; ++h) {
+    // first i < T - 1 with Q[i] <= thr <= Q[i + 1], Q = base + C
     int idx = T - 2;
-    for (int m = 0; m * kWarp < T - 1; ++m) {
-      int i = m * kWarp + lane;
-      bool c = false;
-      if (i < T - 1) {
-        float q0 = base + C[i];
-        float q1 = base + C[i + 1];
-        c = (q1 >= thr) && (q0 <= thr);
+    for (int i0 = 4 * lane, m = 0; m * kFeePass < T - 1; ++m, i0 += kFeePass) {
+      const float4 c = i0 < T ? C4[i0 / 4] : make_float4(0.f, 0.f, 0.f, 0.f);
+      float nx = __shfl_down_sync(0xffffffffu, c.x, 1);
+      if (lane == kWarp - 1) nx = i0 + 4 < T ? C[i0 + 4] : 0.f;
+      const float q0 = base + c.x, q1 = base + c.y, q2 = base + c.z, q3 = base + c.w, q4 = base + nx;
+      int first = 4;
+      if (i0 + 3 < T - 1 && q4 >= thr && q3 <= thr) first = 3;
+      if (i0 + 2 < T - 1 && q3 >= thr && q2 <= thr) first = 2;
+      if (i0 + 1 < T - 1 && q2 >= thr && q1 <= thr) first = 1;
+      if (i0 < T - 1 && q1 >= thr && q0 <= thr) first = 0;
+      const unsigned bal = __ballot_sync(0xffffffffu, first < 4);
+      if (bal) {
+        const int ln = __ffs(bal) - 1;
+        idx = m * kFeePass + 4 * ln + __shfl_sync(0xffffffffu, first, ln);
+        break;
       }
-      unsigned bal = __ballot_sync(0xffffffffu, c);
-      if (bal) { idx = m * kWarp + __ffs(bal) - 1; break; }
     }
     int e = idx + 1 + p.fee_interval;
     if (e >= T) e = T - 1;
@@ -111,20 +122,31 @@ __device__ __forceinline__ void fee_forward(const LsimParams &p, float *C, int T
     if (e2 >= T) e2 = T - 1;
     const float R = C[e2];
     __syncwarp();
+    // reset: C <- where(C - R < 0, 0, C - R); keep bits per lane (bit 4m + q)
     bool nz = false;
-    for (int m = 0; m < nwords; ++m) {
-      int i = m * kWarp + lane;
-      bool keep = true;
-      if (i < T) {
-        float c = C[i] - R;
-        keep = !(c < 0.f);
-        C[i] = keep ? c : 0.f;
-        nz |= keep && c != 0.f;
+    uint64_t km = 0u;
+    for (int i0 = 4 * lane, sh = 0; i0 - 4 * lane < T; i0 += kFeePass, sh += 4) {
+      if (i0 < T) {
+        const float4 c = C4[i0 / 4];
+        float v[4] = {c.x, c.y, c.z, c.w};
+        uint32_t bits = 0u;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (i0 + q < T) {
+            const float d = v[q] - R;
+            const bool keep = !(d < 0.f);
+            v[q] = keep ? d : 0.f;
+            nz |= keep && d != 0.f;
+            bits |= (keep ? 1u : 0u) << q;
+          }
+        }
+        C4[i0 / 4] = make_float4(v[0], v[1], v[2], v[3]);
+        km |= (uint64_t)bits << sh;
       }
-      if (st) {
-        unsigned bal = __ballot_sync(0xffffffffu, keep);
-        if (lane == 0) st->mask[h * kMaskWords + m] = bal;
-      }
+    }
+    if (st) {
+      st->mask[h * kMaskWords + 2 * lane] = (uint32_t)km;
+      st->mask[h * kMaskWords + 2 * lane + 1] = (uint32_t)(km >> 32);
     }
     __syncwarp();
     if (lane == 0) {
@@ -154,30 +176,38 @@ __device__ __forceinline__ void fee_forward(const LsimParams &p, float *C, int T
 
 // Adjoint of fee_forward + cumsum: from dL/d(integrated charge) per hit
 // (gint, identical in all lanes) to dL/dW[i] over T ticks, written to G.
+// T must be a multiple of 4 and G 16-byte aligned.
 __device__ __forceinline__ void fee_backward(const LsimParams &p, float *G, int T, const FeeState *st,
                                              const float *gint, int lane) {
-  const int H = p.max_adc_values;
-  const int nwords = (T + kWarp - 1) / kWarp;
-  for (int i = lane; i < T; i += kWarp) G[i] = 0.f;
+  float4 *G4 = reinterpret_cast<float4 *>(G);
+  for (int i = 4 * lane; i < T; i += kFeePass) G4[i / 4] = make_float4(0.f, 0.f, 0.f, 0.f);
   __syncwarp();
-  // hits skipped by the early exit: all-true masks, reset index T-1, rejected
-  for (int h = H - 1; h >= st->n_done; --h) {
+  // Hits skipped by the early exit have all-true masks, reset index T-1 and
+  // no charge: each maps G to G - e_{T-1} sum(G).  After the first of them
+  // sum(G) is zero, so one application is the whole chain.
+  if (st->n_done < p.max_adc_values) {
     float S = 0.f;
-    for (int i = lane; i < T; i += kWarp) S += G[i];
+    for (int i = 4 * lane; i < T; i += kFeePass) {
+      const float4 g = G4[i / 4];
+      S += (g.x + g.y) + (g.z + g.w);
+    }
     S = warp_sum(S);
     __syncwarp();
     if (lane == 0) G[T - 1] -= S;
     __syncwarp();
   }
   for (int h = st->n_done - 1; h >= 0; --h) {
+    uint64_t km = (uint64_t)st->mask[h * kMaskWords + 2 * lane] |
+                  ((uint64_t)st->mask[h * kMaskWords + 2 * lane + 1] << 32);
     float S = 0.f;
-    for (int m = 0; m < nwords; ++m) {
-      int i = m * kWarp + lane;
-      if (i < T) {
-        bool bit = (st->mask[h * kMaskWords + m] >> lane) & 1u;
-        float g = G[i];
-        if (bit) S += g; else G[i] = 0.f;
-      }
+    for (int i0 = 4 * lane; i0 < T; i0 += kFeePass, km >>= 4) {
+      const uint32_t bits = (uint32_t)km;
+      float4 g = G4[i0 / 4];
+      if (bits & 1u) S += g.x; else g.x = 0.f;
+      if (bits & 2u) S += g.y; else g.y = 0.f;
+      if (bits & 4u) S += g.z; else g.z = 0.f;
+      if (bits & 8u) S += g.w; else g.w = 0.f;
+      G4[i0 / 4] = g;
     }
     S = warp_sum(S);
     __syncwarp();
