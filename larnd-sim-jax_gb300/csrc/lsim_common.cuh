@@ -164,7 +164,7 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
 
 // Prepared LUT tables (see lsim_lut_prepare).
 struct Tables {
-  const float4 *wmp;   // [T][5][5][L] : (T[i-1], T[i], T[i+1], 0) windows, i in [1, T-2]
+  const float4 *wmp;   // [T][5][5][kWinSamples]: (T[i-1], T[i], T[i+1], 0) windows, i in [1, T-2], padded as w0
   const float *cm;     // [T][5][5][Nt] cumulative sums of the main sub-positions
   const float *w0;     // [nx][ny][kWinSamples] template-0 windows: 0, T0[Nt-L .. Nt-1], zeros
   const float *c0;     // [nx][ny][Nt] template-0 cumulative sums
@@ -174,7 +174,7 @@ inline size_t tables_layout(const LsimParams &p, size_t *o_wmp, size_t *o_cm, si
   const size_t T = p.n_templates, L = p.signal_length, Nt = p.lut_nt;
   const size_t nx = p.lut_nx, ny = p.lut_ny, m = kMainSub * kMainSub;
   size_t off = 0;
-  *o_wmp = off; off += align256(sizeof(float4) * T * m * L);
+  *o_wmp = off; off += align256(sizeof(float4) * T * m * kWinSamples);
   *o_cm = off;  off += align256(sizeof(float) * T * m * Nt);
   *o_w0 = off;  off += align256(sizeof(float) * nx * ny * kWinSamples);
   *o_c0 = off;  off += align256(sizeof(float) * nx * ny * Nt);

@@ -75,16 +75,18 @@ int run_build_templates(const float *response, int nx, int ny, int nt, const flo
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 
-// (T[i-1], T[i], T[i+1], 0) windows of the main sub-positions.
+// (T[i-1], T[i], T[i+1], 0) windows of the main sub-positions, padded like
+// the template-0 windows: entry idx is sample idx - 1 (zero at idx = 0 and
+// past the signal length).
 __global__ void k_prep_wmp(LsimParams p, const float *__restrict__ tmpl, float4 *__restrict__ wmp) {
   const int L = p.signal_length, Nt = p.lut_nt, T = p.n_templates;
-  const int64_t total = (int64_t)T * kMainSub * kMainSub * L;
+  const int64_t total = (int64_t)T * kMainSub * kMainSub * kWinSamples;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(i % L);
-    const int64_t q = i / L;
+    const int idx = (int)(i % kWinSamples), k = idx - 1;
+    const int64_t q = i / kWinSamples;
     const int v = (int)(q % kMainSub), u = (int)((q / kMainSub) % kMainSub), t = (int)(q / (kMainSub * kMainSub));
     float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (t >= 1 && t <= T - 2) {
+    if (t >= 1 && t <= T - 2 && idx >= 1 && idx <= L) {
       auto at = [&](int tt) { return tmpl[(((size_t)tt * p.lut_nx + u) * p.lut_ny + v) * Nt + (Nt - L) + k]; };
       o.x = at(t - 1); o.y = at(t); o.z = at(t + 1);
     }
@@ -92,7 +94,6 @@ __global__ void k_prep_wmp(LsimParams p, const float *__restrict__ tmpl, float4 
   }
 }
 
-// Template-0 windows over the full LUT.
 // Template-0 windows padded to kWinSamples: w0[row][idx] is sample idx - 1
 // of the window (0 at idx = 0 and past the signal length), so the window
 // passes read whole 32-sample chunks without bounds tests.

@@ -42,26 +42,27 @@ __device__ __forceinline__ int main_entries(const LsimParams &p, const Tables &t
                                             const SegAdj *a, int dx, int dy, MainSmem &ms, float *wd, float *wdl,
                                             int lane) {
   const int nbp = p.nb_bins_per_pixel;
-  float ex[kMaxTran], ey[kMaxTran], dex[kMaxTran], dey[kMaxTran];
+  // this lane's sub-position (u, v): summed 1-D bin integrals of the bins of
+  // each axis that fall on the pixel with that LUT index (axis_weights, per lane)
+  const int u = lane / kMainSub, v = lane % kMainSub;
+  float xw = 0.f, yw = 0.f, dxw = 0.f, dyw = 0.f;
+  unsigned um = 0u, vm = 0u;
+  const int bx = f.bx, by = f.by, ppx = ifloordiv(bx, nbp), ppy = ifloordiv(by, nbp);
 #pragma unroll
   for (int i = 0; i < kMaxTran; ++i) {
-    ex[i] = f.ex[i];
-    ey[i] = f.ey[i];
-    dex[i] = GRAD ? a->dex[i] : 0.f;
-    dey[i] = GRAD ? a->dey[i] : 0.f;
+    const int bi = bx + i - kMaxTran / 2, bj = by + i - kMaxTran / 2;
+    const bool onx = ifloordiv(bi, nbp) - ppx == dx, ony = ifloordiv(bj, nbp) - ppy == dy;
+    const int ui = lut_index(bi, nbp, 0), vj = lut_index(bj, nbp, 0);
+    if (onx) {
+      um |= 1u << ui;
+      if (ui == u) { xw += f.ex[i]; if (GRAD) dxw += a->dex[i]; }
+    }
+    if (ony) {
+      vm |= 1u << vj;
+      if (vj == v) { yw += f.ey[i]; if (GRAD) dyw += a->dey[i]; }
+    }
   }
-  float Xw[kMainSub], Yw[kMainSub], dXw[kMainSub], dYw[kMainSub];
-  unsigned um, vm;
-  axis_weights(ex, dex, f.bx, nbp, dx, Xw, dXw, &um);
-  axis_weights(ey, dey, f.by, nbp, dy, Yw, dYw, &vm);
-  const int u = lane / kMainSub, v = lane % kMainSub;
   const bool mine = lane < kMainSub * kMainSub && ((um >> u) & 1u) && ((vm >> v) & 1u);
-  float xw = 0.f, yw = 0.f, dxw = 0.f, dyw = 0.f;
-#pragma unroll
-  for (int q = 0; q < kMainSub; ++q) {
-    if (q == u) { xw = Xw[q]; dxw = dXw[q]; }
-    if (q == v) { yw = Yw[q]; dyw = dYw[q]; }
-  }
   const unsigned bal = __ballot_sync(0xffffffffu, mine);
   float s_wd = 0.f, s_wdl = 0.f;
   if (mine) {
@@ -119,23 +120,23 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_records(LsimPa
         float acc[kChunks];
 #pragma unroll
         for (int j = 0; j < kChunks; ++j) acc[j] = 0.f;
+#pragma unroll 1
         for (int e = 0; e < n; ++e) {
-          const float4 *src = tab.wmp + (size_t)ms.off[e] * L;   // record index idx holds sample idx - 1
+          // padded rows: entry idx is sample idx - 1, matching the record layout
+          const float4 *src = tab.wmp + (size_t)ms.off[e] * kWinSamples + lane;
           const float W = ms.W[e];
+          const float wa = W * qa, wb = W * qb, wc = W * qc;
 #pragma unroll
           for (int j = 0; j < kChunks; ++j) {
-            const int idx = lane + j * kWarp;
-            if (idx >= 1 && idx <= L) {
-              const float4 t = __ldg(src + idx - 1);
-              acc[j] += W * ((t.y * qb + t.x * qa) + t.z * qc);
-            }
+            const float4 t = __ldg(src + j * kWarp);
+            acc[j] = fmaf(t.z, wc, fmaf(t.x, wa, fmaf(t.y, wb, acc[j])));
           }
         }
         float *rec = w.mrec + ((size_t)s * kRecPerSeg + (dx - lx) * 2 + (dy - ly)) * kRecFloats;
 #pragma unroll
         for (int j = 0; j < kChunks; ++j) {
           const int idx = lane + j * kWarp;
-          rec[idx] = idx == 0 ? wd * ne : (idx <= L ? acc[j] * ne : 0.f);
+          rec[idx] = idx == 0 ? wd * ne : acc[j] * ne;
         }
         if (lane == 0) rec[kRecDl] = wdl * ne;
         __syncwarp();
@@ -143,7 +144,7 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_records(LsimPa
   }
 }
 
-__global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_adjoint(LsimParams p, Tables tab, Workspace w, Grid g,
+__global__ void __launch_bounds__(kMainBlockWarps * kWarp, 4) k_main_adjoint(LsimParams p, Tables tab, Workspace w, Grid g,
                                                                            int64_t n_rows) {
   __shared__ MainSmem sms[kMainBlockWarps];
   const int lane = threadIdx.x % kWarp;
@@ -173,31 +174,30 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_adjoint(LsimPa
         float wd, wdl;
         const int n = main_entries<true>(p, tab, f, &a, dx, dy, ms, &wd, &wdl, lane);
         const float *rec = w.mrec + ((size_t)s * kRecPerSeg + (dx - lx) * 2 + (dy - ly)) * kRecFloats;
+        // cotangents of the samples (idx >= 1; the padded rows are zero at
+        // idx = 0, where the record holds the boundary term's cotangent)
         float d[kChunks];
 #pragma unroll
-        for (int j = 0; j < kChunks; ++j) {
-          const int idx = lane + j * kWarp;
-          d[j] = (idx >= 1 && idx <= L) ? rec[idx] : 0.f;
-        }
+        for (int j = 0; j < kChunks; ++j) d[j] = rec[lane + j * kWarp];
         const float dcorr = rec[0];
+#pragma unroll 1
         for (int e = 0; e < n; ++e) {
-          const float4 *src = tab.wmp + (size_t)ms.off[e] * L;
-          const float W = ms.W[e], dW = ms.dW[e];
+          const float4 *src = tab.wmp + (size_t)ms.off[e] * kWinSamples + lane;
+          float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
           for (int j = 0; j < kChunks; ++j) {
-            const int idx = lane + j * kWarp;
-            if (idx >= 1 && idx <= L) {
-              const float4 t = __ldg(src + idx - 1);
-              const float B = (t.y * qb + t.x * qa) + t.z * qc;
-              const float dVB = d[j] * B;
-              acc_ne += W * dVB;
-              acc_sig += dW * dVB;
-              const float dVW = d[j] * W;
-              acc_a += dVW * t.x;
-              acc_b += dVW * t.y;
-              acc_c += dVW * t.z;
-            }
+            const float4 t = __ldg(src + j * kWarp);
+            sx = fmaf(d[j], t.x, sx);
+            sy = fmaf(d[j], t.y, sy);
+            sz = fmaf(d[j], t.z, sz);
           }
+          const float W = ms.W[e], dW = ms.dW[e];
+          const float sB = (sy * qb + sx * qa) + sz * qc;
+          acc_ne = fmaf(W, sB, acc_ne);
+          acc_sig = fmaf(dW, sB, acc_sig);
+          acc_a = fmaf(W, sx, acc_a);
+          acc_b = fmaf(W, sy, acc_b);
+          acc_c = fmaf(W, sz, acc_c);
         }
         if (lane < n) {
           acc_ne += dcorr * ms.W[lane] * ms.D[lane];
