@@ -46,7 +46,12 @@ N_NEIGH, SIG_LEN = 4, 150
 PERTURB_SEED = 1234
 L2_FLUSH_BYTES = 512 << 20
 CPU_CHUNK = 150          # segments per CPU reference sample (one run per process)
-KERNELS_PER_STEP = 11   # reset, segments, 3 scan, scatter, sort, pixels, pixel reduce, target-only, finalize
+KERNELS_PER_STEP = 14   # stage 1: reset, segments, 3 scan, scatter, sort; gradient: main records, pixels,
+                        # main adjoint, 2 record reductions, target-only, finalize
+# DRAM bytes per simulated pixel of one k_lut_pixels<grad> launch, from the
+# ncu capture summarised in profiles/k_lut_pixels_grad_8events.md (8 events,
+# 22,066 pixels; traffic scales with the pixel count)
+PIXEL_KERNEL_DRAM_BYTES_PER_PIXEL = 13945   # 307.7 MB over 22,066 pixels
 
 
 def parse():
@@ -184,10 +189,12 @@ def run_ours(args):
     out = None
     for i in range(args.steps):
         flush.fill_(float(i))              # evict L2 between steps (untimed)
+        _abi.set_kernel_events(*kev[i])    # events around the pixel kernel of this step
         starts[i].record()
-        out = step(kev[i])
+        out = step()
         ends[i].record()
     torch.cuda.synchronize()
+    _abi.set_kernel_events(None, None)
     wall = time.perf_counter() - t_wall
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     kern_ms = [a.elapsed_time(b) for a, b in kev]
@@ -211,14 +218,20 @@ def run_ours(args):
         loss, g = grad.lut_value_and_grad(pp, tmpl, host, fields, target, n_events=n_events)
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    # ---- roofline of the fused forward+adjoint kernel (algorithmic bytes)
-    T, H, F_u = 2000, int(params.MAX_ADC_VALUES), 7
+    # ---- roofline of the dominant kernel, k_lut_pixels<grad> (algorithmic bytes)
+    counts = st.counts_dev.cpu().numpy()
+    n_rec = int(counts[7])                 # main-bin records of the last accumulation
+    H = int(params.MAX_ADC_VALUES)
     lut = chain.lut
-    w_lut = lut_bytes_touched(seg_rec[ne > 0, 6], lut.n_templates, lut.shape[1], lut.shape[2], SIG_LEN,
-                              lut.shape[3])
-    a_fwd = 4 * F_u * active + 4 * T * n_pix + 8 * n_pix + 8 * H * n_pix + 4 * w_lut
-    a_fb = a_fwd + 4 * F_u * active + 4 * T * n_pix + 4 * 8 * active + 4 * w_lut
-    a_kernel = a_fb - 2 * 4 * F_u * active       # track columns are read by the segment kernel
+    n_tgt = int(target.pids.numel())
+    halo = max(N_NEIGH, 1)
+    a_kernel = (192 * active                         # per-segment forward + adjoint records
+                + 4 * n_seg                          # slot-sorted segment list
+                + 8 * (2 * halo + 1) ** 2 * n_pix    # neighbourhood slot counts / offsets
+                + 4 * lut.shape[1] * lut.shape[2] * (160 + lut.shape[3])  # template-0 windows + cumulative sums
+                + 656 * n_rec + 640 * n_rec          # main-bin records in, their cotangents out
+                + (4 + 4 * H) * n_tgt                # target pixels and ADCs
+                + 48 * n_pix)                        # per-pixel loss / gradient records
     k_ms = float(np.mean(kern_ms))
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
@@ -226,6 +239,7 @@ def run_ours(args):
         peaks = json.loads(pk.read_text())
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = a_kernel / (k_ms * 1e-3) / 1e9
+    traffic = None if PIXEL_KERNEL_DRAM_BYTES_PER_PIXEL is None else int(PIXEL_KERNEL_DRAM_BYTES_PER_PIXEL * n_pix)
     rec = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -237,10 +251,10 @@ def run_ours(args):
                    "l2": "flushed between timed steps (512 MiB write)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": n_seg * world / e2e_s, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
                 "h2d_bytes_per_step": int(tracks.nbytes), "d2h_bytes_per_step": 4 * (1 + 8)},
-        "roofline": {"bound": "hbm", "kernel": "k_lut_pixels<grad> (fused forward+FEE+loss+adjoint)",
+        "roofline": {"bound": "hbm", "kernel": "k_lut_pixels<grad> (pixel-major forward + front end + loss + adjoint)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "algorithmic_bytes": int(a_kernel), "kernel_ms": k_ms,
-                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None},
+                     "algorithmic_bytes": int(a_kernel), "kernel_ms": k_ms, "main_records": n_rec,
+                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": traffic},
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "clocks": clk,
         "wall_s_timed": wall,
@@ -258,14 +272,21 @@ def run_ours(args):
 
 def _event_sample(tracks, fields, k, chunk=None):
     """k samples from the smallest events; with ``chunk`` each sample is a
-    run of ``chunk`` consecutive segments of the smallest event."""
+    run of ``chunk`` consecutive segments, taken from the smallest events in
+    turn until there are k runs."""
     ev = tracks[:, fields.index("eventID")].astype(int)
     counts = np.bincount(ev)
-    order = np.argsort(counts)
+    order = np.argsort(counts, kind="stable")
+    out = []
     if chunk:
-        rows = tracks[ev == order[0]]
-        out = [rows[i * chunk:(i + 1) * chunk].copy() for i in range(k)]
-        out = [r for r in out if len(r)]
+        for e in order:
+            rows = tracks[ev == e]
+            for i in range(len(rows) // chunk):
+                out.append(rows[i * chunk:(i + 1) * chunk].copy())
+                if len(out) == k:
+                    break
+            if len(out) == k:
+                break
     else:
         out = [tracks[ev == e].copy() for e in order[:k]]
     for r in out:
@@ -274,7 +295,7 @@ def _event_sample(tracks, fields, k, chunk=None):
 
 
 def _cpu_step(args_tuple):
-    """Oracle forward + FP64 pathwise gradient (central differences) of one event."""
+    """Oracle forward + FP64 loss and reverse-mode gradient of one sample."""
     tmpl_path, tracks, fields, params, pp = args_tuple
     from oracle import grad64, reference_np as R
     tmpl = np.load(tmpl_path, mmap_mode="r")
@@ -285,7 +306,7 @@ def _cpu_step(args_tuple):
     fr = grad64.Frozen(pp, tmpl, tracks, fields, u[v], o["grid_adcs"][v])
     th = grad64.theta_dict(pp)
     grad64.loss64(fr, th)
-    grad64.fd_gradient(fr, th)
+    grad64.adjoint64(fr, th)
     return time.perf_counter() - t0, tracks.shape[0]
 
 
@@ -311,7 +332,7 @@ def cpu_baseline(tracks, fields, params, pp, resp, sample_events=2, processes=1)
     return {"value": segs / wall, "unit": UNIT, "cores": processes, "kind": "port",
             "sample": f"{len(sample)} smallest events ({segs} segments): numpy float32 forward "
                       f"(simulate_wfs + simulate_stochastic restatement) + FP64 frozen-decision loss "
-                      f"with an 8-parameter central-difference gradient, {wall:.1f} s"}
+                      f"and its reverse-mode gradient in the 8 parameters, {wall:.1f} s"}
 
 
 def run_reference(args):
@@ -351,12 +372,12 @@ def run_reference(args):
            "config": {"workload": "batched fwd+bwd LUT mode (same generator, n_neighbors=4, L=150, "
                                   "100x45x45x1950 templates), CPU sample: consecutive segment runs of the "
                                   "smallest event",
-                      "segments_per_step": segs, "events_per_step": len(sample)},
+                      "segments_per_step": segs, "samples_per_step": len(sample)},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
                             "sample": f"{len(sample)} runs of {CPU_CHUNK} consecutive segments of the smallest "
-                                      f"event, {segs} segments per step, one process per run: float32 numpy "
-                                      "restatement forward + FP64 frozen-decision central-difference gradient "
-                                      "of the 8 parameters"},
+                                      f"events, {segs} segments per step, one process per run: float32 numpy "
+                                      "restatement forward + FP64 frozen-decision loss and reverse-mode "
+                                      "gradient in the 8 parameters"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(rec), flush=True)
 

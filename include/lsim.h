@@ -91,7 +91,8 @@ typedef struct LsimCounts {
   int32_t max_slot;     /* largest number of segments sharing one pixel */
   int32_t bad_row;      /* first offending track row, or -1 */
   int32_t work;         /* internal work counter */
-  int32_t reserved[9];
+  int32_t n_main_rec;   /* main-bin records written by the last LUT accumulation */
+  int32_t reserved[8];
 } LsimCounts;
 
 int lsim_abi_version(void);
@@ -100,6 +101,13 @@ const char *lsim_last_error(void);
 /* sizeof(LsimParams), sizeof(LsimFieldMap), sizeof(LsimCounts), so a
  * binding can check its structure layout against the library. */
 void lsim_struct_sizes(size_t *params, size_t *fields, size_t *counts);
+
+/* Profiling hook: when both are non-null, the calling thread's subsequent
+ * lsim_lut_stage2 / lsim_lut_adc / lsim_lut_grad calls record start/stop
+ * (cudaEvent_t handles) on their stream around the pixel-accumulation
+ * kernel, the dominant launch of the LUT path; null, null turns it off.
+ * Not part of the reference interface. */
+void lsim_set_kernel_events(void *start, void *stop);
 
 /* ---------------------------------------------------------------- LUT */
 

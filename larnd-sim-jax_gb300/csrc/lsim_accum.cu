@@ -713,8 +713,13 @@ static int launch_mode(const AccumArgs &a0, cudaStream_t st) {
   AccumArgs a = a0;
   a.warp_smem = (int)warp_smem_bytes<MODE>(a0.p);
   if (cudaMemsetAsync(&a.w.counts->work, 0, sizeof(int32_t), st) != cudaSuccess) return LSIM_ERR_CUDA;
+  cudaEvent_t ev0, ev1;
+  kernel_events(&ev0, &ev1);
+  if (ev0 && cudaEventRecord(ev0, st) != cudaSuccess) return LSIM_ERR_CUDA;
   k_lut_pixels<MODE><<<blocks, kAccWarps * kWarp, smem, st>>>(a);
-  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return LSIM_ERR_CUDA;
+  if (ev1 && cudaEventRecord(ev1, st) != cudaSuccess) return LSIM_ERR_CUDA;
+  return LSIM_OK;
 }
 
 int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st) {

@@ -75,6 +75,12 @@ static int check_fields(const LsimFieldMap *f) {
   return LSIM_OK;
 }
 
+static thread_local cudaEvent_t g_ev_start = nullptr, g_ev_stop = nullptr;
+void kernel_events(cudaEvent_t *start, cudaEvent_t *stop) {
+  *start = g_ev_start;
+  *stop = g_ev_stop;
+}
+
 }  // namespace lsim
 
 using namespace lsim;
@@ -82,6 +88,12 @@ using namespace lsim;
 extern "C" {
 
 int lsim_abi_version(void) { return LSIM_ABI_VERSION; }
+
+void lsim_set_kernel_events(void *start, void *stop) {
+  const bool on = start != nullptr && stop != nullptr;
+  lsim::g_ev_start = on ? (cudaEvent_t)start : nullptr;
+  lsim::g_ev_stop = on ? (cudaEvent_t)stop : nullptr;
+}
 
 const char *lsim_last_error(void) { return g_err.c_str(); }
 

@@ -56,6 +56,9 @@ int run_prepare_tables(const LsimParams &p, const float *templates, void *tables
 
 int device_sm_count();
 
+// profiling events around the pixel-accumulation kernel (lsim_set_kernel_events)
+void kernel_events(cudaEvent_t *start, cudaEvent_t *stop);
+
 // lsim_api.cu: thread-local error message shared by all entry points
 int set_error(int code, const char *msg);
 void clear_error();

@@ -98,7 +98,8 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_records(LsimPa
   __shared__ MainSmem sms[kMainBlockWarps];
   const int lane = threadIdx.x % kWarp;
   MainSmem &ms = sms[threadIdx.x / kWarp];
-  const int L = p.signal_length, nbp = p.nb_bins_per_pixel;
+  const int nbp = p.nb_bins_per_pixel;
+  int n_rec = 0;
   int64_t s0, s1;
   warp_range(n_rows, &s0, &s1);
   for (int64_t s = s0; s < s1; ++s) {
@@ -139,9 +140,11 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_records(LsimPa
           rec[idx] = idx == 0 ? wd * ne : acc[j] * ne;
         }
         if (lane == 0) rec[kRecDl] = wdl * ne;
+        ++n_rec;
         __syncwarp();
       }
   }
+  if (lane == 0 && n_rec) atomicAdd(&w.counts->n_main_rec, n_rec);
 }
 
 __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 4) k_main_adjoint(LsimParams p, Tables tab, Workspace w, Grid g,
@@ -228,6 +231,7 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 4) k_main_adjoint(Lsi
 }
 
 int run_main_records(const AccumArgs &a, cudaStream_t st) {
+  if (cudaMemsetAsync(&a.w.counts->n_main_rec, 0, sizeof(int32_t), st) != cudaSuccess) return LSIM_ERR_CUDA;
   if (a.n_rows <= 0) return LSIM_OK;
   k_main_records<<<kMainWarps / kMainBlockWarps, kMainBlockWarps * kWarp, 0, st>>>(a.p, a.tab, a.w, a.g, a.n_rows);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;

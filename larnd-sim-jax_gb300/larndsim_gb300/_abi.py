@@ -61,8 +61,8 @@ class LsimParams(C.Structure):
 
 
 class LsimCounts(C.Structure):
-    _fields_ = [(n, C.c_int32) for n in ("n_valid", "n_em1", "any_m1", "status", "max_slot", "bad_row", "work")] + [
-        ("reserved", C.c_int32 * 9)]
+    _fields_ = [(n, C.c_int32) for n in ("n_valid", "n_em1", "any_m1", "status", "max_slot", "bad_row", "work",
+                                         "n_main_rec")] + [("reserved", C.c_int32 * 8)]
 
 
 _vp, _i64, _i32, _sz = C.c_void_p, C.c_int64, C.c_int32, C.c_size_t
@@ -72,6 +72,7 @@ _SIGNATURES = {
     "lsim_abi_version": (C.c_int, []),
     "lsim_last_error": (C.c_char_p, []),
     "lsim_struct_sizes": (None, [C.POINTER(_sz)] * 3),
+    "lsim_set_kernel_events": (None, [_vp, _vp]),
     "lsim_lut_build_templates": (C.c_int, [_vp, _i32, _i32, _i32, _vp, _i32, _i32, _vp, _vp]),
     "lsim_lut_tables_bytes": (_sz, [_PP]),
     "lsim_lut_prepare": (C.c_int, [_PP, _vp, _vp, _sz, _vp]),
@@ -129,6 +130,20 @@ def load(path: Path | None = None):
         if path is None:
             _lib = lib
         return lib
+
+
+def set_kernel_events(start=None, stop=None):
+    """Record torch.cuda.Event ``start``/``stop`` around the pixel
+    accumulation kernel of every following LUT call on this thread
+    (``None`` turns it off).  The events are recorded once here first so
+    that their CUDA handles exist."""
+    lib = load()
+    if start is None or stop is None:
+        lib.lsim_set_kernel_events(None, None)
+        return
+    start.record()
+    stop.record()
+    lib.lsim_set_kernel_events(C.c_void_p(start.cuda_event), C.c_void_p(stop.cuda_event))
 
 
 def check(lib, rc: int):

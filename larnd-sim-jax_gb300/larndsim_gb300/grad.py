@@ -107,7 +107,7 @@ class LUTChain:
     def loss_and_grad_device(self, params, target: Target, normals=None, events=None):
         """Like ``loss_and_grad`` but returns the device tensor [loss, grads...]
         without a host synchronisation.  ``events`` (start, end) CUDA events,
-        if given, bracket the fused forward+adjoint kernel."""
+        if given, bracket the lsim_lut_grad call (all gradient kernels)."""
         return self._grad(params, target=target, normals=normals, sync=False, events=events)
 
     def set_tracks(self, tracks):
