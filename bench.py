@@ -218,20 +218,29 @@ def run_ours(args):
         loss, g = grad.lut_value_and_grad(pp, tmpl, host, fields, target, n_events=n_events)
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    # ---- roofline of the dominant kernel, k_lut_pixels<grad> (algorithmic bytes)
+    # ---- roofline of the dominant kernel, k_lut_pixels<grad>
+    # Algorithmic bytes: the fixed per-unit formula of the path (S active
+    # segments, P pixels, T ticks, H hits, F_u consumed track columns, W_LUT
+    # distinct LUT floats): A_fwd = 4 F_u S + 4 T P + 8 P + 8 H P + 4 W_LUT,
+    # A_fwd+bwd = A_fwd + 4 F_u S + 4 T P + 32 S + 4 W_LUT; the pixel kernel is
+    # charged A_fwd+bwd - 8 F_u S (the track columns are read by k_segments_lut).
+    T, H, F_u = 2000, int(params.MAX_ADC_VALUES), 7
+    lut = chain.lut
+    w_lut = lut_bytes_touched(seg_rec[ne > 0, 6], lut.n_templates, lut.shape[1], lut.shape[2], SIG_LEN,
+                              lut.shape[3])
+    a_fwd = 4 * F_u * active + 4 * T * n_pix + 8 * n_pix + 8 * H * n_pix + 4 * w_lut
+    a_fb = a_fwd + 4 * F_u * active + 4 * T * n_pix + 4 * 8 * active + 4 * w_lut
+    a_kernel = a_fb - 2 * 4 * F_u * active
+    # Bytes this design must move in that launch (it keeps waveforms on chip):
+    # segment records, slot lists, LUT windows + cumulative sums, main-bin
+    # records in and their cotangents out, targets, per-pixel records.
     counts = st.counts_dev.cpu().numpy()
     n_rec = int(counts[7])                 # main-bin records of the last accumulation
-    H = int(params.MAX_ADC_VALUES)
-    lut = chain.lut
     n_tgt = int(target.pids.numel())
     halo = max(N_NEIGH, 1)
-    a_kernel = (192 * active                         # per-segment forward + adjoint records
-                + 4 * n_seg                          # slot-sorted segment list
-                + 8 * (2 * halo + 1) ** 2 * n_pix    # neighbourhood slot counts / offsets
-                + 4 * lut.shape[1] * lut.shape[2] * (160 + lut.shape[3])  # template-0 windows + cumulative sums
-                + 656 * n_rec + 640 * n_rec          # main-bin records in, their cotangents out
-                + (4 + 4 * H) * n_tgt                # target pixels and ADCs
-                + 48 * n_pix)                        # per-pixel loss / gradient records
+    design_bytes = (192 * active + 4 * n_seg + 8 * (2 * halo + 1) ** 2 * n_pix
+                    + 4 * lut.shape[1] * lut.shape[2] * (160 + lut.shape[3])
+                    + (656 + 640) * n_rec + (4 + 4 * H) * n_tgt + 48 * n_pix)
     k_ms = float(np.mean(kern_ms))
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
@@ -253,7 +262,8 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(tracks.nbytes), "d2h_bytes_per_step": 4 * (1 + 8)},
         "roofline": {"bound": "hbm", "kernel": "k_lut_pixels<grad> (pixel-major forward + front end + loss + adjoint)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "algorithmic_bytes": int(a_kernel), "kernel_ms": k_ms, "main_records": n_rec,
+                     "algorithmic_bytes": int(a_kernel), "design_bytes": int(design_bytes), "kernel_ms": k_ms,
+                     "main_records": n_rec,
                      "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": traffic},
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "clocks": clk,
