@@ -45,13 +45,19 @@ struct NBatch {
   float dne[5][kWarp], dt0[kWarp];   // adjoint only
 };
 
+// Compacted neighbourhood slot list of one pixel.  cd packs the slot's
+// segment count (bits 8..31, at most kMaxSlotSegments, checked in stage 1)
+// with its offset from the pixel, (dx + 4) | (dy + 4) << 4 (bits 0..7).
 struct ListSmem {
   int off[kMaxList];
-  int cnt[kMaxList];
-  int dxy[kMaxList];
+  int cd[kMaxList];
   int pre_n[kMaxList + 1];   // prefix of neighbour contributions (centre slot excluded)
   int n;
 };
+
+__device__ __forceinline__ int list_count(int cd) { return cd >> 8; }
+__device__ __forceinline__ int list_dx(int cd) { return (cd & 15) - 4; }
+__device__ __forceinline__ int list_dy(int cd) { return ((cd >> 4) & 15) - 4; }
 
 
 // ---------------------------------------------------------------- neighbour batches
@@ -64,9 +70,9 @@ __device__ __forceinline__ bool neigh_lookup(const ListSmem &ls, const int32_t *
     int mid = (lo + hi) >> 1;
     if (ls.pre_n[mid] <= g) lo = mid; else hi = mid;
   }
-  const int dxy = ls.dxy[lo];
-  *dx = (dxy & 0xff) - 16;
-  *dy = ((dxy >> 8) & 0xff) - 16;
+  const int cd = ls.cd[lo];
+  *dx = list_dx(cd);
+  *dy = list_dy(cd);
   if (*dx == 0 && *dy == 0) return false;
   *s = __ldg(seg_list + ls.off[lo] + (g - ls.pre_n[lo]));
   return true;
@@ -136,8 +142,10 @@ __device__ __forceinline__ bool window_interior(int cb, int L, int NT) {
 
 // Window that crosses the edge of the waveform: value parts are kept only
 // in columns [2, Nticks-1], correction parts only in [1, Nticks-2].
-__device__ __noinline__ void window_apply_edge(const float U[kChunks], int cb, int rl, float a, float b, int L,
-                                               int NT, float *row, int lane) {
+__device__ __noinline__ void window_apply_edge(float U0, float U1, float U2, float U3, float U4, int cb, int rl,
+                                               float a, float b, int L, int NT, float *row, int lane) {
+  static_assert(kChunks == 5, "window_apply_edge takes the five chunks by value");
+  const float U[kChunks] = {U0, U1, U2, U3, U4};
   float sprev = 0.f;
 #pragma unroll
   for (int j = 0; j < kChunks; ++j) {
@@ -170,7 +178,7 @@ __device__ __forceinline__ void window_apply(const float U[kChunks], int cb, int
       x = fmaf(U[j], b, fmaf(prev, a, x));
     }
   } else {
-    window_apply_edge(U, cb, rl, a, b, L, NT, row, lane);
+    window_apply_edge(U[0], U[1], U[2], U[3], U[4], cb, rl, a, b, L, NT, row, lane);
   }
 }
 
@@ -312,10 +320,10 @@ __device__ __forceinline__ void main_batches(const LsimParams &p, const Workspac
   const int nbp = p.nb_bins_per_pixel;
   int m = 0;
   for (int e = 0; e < ls.n; ++e) {
-    const int dxy = ls.dxy[e];
-    const int dx = (dxy & 0xff) - 16, dy = ((dxy >> 8) & 0xff) - 16;
+    const int cd = ls.cd[e];
+    const int dx = list_dx(cd), dy = list_dy(cd);
     if (dx < -1 || dx > 1 || dy < -1 || dy > 1) continue;
-    const int o = ls.off[e], c = ls.cnt[e];
+    const int o = ls.off[e], c = list_count(cd);
     for (int j0 = 0; j0 < c; j0 += kWarp) {
       int s = 0, slot = 0;
       bool hit = false;
@@ -459,7 +467,7 @@ __device__ __forceinline__ void build_list(const Grid &g, const int32_t *__restr
       const int64_t q = slot - (int64_t)dy * g.nxe - dx;
       c = __ldg(cnt + q);
       if (c > 0) o = __ldg(off + q);
-      dxy = (dx + 16) | ((dy + 16) << 8);
+      dxy = (dx + 4) | ((dy + 4) << 4);
       neigh = !(dx == 0 && dy == 0) && abs(dx) <= g.n && abs(dy) <= g.n;
     }
     const bool has = c > 0;
@@ -473,8 +481,7 @@ __device__ __forceinline__ void build_list(const Grid &g, const int32_t *__restr
     if (has) {
       const int pos = base + __popc(bal & ((1u << lane) - 1u));
       ls.off[pos] = o;
-      ls.cnt[pos] = c;
-      ls.dxy[pos] = dxy;
+      ls.cd[pos] = (c << 8) | dxy;
       ls.pre_n[pos] = nbase + incl - nc;
     }
     base += __popc(bal);
@@ -497,14 +504,14 @@ __device__ __forceinline__ int32_t slot_pid(const LsimParams &p, const Grid &g, 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kAccWarps * kWarp, 4) k_lut_pixels(AccumArgs a) {
+__global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a) {
   constexpr bool GRAD = (MODE == kModeGrad);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x % kWarp, wid = threadIdx.x / kWarp;
   unsigned char *wbase = smem_raw + (size_t)wid * a.warp_smem;
   WarpSmem<GRAD> &sm = *reinterpret_cast<WarpSmem<GRAD> *>(wbase);
   if constexpr (GRAD) {
-    if (lane == 0) sm.fee.mask = reinterpret_cast<uint32_t *>(wbase + sizeof(WarpSmem<true>));
+    if (lane == 0) sm.fee.mask = a.w.fee_masks + (size_t)(blockIdx.x * kAccWarps + wid) * kFeeMaskWords;
     __syncwarp();
   }
   const LsimParams &p = a.p;
@@ -678,13 +685,11 @@ __global__ void k_grad_finalize(const double *partials, int n_rec_blocks, const 
 // ---------------------------------------------------------------- launch
 
 // Persistent grid: every SM filled to its occupancy limit.
-// Per-warp shared memory: the WarpSmem block, then (adjoint mode) the
-// per-hit reset masks of the front end, max_adc_values x kMaskWords words.
+// Per-warp shared memory (the front end's reset masks live in the
+// workspace, one kFeeMaskWords block per warp).
 template <int MODE>
-static size_t warp_smem_bytes(const LsimParams &p) {
-  size_t b = sizeof(WarpSmem<MODE == kModeGrad>);
-  if (MODE == kModeGrad) b += sizeof(uint32_t) * kMaskWords * (size_t)p.max_adc_values;
-  return (b + 15) & ~size_t(15);
+static size_t warp_smem_bytes(const LsimParams &) {
+  return (sizeof(WarpSmem<MODE == kModeGrad>) + 15) & ~size_t(15);
 }
 
 // Persistent grid: every SM filled to its occupancy limit.
@@ -699,7 +704,7 @@ static int grid_blocks(const LsimParams &p, int *blocks, size_t *smem_out) {
       cudaSuccess)
     return LSIM_ERR_CUDA;
   if (per_sm < 1) per_sm = 1;
-  *blocks = device_sm_count() * per_sm;
+  *blocks = min(device_sm_count() * per_sm, kMaxPixelWarps / kAccWarps);
   *smem_out = smem;
   return LSIM_OK;
 }

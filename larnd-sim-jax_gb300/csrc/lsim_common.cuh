@@ -16,6 +16,7 @@ constexpr int kWarp = 32;
 constexpr int kMaxNeigh = 8;             // number_pix_neighbors supported: 0..8
 constexpr int kMaxTran = 5;              // nb_tran_diff_bins supported: 5
 constexpr int kMainSub = 5;              // main-bin LUT sub-positions (nb_bins_per_pixel / 2)
+constexpr int kMaxSlotSegments = (1 << 23) - 1;   // segments sharing one principal pixel
 constexpr int kWinSamples = 160;         // padded window samples k = -1 .. 158 (signal_length <= 158)
 constexpr int kScanTile = 2048;          // slots per scan block
 constexpr int kScanThreads = 256;
@@ -107,6 +108,7 @@ struct Workspace {
   float *pix_out;           // per valid pixel: [loss, 8 gradient terms] (kPixRec floats)
   double *red_partials;     // fixed-order reduction partials (kRedSlots * 16 doubles)
   float *mrec;              // main-bin records: kMainRecPerSeg per segment, kMainRecFloats each
+  uint32_t *fee_masks;      // per pixel-kernel warp: front-end reset masks (kFeeMaskWords)
   float *main_out;          // per main-adjoint warp: [0, 8 gradient terms] (kPixRec floats)
   size_t bytes;
 };
@@ -116,6 +118,8 @@ constexpr int kRedSlots = 4096;  // reduction blocks (pixels + main-bin warps + 
 constexpr int kMainWarps = 8192; // warps of the segment-major main-bin kernels
 constexpr int kMainRecPerSeg = 4;      // a segment's main bins cover at most 2 x 2 pixels
 constexpr int kMainRecFloats = 164;    // window of 160 samples + d(corr)/d(frac), padded to 16 bytes
+constexpr int kMaxPixelWarps = 8192;   // warps of the persistent pixel kernel
+constexpr int kFeeMaskWords = LSIM_MAX_HITS * 64;   // reset masks per warp: hits x (2 words per lane)
 
 inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows, int32_t n_events) {
   Grid g = make_grid(p, n_events);
@@ -139,6 +143,7 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   size_t o_red = take(8 * (size_t)kRedSlots * 16);
   size_t o_mrec = take(4 * (size_t)kMainRecFloats * kMainRecPerSeg * (size_t)n_rows);
   size_t o_mout = take(4 * (size_t)kPixRec * kMainWarps);
+  size_t o_fmask = take(4 * (size_t)kFeeMaskWords * kMaxPixelWarps);
   Workspace w;
   char *b = (char *)base;
   w.counts = (LsimCounts *)(b + o_counts);
@@ -158,6 +163,7 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   w.red_partials = (double *)(b + o_red);
   w.mrec = (float *)(b + o_mrec);
   w.main_out = (float *)(b + o_mout);
+  w.fee_masks = (uint32_t *)(b + o_fmask);
   w.bytes = off;
   return w;
 }

@@ -15,6 +15,7 @@
 namespace lsim {
 
 constexpr int kMaskWords = 64;   // words per hit: 2 per lane, bit 4m + q for tick 128m + 4 lane + q (T <= 2048)
+static_assert(kFeeMaskWords == LSIM_MAX_HITS * kMaskWords, "reset-mask scratch per warp");
 constexpr int kFeePass = 4 * kWarp;   // ticks per warp pass: lane l holds ticks 4l .. 4l + 3
 
 struct FeeState {

@@ -439,6 +439,7 @@ __global__ void k_sort_slots(const int32_t *__restrict__ cnt, const int32_t *__r
   int c = cnt[slot];
   if (c <= 1) return;
   atomicMax(&counts->max_slot, c);
+  if (c > kMaxSlotSegments) atomicCAS(&counts->status, 0, (int)LSIM_ERR_CAPACITY);
   int32_t *l = seg_list + off[slot];
   for (int i = 1; i < c; ++i) {
     int32_t x = l[i];

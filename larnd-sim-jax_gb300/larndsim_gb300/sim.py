@@ -180,6 +180,8 @@ class Stage1:
 
     def raise_status(self):
         c = self.counts()
+        if c[3] == _abi.LSIM_ERR_CAPACITY:
+            raise ValueError(f"{int(c[4])} segments share one principal pixel; at most {(1 << 23) - 1} are supported")
         if c[3] != 0:
             row = int(c[5])
             raise ValueError(f"invalid track input: eventID outside [-1, {self.n_events}) at row {row} "
