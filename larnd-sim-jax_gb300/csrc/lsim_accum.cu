@@ -37,13 +37,30 @@ constexpr int kRowPad = 3;            // row[col] at buf[kRowPad + col]: col 1 i
 constexpr int kRowFloats = 2052;      // >= kRowPad + n_ticks (2001), multiple of 4
 constexpr int kMaxList = 81;          // (2 * 4 + 1)^2 neighbourhood slots
 
-// Descriptors of one batch of 32 neighbour contributions (structure of arrays).
-struct NBatch {
-  int row[kWarp];       // LUT row (cx * ny + cy) of template 0, -1 = skip
-  int cb[kWarp];        // window origin column
-  float frac[kWarp], ne[kWarp], D[kWarp], dl[kWarp];
-  float dne[5][kWarp], dt0[kWarp];   // adjoint only
+// Descriptor of one contribution, written by one lane of the batch setup
+// and read by the whole warp with 16-byte broadcast loads.
+//   neighbour, forward:  w = (n_e (1 - f), n_e f, D, pack)
+//   neighbour, adjoint:  w = (f, 1 - f, D, pack), g0 = (dD/df, n_e dt0/ts, dn_e[4], 0),
+//                        g1 = dn_e[0..3]
+//   main-bin record:     w = (1 - f, f, d corr/df, pack), g0 = (dt0/ts, record index, 0, 0)
+// with pack = window origin + 16384 in bits 16..30, the LUT row in bits
+// 0..14 (0 for records) and bit 15 set for a window that is not interior;
+// pack = -1 marks an empty descriptor (valid packs are non-negative).
+struct __align__(16) NDesc {
+  float4 w, g0, g1;
 };
+struct NBatch {
+  NDesc d[kWarp];
+};
+constexpr int kPackEdge = 1 << 15;
+constexpr int kPackRowMask = kPackEdge - 1;
+
+constexpr int kPackCbBias = 1 << 14;   // window origins in [-16384, 16383]
+
+__device__ __forceinline__ float pack_window(int row, int cb, bool interior) {
+  return __int_as_float(((cb + kPackCbBias) << 16) | row | (interior ? 0 : kPackEdge));
+}
+__device__ __forceinline__ int pack_cb(int pk) { return (pk >> 16) - kPackCbBias; }
 
 // Compacted neighbourhood slot list of one pixel.  cd packs the slot's
 // segment count (bits 8..31, at most kMaxSlotSegments, checked in stage 1)
@@ -81,38 +98,7 @@ __device__ __forceinline__ bool neigh_lookup(const ListSmem &ls, const int32_t *
 // Lane-parallel descriptor setup for neighbour contributions [g0, g0 + 32).
 template <bool GRAD>
 __device__ __forceinline__ void neigh_setup(const LsimParams &p, const Tables &tab, const Workspace &w,
-                                            const ListSmem &ls, NBatch &nb, int g0, int n_total, int lane) {
-  const int g = g0 + lane;
-  int row = -1, cb = 0, s = 0, dx = 0, dy = 0;
-  float frac = 0.f, ne = 0.f, D = 0.f, dl = 0.f;
-  if (g < n_total && neigh_lookup(ls, w.seg_list, g, &s, &dx, &dy)) {
-    const SegFwd &f = w.segf[s];
-    ne = __ldg(&f.ne);
-    if (ne != 0.f) {
-      const int nbp = p.nb_bins_per_pixel;
-      const int cx = lut_index(__ldg(&f.bx), nbp, dx * nbp);
-      const int cy = lut_index(__ldg(&f.by), nbp, dy * nbp);
-      row = cx * p.lut_ny + cy;
-      const int cath = __ldg(&f.cath);
-      frac = __ldg(&f.frac);
-      cb = p.lut_nt - p.signal_length - cath - 1;
-      D = cum_terms(tab.c0 + (size_t)row * p.lut_nt, cath, p.lut_nt, p.signal_length, frac, &dl);
-      if (GRAD) {
-        const SegAdj &a = w.sega[s];
-#pragma unroll
-        for (int i = 0; i < 5; ++i) nb.dne[i][lane] = __ldg(&a.dne[i]);
-        nb.dt0[lane] = __ldg(&a.dt0);
-      }
-    }
-  }
-  nb.row[lane] = row;
-  nb.cb[lane] = cb;
-  nb.frac[lane] = frac;
-  nb.ne[lane] = ne;
-  nb.D[lane] = D;
-  nb.dl[lane] = dl;
-  __syncwarp();
-}
+                                            const ListSmem &ls, NBatch &nb, int g0, int n_total, int lane);
 
 // Forward window update with a column-owner lane map: lane l handles the
 // window positions r with (cb + r) = l (mod 32), i.e. r = rl + 32j with
@@ -164,28 +150,62 @@ __device__ __noinline__ void window_apply_edge(float U0, float U1, float U2, flo
   }
 }
 
-__device__ __forceinline__ void window_apply(const float U[kChunks], int cb, int rl, float a, float b, int L, int NT,
-                                             float *row, int lane) {
-  if (window_interior(cb, L, NT)) {
-    // interior: all columns valid; positions past L + 1 add exact zeros
-    float sprev = 0.f;
+// Interior window (window_interior): all columns valid; positions past
+// L + 1 add exact zeros.
+__device__ __forceinline__ void window_apply_interior(const float U[kChunks], int cb, int rl, float a, float b,
+                                                      float *row, int lane) {
+  float sprev = 0.f;
 #pragma unroll
-    for (int j = 0; j < kChunks; ++j) {
-      const float sh = __shfl_sync(0xffffffffu, U[j], (lane + kWarp - 1) & (kWarp - 1));
-      const float prev = rl == 0 ? sprev : sh;
-      sprev = sh;
-      float &x = row[cb + rl + j * kWarp];
-      x = fmaf(U[j], b, fmaf(prev, a, x));
-    }
-  } else {
-    window_apply_edge(U[0], U[1], U[2], U[3], U[4], cb, rl, a, b, L, NT, row, lane);
+  for (int j = 0; j < kChunks; ++j) {
+    const float sh = __shfl_sync(0xffffffffu, U[j], (lane + kWarp - 1) & (kWarp - 1));
+    const float prev = rl == 0 ? sprev : sh;
+    sprev = sh;
+    float &x = row[cb + rl + j * kWarp];
+    x = fmaf(U[j], b, fmaf(prev, a, x));
   }
+}
+
+template <bool GRAD>
+__device__ __forceinline__ void neigh_setup(const LsimParams &p, const Tables &tab, const Workspace &w,
+                                            const ListSmem &ls, NBatch &nb, int g0, int n_total, int lane) {
+  const int g = g0 + lane;
+  int s = 0, dx = 0, dy = 0;
+  NDesc d;
+  d.w = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+  d.g0 = make_float4(0.f, 0.f, 0.f, 0.f);
+  d.g1 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (g < n_total && neigh_lookup(ls, w.seg_list, g, &s, &dx, &dy)) {
+    const SegFwd &f = w.segf[s];
+    const float ne = __ldg(&f.ne);
+    if (ne != 0.f) {
+      const int nbp = p.nb_bins_per_pixel;
+      const int cx = lut_index(__ldg(&f.bx), nbp, dx * nbp);
+      const int cy = lut_index(__ldg(&f.by), nbp, dy * nbp);
+      const int row = cx * p.lut_ny + cy;
+      const int cath = __ldg(&f.cath);
+      const float frac = __ldg(&f.frac);
+      const int cb = p.lut_nt - p.signal_length - cath - 1;
+      float dl;
+      const float D = cum_terms(tab.c0 + (size_t)row * p.lut_nt, cath, p.lut_nt, p.signal_length, frac, &dl);
+      const float pk = pack_window(row, cb, window_interior(cb, p.signal_length, p.n_ticks));
+      if (GRAD) {
+        const SegAdj &a = w.sega[s];
+        d.w = make_float4(frac, 1.f - frac, D, pk);
+        d.g0 = make_float4(dl, ne * __ldg(&a.dt0) / p.t_sampling, __ldg(&a.dne[4]), 0.f);
+        d.g1 = make_float4(__ldg(&a.dne[0]), __ldg(&a.dne[1]), __ldg(&a.dne[2]), __ldg(&a.dne[3]));
+      } else {
+        d.w = make_float4(ne * (1.f - frac), ne * frac, D, pk);
+      }
+    }
+  }
+  nb.d[lane] = d;
+  __syncwarp();
 }
 
 // Template-0 window samples of a neighbour contribution (per electron),
 // with the boundary term D as sample k = -1 (padded table: idx = k + 1).
-__device__ __forceinline__ void neigh_samples(const Tables &tab, int rowidx, int rl, float D, float U[kChunks]) {
-  const float *src = tab.w0 + (size_t)(rowidx < 0 ? 0 : rowidx) * kWinSamples + rl;
+__device__ __forceinline__ void neigh_samples(const Tables &tab, int row, int rl, float D, float U[kChunks]) {
+  const float *src = tab.w0 + (size_t)row * kWinSamples + rl;
 #pragma unroll
   for (int j = 0; j < kChunks; ++j) U[j] = __ldg(src + j * kWarp);
   if (rl == 0) U[0] = D;
@@ -200,27 +220,26 @@ __device__ __forceinline__ void neigh_forward(const LsimParams &p, const Tables 
     neigh_setup<false>(p, tab, w, ls, nb, g0, n_total, lane);
     const int m = min(kWarp, n_total - g0);
     for (int j = 0; j < m; j += 4) {
-      float u0[kChunks], u1[kChunks], u2[kChunks], u3[kChunks];
-      const int r0 = nb.row[j];
-      const int r1 = j + 1 < m ? nb.row[j + 1] : -1;
-      const int r2 = j + 2 < m ? nb.row[j + 2] : -1;
-      const int r3 = j + 3 < m ? nb.row[j + 3] : -1;
-      const int c0 = nb.cb[j], c1 = nb.cb[j + 1], c2 = nb.cb[j + 2], c3 = nb.cb[j + 3];
-      const int l0 = owner_rl(c0, lane), l1 = owner_rl(c1, lane), l2 = owner_rl(c2, lane), l3 = owner_rl(c3, lane);
-      neigh_samples(tab, r0, l0, nb.D[j], u0);
-      neigh_samples(tab, r1, l1, nb.D[j + 1], u1);
-      neigh_samples(tab, r2, l2, nb.D[j + 2], u2);
-      neigh_samples(tab, r3, l3, nb.D[j + 3], u3);
-#define LSIM_NEIGH_APPLY(r, u, c, l, q)                                                                     \
-  if (r >= 0) {                                                                                          \
-    const float ne = nb.ne[j + q], f = nb.frac[j + q];                                                   \
-    window_apply(u, c, l, ne * (1.f - f), ne * f, L, NT, row, lane);                                     \
-  }
-      LSIM_NEIGH_APPLY(r0, u0, c0, l0, 0)
-      LSIM_NEIGH_APPLY(r1, u1, c1, l1, 1)
-      LSIM_NEIGH_APPLY(r2, u2, c2, l2, 2)
-      LSIM_NEIGH_APPLY(r3, u3, c3, l3, 3)
-#undef LSIM_NEIGH_APPLY
+      float u[4][kChunks];
+      float4 dw[4];
+      int pk[4], cb[4], rl[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        dw[q] = nb.d[j + q].w;                   // stale descriptors past m are masked below
+        pk[q] = j + q < m ? __float_as_int(dw[q].w) : -1;
+        cb[q] = pack_cb(pk[q]);
+        rl[q] = owner_rl(cb[q], lane);
+        neigh_samples(tab, pk[q] < 0 ? 0 : (pk[q] & kPackRowMask), rl[q], dw[q].z, u[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (pk[q] < 0) continue;
+        if (pk[q] & kPackEdge)
+          window_apply_edge(u[q][0], u[q][1], u[q][2], u[q][3], u[q][4], cb[q], rl[q], dw[q].x, dw[q].y, L, NT, row,
+                            lane);
+        else
+          window_apply_interior(u[q], cb[q], rl[q], dw[q].x, dw[q].y, row, lane);
+      }
     }
     __syncwarp();
   }
@@ -230,17 +249,18 @@ struct Theta {
   float v[LSIM_NPARAM];
 };
 
-// Adjoint of one neighbour contribution (descriptor j of the batch) given
-// its padded template-0 samples v[c] = w0[row][32c + lane] (sample
-// idx - 1 of the window, idx = 32c + lane): sample k lands on columns
-// cb + k + 1 (x frac) and cb + k + 2 (x (1 - frac)); lane 0's idx = 0 is the
-// boundary correction D * n_e (table value 0).  Accumulates dL/dtheta.
-__device__ __forceinline__ void neigh_vjp_one(const NBatch &nb, int j, const float v[kChunks], int L, int NT,
-                                              float inv_ts, const float *grow, Theta &th, int lane) {
-  const int cb = nb.cb[j];
-  const float f = nb.frac[j], f1 = 1.f - f, ne = nb.ne[j];
+// Adjoint of one neighbour contribution (descriptor d) given its padded
+// template-0 samples v[c] = w0[row][32c + lane] (sample idx - 1 of the
+// window, idx = 32c + lane): sample k lands on columns cb + k + 1 (x frac)
+// and cb + k + 2 (x (1 - frac)); lane 0's idx = 0 is the boundary
+// correction D * n_e (table value 0).  Accumulates dL/dtheta.
+__device__ __forceinline__ void neigh_vjp_one(const NDesc &d, const float v[kChunks], int L, int NT,
+                                              const float *grow, Theta &th, int lane) {
+  const int pk = __float_as_int(d.w.w);
+  const int cb = pack_cb(pk);
+  const float f = d.w.x, f1 = d.w.y, D = d.w.z;
   float sA = 0.f, sB = 0.f, gA0 = 0.f, gB0 = 0.f;   // sum v gA, sum v gB
-  if (window_interior(cb, L, NT)) {
+  if (!(pk & kPackEdge)) {
     // interior window: every column in range (columns past cb + L + 1 hold
     // zeros of the row padding and meet zero samples)
 #pragma unroll
@@ -269,19 +289,18 @@ __device__ __forceinline__ void neigh_vjp_one(const NBatch &nb, int j, const flo
   float acc_ne = sA * f + sB * f1, acc_fr = sA - sB;
   if (lane == 0) {
     const float dcorr = gA0 * f + gB0 * f1;
-    acc_ne += dcorr * nb.D[j];
-    acc_fr += dcorr * nb.dl[j] + nb.D[j] * (gA0 - gB0);
+    acc_ne += dcorr * D;
+    acc_fr += dcorr * d.g0.x + D * (gA0 - gB0);
   }
-  const float dt = acc_fr * ne * inv_ts;
-  th.v[0] += acc_ne * nb.dne[0][j];
-  th.v[1] += acc_ne * nb.dne[1][j];
-  th.v[2] += acc_ne * nb.dne[2][j] + dt * nb.dt0[j];
-  th.v[3] += acc_ne * nb.dne[3][j];
-  th.v[7] += acc_ne * nb.dne[4][j];
+  th.v[0] = fmaf(acc_ne, d.g1.x, th.v[0]);
+  th.v[1] = fmaf(acc_ne, d.g1.y, th.v[1]);
+  th.v[2] = fmaf(acc_ne, d.g1.z, fmaf(acc_fr, d.g0.y, th.v[2]));
+  th.v[3] = fmaf(acc_ne, d.g1.w, th.v[3]);
+  th.v[7] = fmaf(acc_ne, d.g0.z, th.v[7]);
 }
 
-__device__ __forceinline__ void neigh_rows(const Tables &tab, int rowidx, float v[kChunks], int lane) {
-  const float *src = tab.w0 + (size_t)rowidx * kWinSamples + lane;
+__device__ __forceinline__ void neigh_rows(const Tables &tab, int row, float v[kChunks], int lane) {
+  const float *src = tab.w0 + (size_t)row * kWinSamples + lane;
 #pragma unroll
   for (int c = 0; c < kChunks; ++c) v[c] = __ldg(src + c * kWarp);
 }
@@ -292,16 +311,16 @@ __device__ __forceinline__ void neigh_backward(const LsimParams &p, const Tables
                                                int lane) {
   const int L = p.signal_length, NT = p.n_ticks;
   const int n_total = ls.pre_n[ls.n];
-  const float inv_ts = 1.f / p.t_sampling;
   for (int g0 = 0; g0 < n_total; g0 += kWarp) {
     neigh_setup<true>(p, tab, w, ls, nb, g0, n_total, lane);
     const int m = min(kWarp, n_total - g0);
     for (int j = 0; j < m; ++j) {
-      const int rowidx = nb.row[j];
-      if (rowidx < 0) continue;
+      const NDesc d = nb.d[j];
+      const int pk = __float_as_int(d.w.w);
+      if (pk < 0) continue;
       float v[kChunks];
-      neigh_rows(tab, rowidx, v, lane);
-      neigh_vjp_one(nb, j, v, L, NT, inv_ts, grow, th, lane);
+      neigh_rows(tab, pk & kPackRowMask, v, lane);
+      neigh_vjp_one(d, v, L, NT, grow, th, lane);
     }
     __syncwarp();
   }
@@ -311,9 +330,8 @@ __device__ __forceinline__ void neigh_backward(const LsimParams &p, const Tables
 
 // The main-bin records that land on this pixel: segments of the 3x3 slots
 // whose bins reach it (tested 32 candidates at a time).  Accepted records
-// are packed into the batch -- record index in nb.row, window origin,
-// sub-tick fraction, and for the adjoint d t0/d eField in nb.dt0 and the
-// record's d corr/d frac in nb.D -- and handed to flush(m) 32 at a time.
+// are packed into the batch as descriptors (NDesc) and handed to flush(m)
+// 32 at a time.
 template <bool GRAD, typename F>
 __device__ __forceinline__ void main_batches(const LsimParams &p, const Workspace &w, const ListSmem &ls, NBatch &nb,
                                              int lane, F &&flush) {
@@ -346,13 +364,14 @@ __device__ __forceinline__ void main_batches(const LsimParams &p, const Workspac
         const int pos = m + __popc(bal & ((1u << lane) - 1u));
         const SegFwd &f = w.segf[s];
         const int rec = s * kRecPerSeg + slot;
-        nb.row[pos] = rec;
-        nb.cb[pos] = p.lut_nt - p.signal_length - __ldg(&f.cath) - 1;
-        nb.frac[pos] = __ldg(&f.frac);
-        if (GRAD) {
-          nb.dt0[pos] = __ldg(&w.sega[s].dt0);
-          nb.D[pos] = w.mrec[(size_t)rec * kRecFloats + kRecDl];
-        }
+        const int cb = p.lut_nt - p.signal_length - __ldg(&f.cath) - 1;
+        const float frac = __ldg(&f.frac);
+        NDesc d;
+        d.w = make_float4(1.f - frac, frac, GRAD ? w.mrec[(size_t)rec * kRecFloats + kRecDl] : 0.f,
+                          pack_window(0, cb, window_interior(cb, p.signal_length, p.n_ticks)));
+        d.g0 = make_float4(GRAD ? __ldg(&w.sega[s].dt0) / p.t_sampling : 0.f, __int_as_float(rec), 0.f, 0.f);
+        d.g1 = make_float4(0.f, 0.f, 0.f, 0.f);
+        nb.d[pos] = d;
       }
       m += nh;
       __syncwarp();
@@ -369,19 +388,29 @@ __device__ __forceinline__ void main_rec_forward(const LsimParams &p, const floa
   __syncwarp();
   for (int j = 0; j < m; j += 4) {
     float u[4][kChunks];
-    int cb[4], rl[4];
+    float4 dw[4];
+    int pk[4], cb[4], rl[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const bool ok = j + q < m;
-      cb[q] = nb.cb[j + q];
+      dw[q] = nb.d[j + q].w;
+      pk[q] = __float_as_int(dw[q].w);
+      cb[q] = pack_cb(pk[q]);
       rl[q] = owner_rl(cb[q], lane);
-      const float *src = mrec + (size_t)(ok ? nb.row[j + q] : 0) * kRecFloats + rl[q];
+      const int rec = ok ? __float_as_int(nb.d[j + q].g0.y) : 0;
+      const float *src = mrec + (size_t)rec * kRecFloats + rl[q];
 #pragma unroll
       for (int c = 0; c < kChunks; ++c) u[q][c] = ok ? src[c * kWarp] : 0.f;
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (j + q < m) window_apply(u[q], cb[q], rl[q], 1.f - nb.frac[j + q], nb.frac[j + q], L, NT, row, lane);
+    for (int q = 0; q < 4; ++q) {
+      if (j + q >= m) continue;
+      if (pk[q] & kPackEdge)
+        window_apply_edge(u[q][0], u[q][1], u[q][2], u[q][3], u[q][4], cb[q], rl[q], dw[q].x, dw[q].y, L, NT, row,
+                          lane);
+      else
+        window_apply_interior(u[q], cb[q], rl[q], dw[q].x, dw[q].y, row, lane);
+    }
   }
   __syncwarp();
 }
@@ -393,13 +422,14 @@ __device__ __forceinline__ void main_rec_forward(const LsimParams &p, const floa
 __device__ __forceinline__ void main_rec_backward(const LsimParams &p, float *mrec, const NBatch &nb, int m,
                                                   const float *grow, Theta &th, int lane) {
   const int L = p.signal_length, NT = p.n_ticks;
-  const float inv_ts = 1.f / p.t_sampling;
   __syncwarp();
   for (int j = 0; j < m; ++j) {
-    float *rec = mrec + (size_t)nb.row[j] * kRecFloats;
-    const int cb = nb.cb[j];
-    const float f = nb.frac[j], f1 = 1.f - f;
-    const bool interior = window_interior(cb, L, NT);
+    const NDesc d = nb.d[j];
+    float *rec = mrec + (size_t)__float_as_int(d.g0.y) * kRecFloats;
+    const int pk = __float_as_int(d.w.w);
+    const int cb = pack_cb(pk);
+    const float f1 = d.w.x, f = d.w.y;
+    const bool interior = !(pk & kPackEdge);
     float dfr = 0.f, dcorr = 0.f;
 #pragma unroll
     for (int c = 0; c < kChunks; ++c) {
@@ -422,8 +452,8 @@ __device__ __forceinline__ void main_rec_backward(const LsimParams &p, float *mr
         if (idx == 0) dcorr = du;
       }
     }
-    if (lane == 0) dfr += dcorr * nb.D[j];
-    th.v[2] += dfr * inv_ts * nb.dt0[j];
+    if (lane == 0) dfr += dcorr * d.w.z;
+    th.v[2] = fmaf(dfr, d.g0.x, th.v[2]);
   }
   __syncwarp();
 }
@@ -737,6 +767,9 @@ int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st) {
   if (a.p.lut_nx < need || a.p.lut_ny < need || a.p.lut_nx < kMainSub || a.p.lut_ny < kMainSub)
     return LSIM_ERR_UNSUPPORTED;
   if (a.n_rows > 0x7fffffff / kRecPerSeg) return LSIM_ERR_UNSUPPORTED;   // record indices are int32
+  // descriptor packing: LUT rows in 15 bits, window origins within +-16384
+  if (a.p.lut_nx * a.p.lut_ny > kPackRowMask + 1 || a.p.lut_nt >= kPackCbBias || a.p.signal_length >= kPackCbBias)
+    return LSIM_ERR_UNSUPPORTED;
   int rc = run_main_records(a, st);
   if (rc != LSIM_OK) return rc;
   switch (mode) {
