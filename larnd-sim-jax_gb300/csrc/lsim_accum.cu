@@ -178,7 +178,7 @@ __device__ __forceinline__ void neigh_setup(const LsimParams &p, const Tables &t
     const SegFwd &f = w.segf[s];
     const float ne = __ldg(&f.ne);
     if (ne != 0.f) {
-      const int nbp = p.nb_bins_per_pixel;
+      constexpr int nbp = kBinsPerPixel;
       const int cx = lut_index(__ldg(&f.bx), nbp, dx * nbp);
       const int cy = lut_index(__ldg(&f.by), nbp, dy * nbp);
       const int row = cx * p.lut_ny + cy;
@@ -335,7 +335,7 @@ __device__ __forceinline__ void neigh_backward(const LsimParams &p, const Tables
 template <bool GRAD, typename F>
 __device__ __forceinline__ void main_batches(const LsimParams &p, const Workspace &w, const ListSmem &ls, NBatch &nb,
                                              int lane, F &&flush) {
-  const int nbp = p.nb_bins_per_pixel;
+  constexpr int nbp = kBinsPerPixel;
   int m = 0;
   for (int e = 0; e < ls.n; ++e) {
     const int cd = ls.cd[e];
@@ -758,7 +758,7 @@ static int launch_mode(const AccumArgs &a0, cudaStream_t st) {
 }
 
 int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st) {
-  if (a.p.n_neighbors > 4 || a.p.n_tran_bins != kMaxTran || a.p.nb_bins_per_pixel != 2 * kMainSub ||
+  if (a.p.n_neighbors > 4 || a.p.n_tran_bins != kMaxTran || a.p.nb_bins_per_pixel != kBinsPerPixel ||
       a.p.n_ticks - 1 + kRowPad > kRowFloats || (a.p.n_ticks - 1) % 4 != 0 || a.p.max_adc_values > LSIM_MAX_HITS ||
       a.p.signal_length + 2 > kChunks * kWarp || a.p.signal_length > a.p.lut_nt)
     return LSIM_ERR_UNSUPPORTED;

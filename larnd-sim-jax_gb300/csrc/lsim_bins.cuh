@@ -8,6 +8,9 @@
 namespace lsim {
 
 constexpr int kChunks = kWinSamples / kWarp;   // window chunks per lane
+// Sub-pixel bins per pixel (nb_sampling_bins_per_pixel); the LUT kernels
+// require it, so divisions by it compile to multiplications.
+constexpr int kBinsPerPixel = 2 * kMainSub;
 
 // Main-bin record of one (segment, pixel whose main bins it covers) pair:
 //   rec[0]        boundary correction  n_e * sum_uv W_uv D_uv

@@ -15,15 +15,16 @@
 // record like a neighbour part.  After the pixel-major adjoint has replaced
 // the record by its cotangent, k_main_adjoint projects it back onto n_e,
 // sigma_T and (a, b, c) and accumulates dL/dtheta per warp.  One warp owns
-// one segment at a time; warps own fixed contiguous segment ranges, so the
-// per-warp gradient records and their reduction order are fixed.
+// one segment at a time; blocks own fixed contiguous segment ranges that
+// their warps interleave, so the per-warp gradient records and their
+// reduction order are fixed.
 #include "lsim_internal.cuh"
 #include "lsim_bins.cuh"
 #include "lsim_fee.cuh"
 
 namespace lsim {
 
-constexpr int kMainBlockWarps = 4;
+constexpr int kMainBlockWarps = 8;
 
 // Grouped LUT sub-positions of one (segment, pixel) pair: row offset
 // (tidx*5 + u)*5 + v into the window tables, W, dW/dsigma_T, the
@@ -41,26 +42,34 @@ template <bool GRAD>
 __device__ __forceinline__ int main_entries(const LsimParams &p, const Tables &tab, const SegFwd &f,
                                             const SegAdj *a, int dx, int dy, MainSmem &ms, float *wd, float *wdl,
                                             int lane) {
-  const int nbp = p.nb_bins_per_pixel;
+  constexpr int nbp = kBinsPerPixel;
   // this lane's sub-position (u, v): summed 1-D bin integrals of the bins of
   // each axis that fall on the pixel with that LUT index (axis_weights, per lane)
   const int u = lane / kMainSub, v = lane % kMainSub;
   float xw = 0.f, yw = 0.f, dxw = 0.f, dyw = 0.f;
   unsigned um = 0u, vm = 0u;
   const int bx = f.bx, by = f.by, ppx = ifloordiv(bx, nbp), ppy = ifloordiv(by, nbp);
+  // the record's bin integrals, loaded up front (one 96-byte segment record)
+  float ex[kMaxTran], ey[kMaxTran], dex[kMaxTran], dey[kMaxTran];
+#pragma unroll
+  for (int i = 0; i < kMaxTran; ++i) {
+    ex[i] = f.ex[i];
+    ey[i] = f.ey[i];
+    dex[i] = GRAD ? a->dex[i] : 0.f;
+    dey[i] = GRAD ? a->dey[i] : 0.f;
+  }
 #pragma unroll
   for (int i = 0; i < kMaxTran; ++i) {
     const int bi = bx + i - kMaxTran / 2, bj = by + i - kMaxTran / 2;
     const bool onx = ifloordiv(bi, nbp) - ppx == dx, ony = ifloordiv(bj, nbp) - ppy == dy;
     const int ui = lut_index(bi, nbp, 0), vj = lut_index(bj, nbp, 0);
-    if (onx) {
-      um |= 1u << ui;
-      if (ui == u) { xw += f.ex[i]; if (GRAD) dxw += a->dex[i]; }
-    }
-    if (ony) {
-      vm |= 1u << vj;
-      if (vj == v) { yw += f.ey[i]; if (GRAD) dyw += a->dey[i]; }
-    }
+    um |= onx ? 1u << ui : 0u;
+    vm |= ony ? 1u << vj : 0u;
+    const bool tx = onx && ui == u, ty = ony && vj == v;
+    xw += tx ? ex[i] : 0.f;
+    dxw += tx ? dex[i] : 0.f;
+    yw += ty ? ey[i] : 0.f;
+    dyw += ty ? dey[i] : 0.f;
   }
   const bool mine = lane < kMainSub * kMainSub && ((um >> u) & 1u) && ((vm >> v) & 1u);
   const unsigned bal = __ballot_sync(0xffffffffu, mine);
@@ -85,24 +94,26 @@ __device__ __forceinline__ int main_entries(const LsimParams &p, const Tables &t
   return __popc(bal);
 }
 
-__device__ __forceinline__ void warp_range(int64_t n_rows, int64_t *s0, int64_t *s1) {
-  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-  const int64_t nw = (int64_t)gridDim.x * blockDim.x / kWarp;
-  const int64_t chunk = (n_rows + nw - 1) / nw;
-  *s0 = gw * chunk;
-  *s1 = min(n_rows, *s0 + chunk);
+// Segments of this block: a contiguous range, interleaved over its warps
+// (warp w takes s0 + w, s0 + w + kMainBlockWarps, ...), so the warps of a
+// block work on neighbouring segments -- usually of one track, with the same
+// template index -- and share their LUT rows in L1.
+__device__ __forceinline__ void block_range(int64_t n_rows, int64_t *s0, int64_t *s1) {
+  const int64_t chunk = (n_rows + gridDim.x - 1) / gridDim.x;
+  *s0 = (int64_t)blockIdx.x * chunk + threadIdx.x / kWarp;
+  *s1 = min(n_rows, (int64_t)blockIdx.x * chunk + chunk);
 }
 
-__global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_records(LsimParams p, Tables tab, Workspace w, Grid g,
+__global__ void __launch_bounds__(kMainBlockWarps * kWarp, 2) k_main_records(LsimParams p, Tables tab, Workspace w, Grid g,
                                                                            int64_t n_rows) {
   __shared__ MainSmem sms[kMainBlockWarps];
   const int lane = threadIdx.x % kWarp;
   MainSmem &ms = sms[threadIdx.x / kWarp];
-  const int nbp = p.nb_bins_per_pixel;
+  constexpr int nbp = kBinsPerPixel;
   int n_rec = 0;
   int64_t s0, s1;
-  warp_range(n_rows, &s0, &s1);
-  for (int64_t s = s0; s < s1; ++s) {
+  block_range(n_rows, &s0, &s1);
+  for (int64_t s = s0; s < s1; s += kMainBlockWarps) {
     const SegFwd &f = w.segf[s];
     const float ne = f.ne;
     const int32_t key = w.key[s];
@@ -111,7 +122,9 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_records(LsimPa
     int lx, hx, ly, hy;
     axis_range(f.bx, nbp, &lx, &hx);
     axis_range(f.by, nbp, &ly, &hy);
+#pragma unroll 1
     for (int dx = lx; dx <= hx; ++dx)
+#pragma unroll 1
       for (int dy = ly; dy <= hy; ++dy) {
         // records of pixels that are not simulated are never read (the
         // reference drops main bins outside unique_pixels, sim_jax.py:152-154)
@@ -121,7 +134,7 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_records(LsimPa
         float acc[kChunks];
 #pragma unroll
         for (int j = 0; j < kChunks; ++j) acc[j] = 0.f;
-#pragma unroll 1
+#pragma unroll 2
         for (int e = 0; e < n; ++e) {
           // padded rows: entry idx is sample idx - 1, matching the record layout
           const float4 *src = tab.wmp + (size_t)ms.off[e] * kWinSamples + lane;
@@ -147,18 +160,19 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp) k_main_records(LsimPa
   if (lane == 0 && n_rec) atomicAdd(&w.counts->n_main_rec, n_rec);
 }
 
-__global__ void __launch_bounds__(kMainBlockWarps * kWarp, 4) k_main_adjoint(LsimParams p, Tables tab, Workspace w, Grid g,
+__global__ void __launch_bounds__(kMainBlockWarps * kWarp, 3) k_main_adjoint(LsimParams p, Tables tab, Workspace w, Grid g,
                                                                            int64_t n_rows) {
   __shared__ MainSmem sms[kMainBlockWarps];
   const int lane = threadIdx.x % kWarp;
   MainSmem &ms = sms[threadIdx.x / kWarp];
-  const int L = p.signal_length, nbp = p.nb_bins_per_pixel;
+  const int L = p.signal_length;
+  constexpr int nbp = kBinsPerPixel;
   float th[LSIM_NPARAM];
 #pragma unroll
   for (int i = 0; i < LSIM_NPARAM; ++i) th[i] = 0.f;
   int64_t s0, s1;
-  warp_range(n_rows, &s0, &s1);
-  for (int64_t s = s0; s < s1; ++s) {
+  block_range(n_rows, &s0, &s1);
+  for (int64_t s = s0; s < s1; s += kMainBlockWarps) {
     const SegFwd &f = w.segf[s];
     const float ne = f.ne;
     const int32_t key = w.key[s];
@@ -169,7 +183,9 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 4) k_main_adjoint(Lsi
     int lx, hx, ly, hy;
     axis_range(f.bx, nbp, &lx, &hx);
     axis_range(f.by, nbp, &ly, &hy);
+#pragma unroll 1
     for (int dx = lx; dx <= hx; ++dx)
+#pragma unroll 1
       for (int dy = ly; dy <= hy; ++dy) {
         // records of pixels that are not simulated are never read (the
         // reference drops main bins outside unique_pixels, sim_jax.py:152-154)
