@@ -314,13 +314,18 @@ __device__ __forceinline__ void neigh_backward(const LsimParams &p, const Tables
   for (int g0 = 0; g0 < n_total; g0 += kWarp) {
     neigh_setup<true>(p, tab, w, ls, nb, g0, n_total, lane);
     const int m = min(kWarp, n_total - g0);
+    // software pipeline: the template row of contribution j + 1 is in
+    // flight while contribution j is projected (empty descriptors read row 0)
+    float vn[kChunks];
+    neigh_rows(tab, max(__float_as_int(nb.d[0].w.w), 0) & kPackRowMask, vn, lane);
     for (int j = 0; j < m; ++j) {
       const NDesc d = nb.d[j];
       const int pk = __float_as_int(d.w.w);
-      if (pk < 0) continue;
       float v[kChunks];
-      neigh_rows(tab, pk & kPackRowMask, v, lane);
-      neigh_vjp_one(d, v, L, NT, grow, th, lane);
+#pragma unroll
+      for (int c = 0; c < kChunks; ++c) v[c] = vn[c];
+      if (j + 1 < m) neigh_rows(tab, max(__float_as_int(nb.d[j + 1].w.w), 0) & kPackRowMask, vn, lane);
+      if (pk >= 0) neigh_vjp_one(d, v, L, NT, grow, th, lane);
     }
     __syncwarp();
   }
