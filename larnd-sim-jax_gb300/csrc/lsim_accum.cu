@@ -428,7 +428,19 @@ __device__ __forceinline__ void main_rec_backward(const LsimParams &p, float *mr
                                                   const float *grow, Theta &th, int lane) {
   const int L = p.signal_length, NT = p.n_ticks;
   __syncwarp();
+  // samples of record j + 1 are in flight while record j is processed
+  auto load = [&](int j, float u[kChunks]) {
+    const float *rec = mrec + (size_t)__float_as_int(nb.d[j].g0.y) * kRecFloats + lane;
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) u[c] = lane + c * kWarp <= L ? rec[c * kWarp] : 0.f;
+  };
+  float un[kChunks];
+  load(0, un);
   for (int j = 0; j < m; ++j) {
+    float u[kChunks];
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) u[c] = un[c];
+    if (j + 1 < m) load(j + 1, un);
     const NDesc d = nb.d[j];
     float *rec = mrec + (size_t)__float_as_int(d.g0.y) * kRecFloats;
     const int pk = __float_as_int(d.w.w);
@@ -440,7 +452,6 @@ __device__ __forceinline__ void main_rec_backward(const LsimParams &p, float *mr
     for (int c = 0; c < kChunks; ++c) {
       const int idx = lane + c * kWarp;     // sample idx - 1 lands on columns cb + idx (x frac), cb + idx + 1
       if (idx <= L) {
-        const float u = rec[idx];
         const int c1 = cb + idx;
         float gA, gB;
         if (interior) {
@@ -453,7 +464,7 @@ __device__ __forceinline__ void main_rec_backward(const LsimParams &p, float *mr
         }
         const float du = gA * f + gB * f1;
         rec[idx] = du;
-        dfr += u * (gA - gB);
+        dfr += u[c] * (gA - gB);
         if (idx == 0) dcorr = du;
       }
     }

@@ -197,9 +197,15 @@ __device__ __forceinline__ void fee_backward(const LsimParams &p, float *G, int 
     if (lane == 0) G[T - 1] -= S;
     __syncwarp();
   }
+  // this lane's 64 keep bits of hit h (the next hit's are loaded ahead)
+  auto keep_bits = [&](int h) {
+    const uint2 m = *reinterpret_cast<const uint2 *>(st->mask + h * kMaskWords + 2 * lane);
+    return (uint64_t)m.x | ((uint64_t)m.y << 32);
+  };
+  uint64_t kn = st->n_done > 0 ? keep_bits(st->n_done - 1) : 0u;
   for (int h = st->n_done - 1; h >= 0; --h) {
-    uint64_t km = (uint64_t)st->mask[h * kMaskWords + 2 * lane] |
-                  ((uint64_t)st->mask[h * kMaskWords + 2 * lane + 1] << 32);
+    uint64_t km = kn;
+    if (h > 0) kn = keep_bits(h - 1);
     float S = 0.f;
     for (int i0 = 4 * lane; i0 < T; i0 += kFeePass, km >>= 4) {
       const uint32_t bits = (uint32_t)km;
