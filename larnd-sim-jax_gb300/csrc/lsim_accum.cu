@@ -573,6 +573,19 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a
     r = __shfl_sync(0xffffffffu, r, 0);
     if (r >= n_valid) break;
     const int64_t slot = a.w.pix_slot[r];
+    // adjoint mode: this lane's hit cotangent, or the target ADC of the
+    // pixel (digitize(0) where the target has no such pixel), loaded early
+    float cot = 0.f;
+    if constexpr (GRAD) {
+      if (lane < H) {
+        if (a.g_adc) {
+          cot = a.g_adc[(int64_t)r * H + lane];
+        } else {
+          const int tr = a.n_tgt > 0 ? a.w.tgt_index[r] : -1;
+          cot = tr >= 0 ? a.tgt_adc[(int64_t)tr * H + lane] : digitize(p, 0.f);
+        }
+      }
+    }
     float4 *b4 = reinterpret_cast<float4 *>(sm.buf);
     for (int i = lane; i < kRowFloats / 4; i += kWarp) b4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     build_list(a.g, a.w.cnt, a.w.off, slot, sm.list, lane);
@@ -598,34 +611,22 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a
     }
     if constexpr (GRAD) {
       fee_forward(p, row + 1, T, nrm, adc_dst, tick_dst, &sm.fee, nullptr, early_exit, lane);
+      // loss terms and digitisation adjoint, lane h for hit h
       float loss = 0.f;
-      if (lane == 0) {
-        int64_t tr = -1;
-        if (!a.g_adc) {
-          const int32_t pid = slot_pid(p, a.g, slot);
-          int64_t lo = 0, hi = a.n_tgt;
-          while (lo < hi) {
-            const int64_t mid = (lo + hi) >> 1;
-            if (a.tgt_pids[mid] < pid) lo = mid + 1; else hi = mid;
-          }
-          if (lo < a.n_tgt && a.tgt_pids[lo] == pid) tr = lo;
+      if (lane < H) {
+        const float raw = sm.fee.raw[lane];
+        const float adc = digitize(p, raw);
+        float g;
+        if (a.g_adc) {
+          g = cot;
+        } else {
+          const float d = adc - cot;
+          loss = d * d;
+          g = 2.f * d;
         }
-        const float adc0 = digitize(p, 0.f);
-        for (int h = 0; h < H; ++h) {
-          const float raw = sm.fee.raw[h];
-          const float adc = digitize(p, raw);
-          float g;
-          if (a.g_adc) {
-            g = a.g_adc[(int64_t)r * H + h];
-          } else {
-            const float tgt = tr >= 0 ? a.tgt_adc[tr * H + h] : adc0;
-            const float d = adc - tgt;
-            loss += d * d;
-            g = 2.f * d;
-          }
-          sm.gint[h] = digitize_vjp(p, raw, g);
-        }
+        sm.gint[lane] = digitize_vjp(p, raw, g);
       }
+      loss = warp_sum(loss);
       __syncwarp();
       fee_backward(p, row + 1, T, &sm.fee, sm.gint, lane);
       if (lane == 0) row[0] = 0.f;
@@ -679,6 +680,20 @@ __global__ void k_reduce_records(const float *__restrict__ pix, int64_t n_fixed,
     if (threadIdx.x == 0) partials[(size_t)blockIdx.x * 16 + q] = sh[0];
     __syncthreads();
   }
+}
+
+// Row of the loss target with the pixel id of each valid pixel (both lists
+// are sorted), or -1.
+__global__ void k_target_index(AccumArgs a) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= a.w.counts->n_valid) return;
+  const int32_t pid = slot_pid(a.p, a.g, a.w.pix_slot[r]);
+  int64_t lo = 0, hi = a.n_tgt;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (a.tgt_pids[mid] < pid) lo = mid + 1; else hi = mid;
+  }
+  a.w.tgt_index[r] = (lo < a.n_tgt && a.tgt_pids[lo] == pid) ? (int32_t)lo : -1;
 }
 
 // Loss terms of target pixels that the prediction does not have.
@@ -792,6 +807,10 @@ int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st) {
     case kModeWfs: return launch_mode<kModeWfs>(a, st);
     case kModeAdc: return launch_mode<kModeAdc>(a, st);
     case kModeGrad:
+      if (!a.g_adc && a.n_tgt > 0 && a.n_rows > 0) {
+        k_target_index<<<(unsigned)((a.n_rows + 255) / 256), 256, 0, st>>>(a);
+        if (cudaGetLastError() != cudaSuccess) return LSIM_ERR_CUDA;
+      }
       rc = launch_mode<kModeGrad>(a, st);
       return rc != LSIM_OK ? rc : run_main_adjoint(a, st);
   }

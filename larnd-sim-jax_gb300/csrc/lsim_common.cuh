@@ -109,6 +109,7 @@ struct Workspace {
   double *red_partials;     // fixed-order reduction partials (kRedSlots * 16 doubles)
   float *mrec;              // main-bin records: kMainRecPerSeg per segment, kMainRecFloats each
   uint32_t *fee_masks;      // per pixel-kernel warp: front-end reset masks (kFeeMaskWords)
+  int32_t *tgt_index;       // per valid pixel: row of the loss target with the same pixel id, or -1
   float *main_out;          // per main-adjoint warp: [0, 8 gradient terms] (kPixRec floats)
   size_t bytes;
 };
@@ -144,6 +145,7 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   size_t o_mrec = take(4 * (size_t)kMainRecFloats * kMainRecPerSeg * (size_t)n_rows);
   size_t o_mout = take(4 * (size_t)kPixRec * kMainWarps);
   size_t o_fmask = take(4 * (size_t)kFeeMaskWords * kMaxPixelWarps);
+  size_t o_tidx = take(4 * (size_t)n_rows);
   Workspace w;
   char *b = (char *)base;
   w.counts = (LsimCounts *)(b + o_counts);
@@ -164,6 +166,7 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   w.mrec = (float *)(b + o_mrec);
   w.main_out = (float *)(b + o_mout);
   w.fee_masks = (uint32_t *)(b + o_fmask);
+  w.tgt_index = (int32_t *)(b + o_tidx);
   w.bytes = off;
   return w;
 }
