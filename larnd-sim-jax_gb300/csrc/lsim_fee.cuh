@@ -71,6 +71,20 @@ __device__ __forceinline__ void warp_cumsum_charge(float *X, int T, float ts, in
   __syncwarp();
 }
 
+// First q in 0..3 with Q[i0+q] <= thr <= Q[i0+q+1] (Q = base + value) over
+// the ticks v0..v3 and the following tick nx, counting only pairs with
+// i0 + q < lim - 1; 4 if none.
+__device__ __forceinline__ int first_crossing(float v0, float v1, float v2, float v3, float nx, float base, float thr,
+                                              int i0, int lim) {
+  const float q0 = base + v0, q1 = base + v1, q2 = base + v2, q3 = base + v3, q4 = base + nx;
+  int first = 4;
+  if (i0 + 3 < lim - 1 && q4 >= thr && q3 <= thr) first = 3;
+  if (i0 + 2 < lim - 1 && q3 >= thr && q2 <= thr) first = 2;
+  if (i0 + 1 < lim - 1 && q2 >= thr && q1 <= thr) first = 1;
+  if (i0 < lim - 1 && q1 >= thr && q0 <= thr) first = 0;
+  return first;
+}
+
 // Forward self-trigger on C (in place).  normals: per-pixel standard
 // normals [1 + 3H] or null (noise off).  Writes adc (digitized) and tick
 // per hit through lane 0; fills st when non-null.  C must be 16-byte
@@ -89,26 +103,22 @@ __device__ __forceinline__ void fee_forward(const LsimParams &p, float *C, int T
   const int H = p.max_adc_values;
   float base = normals ? normals[0] * p.reset_noise : 0.f;
   float4 *C4 = reinterpret_cast<float4 *>(C);
-  for (int h = 0; h < H; ++h) {
-    // first i < T - 1 with Q[i] <= thr <= Q[i + 1], Q = base + C
-    int idx = T - 2;
-    for (int i0 = 4 * lane, m = 0; m * kFeePass < T - 1; ++m, i0 += kFeePass) {
-      const float4 c = i0 < T ? C4[i0 / 4] : make_float4(0.f, 0.f, 0.f, 0.f);
-      float nx = __shfl_down_sync(0xffffffffu, c.x, 1);
-      if (lane == kWarp - 1) nx = i0 + 4 < T ? C[i0 + 4] : 0.f;
-      const float q0 = base + c.x, q1 = base + c.y, q2 = base + c.z, q3 = base + c.w, q4 = base + nx;
-      int first = 4;
-      if (i0 + 3 < T - 1 && q4 >= thr && q3 <= thr) first = 3;
-      if (i0 + 2 < T - 1 && q3 >= thr && q2 <= thr) first = 2;
-      if (i0 + 1 < T - 1 && q2 >= thr && q1 <= thr) first = 1;
-      if (i0 < T - 1 && q1 >= thr && q0 <= thr) first = 0;
-      const unsigned bal = __ballot_sync(0xffffffffu, first < 4);
-      if (bal) {
-        const int ln = __ffs(bal) - 1;
-        idx = m * kFeePass + 4 * ln + __shfl_sync(0xffffffffu, first, ln);
-        break;
-      }
+  // first i < T - 1 with Q[i] <= thr <= Q[i + 1], Q = base + C, for hit 0;
+  // later hits' searches run inside the previous hit's reset sweep
+  int idx = T - 2;
+  for (int i0 = 4 * lane, m = 0; m * kFeePass < T - 1; ++m, i0 += kFeePass) {
+    const float4 c = i0 < T ? C4[i0 / 4] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float nx = __shfl_down_sync(0xffffffffu, c.x, 1);
+    if (lane == kWarp - 1) nx = i0 + 4 < T ? C[i0 + 4] : 0.f;
+    const int first = first_crossing(c.x, c.y, c.z, c.w, nx, base, thr, i0, T);
+    const unsigned bal = __ballot_sync(0xffffffffu, first < 4);
+    if (bal) {
+      const int ln = __ffs(bal) - 1;
+      idx = m * kFeePass + 4 * ln + __shfl_sync(0xffffffffu, first, ln);
+      break;
     }
+  }
+  for (int h = 0; h < H; ++h) {
     int e = idx + 1 + p.fee_interval;
     if (e >= T) e = T - 1;
     const float qvn = C[e];
@@ -123,13 +133,20 @@ __device__ __forceinline__ void fee_forward(const LsimParams &p, float *C, int T
     if (e2 >= T) e2 = T - 1;
     const float R = C[e2];
     __syncwarp();
-    // reset: C <- where(C - R < 0, 0, C - R); keep bits per lane (bit 4m + q)
+    // reset: C <- where(C - R < 0, 0, C - R), keep bits per lane (bit 4m + q),
+    // and the next hit's crossing search on the reset values: pairs inside a
+    // lane's 4 ticks and with the next lane's first tick are tested in the
+    // pass; lane 31's last pair waits for lane 0's first value of the next pass
     bool nz = false;
     uint64_t km = 0u;
-    for (int i0 = 4 * lane, sh = 0; i0 - 4 * lane < T; i0 += kFeePass, sh += 4) {
+    int nidx = T - 2;
+    bool found = false;
+    float carry = 0.f;          // lane 31's last reset value of the previous pass
+    for (int i0 = 4 * lane, sh = 0, m = 0; i0 - 4 * lane < T; i0 += kFeePass, sh += 4, ++m) {
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
       if (i0 < T) {
         const float4 c = C4[i0 / 4];
-        float v[4] = {c.x, c.y, c.z, c.w};
+        v[0] = c.x; v[1] = c.y; v[2] = c.z; v[3] = c.w;
         uint32_t bits = 0u;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -144,7 +161,28 @@ __device__ __forceinline__ void fee_forward(const LsimParams &p, float *C, int T
         C4[i0 / 4] = make_float4(v[0], v[1], v[2], v[3]);
         km |= (uint64_t)bits << sh;
       }
+      const float nx = __shfl_down_sync(0xffffffffu, v[0], 1);
+      const float v0 = __shfl_sync(0xffffffffu, v[0], 0);
+      if (!found) {
+        // the pair (128m - 1, 128m) left over from the previous pass
+        const int ip = m * kFeePass - 1;
+        if (m > 0 && ip < T - 1 && base + v0 >= thr && base + carry <= thr) {
+          nidx = ip;
+          found = true;
+        } else {
+          const int first = lane < kWarp - 1 ? first_crossing(v[0], v[1], v[2], v[3], nx, base, thr, i0, T)
+                                             : first_crossing(v[0], v[1], v[2], v[3], 0.f, base, thr, i0, min(T, i0 + 4));
+          const unsigned bal = __ballot_sync(0xffffffffu, first < 4);
+          if (bal) {
+            const int ln = __ffs(bal) - 1;
+            nidx = m * kFeePass + 4 * ln + __shfl_sync(0xffffffffu, first, ln);
+            found = true;
+          }
+        }
+      }
+      carry = __shfl_sync(0xffffffffu, v[3], kWarp - 1);
     }
+    idx = nidx;
     if (st) {
       st->mask[h * kMaskWords + 2 * lane] = (uint32_t)km;
       st->mask[h * kMaskWords + 2 * lane + 1] = (uint32_t)(km >> 32);
