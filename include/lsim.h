@@ -92,7 +92,8 @@ typedef struct LsimCounts {
   int32_t bad_row;      /* first offending track row, or -1 */
   int32_t work;         /* internal work counter */
   int32_t n_main_rec;   /* main-bin records written by the last LUT accumulation */
-  int32_t reserved[8];
+  int32_t n_main_seg;   /* segments with main-bin records in the last LUT accumulation */
+  int32_t reserved[7];
 } LsimCounts;
 
 int lsim_abi_version(void);

@@ -655,7 +655,7 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a
 
 constexpr int kRedThreads = 256;
 constexpr int kPixBlocks = 1024;     // reduction blocks over pixel records
-constexpr int kMainBlocks = 256;     // reduction blocks over main-bin adjoint warps
+constexpr int kMainBlocks = 256;     // reduction blocks over per-segment main-bin adjoint records
 constexpr int kTgtBlocks = 256;      // reduction blocks over target-only rows
 static_assert(kPixBlocks + kMainBlocks + kTgtBlocks <= kRedSlots, "reduction partials");
 
@@ -821,7 +821,7 @@ int run_grad_finalize(const AccumArgs &a, float *loss_out, float *grad_out, cuda
   double *rec_partials = a.w.red_partials;
   double *tgt_partials = a.w.red_partials + (size_t)(kPixBlocks + kMainBlocks) * 16;
   k_reduce_records<<<kPixBlocks, kRedThreads, 0, st>>>(a.w.pix_out, -1, a.w.counts, rec_partials);
-  k_reduce_records<<<kMainBlocks, kRedThreads, 0, st>>>(a.w.main_out, kMainWarps, a.w.counts,
+  k_reduce_records<<<kMainBlocks, kRedThreads, 0, st>>>(a.w.main_out, a.n_rows, a.w.counts,
                                                         rec_partials + (size_t)kPixBlocks * 16);
   int tb = 0;
   if (!a.g_adc && a.n_tgt > 0) {

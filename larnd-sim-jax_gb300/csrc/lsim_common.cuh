@@ -110,13 +110,16 @@ struct Workspace {
   float *mrec;              // main-bin records: kMainRecPerSeg per segment, kMainRecFloats each
   uint32_t *fee_masks;      // per pixel-kernel warp: front-end reset masks (kFeeMaskWords)
   int32_t *tgt_index;       // per valid pixel: row of the loss target with the same pixel id, or -1
-  float *main_out;          // per main-adjoint warp: [0, 8 gradient terms] (kPixRec floats)
+  float *main_out;          // per segment: main-bin adjoint [0, 8 gradient terms] (kPixRec floats)
+  int32_t *seg_order;       // segments with main-bin records, grouped by template index
+  int32_t *tidx_hist;       // kMaxTemplates counts, then kMaxTemplates cursors
   size_t bytes;
 };
 
 constexpr int kPixRec = 12;      // floats per per-pixel record (loss + 8 grads, padded)
 constexpr int kRedSlots = 4096;  // reduction blocks (pixels + main-bin warps + target-only)
 constexpr int kMainWarps = 8192; // warps of the segment-major main-bin kernels
+constexpr int kMaxTemplates = 1024;    // long-diffusion templates the main-bin ordering supports
 constexpr int kMainRecPerSeg = 4;      // a segment's main bins cover at most 2 x 2 pixels
 constexpr int kMainRecFloats = 164;    // window of 160 samples + d(corr)/d(frac), padded to 16 bytes
 constexpr int kMaxPixelWarps = 8192;   // warps of the persistent pixel kernel
@@ -143,7 +146,9 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   size_t o_pix = take(4 * (size_t)kPixRec * (size_t)n_rows);
   size_t o_red = take(8 * (size_t)kRedSlots * 16);
   size_t o_mrec = take(4 * (size_t)kMainRecFloats * kMainRecPerSeg * (size_t)n_rows);
-  size_t o_mout = take(4 * (size_t)kPixRec * kMainWarps);
+  size_t o_mout = take(4 * (size_t)kPixRec * (size_t)n_rows);
+  size_t o_sord = take(4 * (size_t)n_rows);
+  size_t o_thist = take(4 * (size_t)kMaxTemplates * 2);
   size_t o_fmask = take(4 * (size_t)kFeeMaskWords * kMaxPixelWarps);
   size_t o_tidx = take(4 * (size_t)n_rows);
   Workspace w;
@@ -165,6 +170,8 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   w.red_partials = (double *)(b + o_red);
   w.mrec = (float *)(b + o_mrec);
   w.main_out = (float *)(b + o_mout);
+  w.seg_order = (int32_t *)(b + o_sord);
+  w.tidx_hist = (int32_t *)(b + o_thist);
   w.fee_masks = (uint32_t *)(b + o_fmask);
   w.tgt_index = (int32_t *)(b + o_tidx);
   w.bytes = off;

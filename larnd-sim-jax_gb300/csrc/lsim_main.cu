@@ -14,10 +14,11 @@
 // pixel) and stores them as a record; the pixel-major accumulation adds the
 // record like a neighbour part.  After the pixel-major adjoint has replaced
 // the record by its cotangent, k_main_adjoint projects it back onto n_e,
-// sigma_T and (a, b, c) and accumulates dL/dtheta per warp.  One warp owns
-// one segment at a time; blocks own fixed contiguous segment ranges that
-// their warps interleave, so the per-warp gradient records and their
-// reduction order are fixed.
+// sigma_T and (a, b, c) and writes dL/dtheta per segment (reduced later in
+// segment order, so the result does not depend on the processing order).
+// Both kernels take the segments grouped by template index: one warp owns
+// one segment at a time, the warps of a block interleave a contiguous range
+// of that order, so a block's segments share their 25 LUT window rows in L1.
 #include "lsim_internal.cuh"
 #include "lsim_bins.cuh"
 #include "lsim_fee.cuh"
@@ -94,15 +95,70 @@ __device__ __forceinline__ int main_entries(const LsimParams &p, const Tables &t
   return __popc(bal);
 }
 
-// Segments of this block: a contiguous range, interleaved over its warps
-// (warp w takes s0 + w, s0 + w + kMainBlockWarps, ...), so the warps of a
-// block work on neighbouring segments -- usually of one track, with the same
-// template index -- and share their LUT rows in L1.
-__device__ __forceinline__ void block_range(int64_t n_rows, int64_t *s0, int64_t *s1) {
-  const int64_t chunk = (n_rows + gridDim.x - 1) / gridDim.x;
-  *s0 = (int64_t)blockIdx.x * chunk + threadIdx.x / kWarp;
-  *s1 = min(n_rows, (int64_t)blockIdx.x * chunk + chunk);
+// Positions [i0, i1) of the template-ordered segment list owned by this
+// block, interleaved over its warps (warp w takes i0 + w, i0 + w + 8, ...).
+__device__ __forceinline__ void block_range(int64_t n, int64_t *i0, int64_t *i1) {
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  *i0 = (int64_t)blockIdx.x * chunk + threadIdx.x / kWarp;
+  *i1 = min(n, (int64_t)blockIdx.x * chunk + chunk);
 }
+
+// ---------------------------------------------------------------- order
+
+// Segments with main-bin records (n_e != 0 and a grid slot), grouped by
+// template index with a counting sort (the order inside a group is
+// arbitrary).  Warp-aggregated atomics: one per distinct index per warp.
+__device__ __forceinline__ bool main_active(const Workspace &w, int64_t s, int64_t n_rows, int *bin) {
+  if (s >= n_rows) return false;
+  const SegFwd &f = w.segf[s];
+  *bin = f.tidx;
+  return f.ne != 0.f && w.key[s] >= 0;
+}
+
+__global__ void k_main_order_count(Workspace w, int64_t n_rows) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int bin = 0;
+  const bool act = main_active(w, s, n_rows, &bin);
+  const unsigned am = __ballot_sync(0xffffffffu, act);
+  if (act) {
+    const unsigned peers = __match_any_sync(am, bin);
+    if ((threadIdx.x % kWarp) == __ffs(peers) - 1) atomicAdd(&w.tidx_hist[bin], __popc(peers));
+  }
+}
+
+__global__ void k_main_order_scan(Workspace w) {
+  __shared__ int sh[kMaxTemplates];
+  const int t = threadIdx.x;
+  const int c = w.tidx_hist[t];
+  sh[t] = c;
+  __syncthreads();
+  for (int o = 1; o < kMaxTemplates; o <<= 1) {
+    const int v = t >= o ? sh[t - o] : 0;
+    __syncthreads();
+    sh[t] += v;
+    __syncthreads();
+  }
+  w.tidx_hist[kMaxTemplates + t] = sh[t] - c;
+  if (t == kMaxTemplates - 1) w.counts->n_main_seg = sh[t];
+}
+
+__global__ void k_main_order_scatter(Workspace w, int64_t n_rows) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x % kWarp;
+  int bin = 0;
+  const bool act = main_active(w, s, n_rows, &bin);
+  const unsigned am = __ballot_sync(0xffffffffu, act);
+  if (act) {
+    const unsigned peers = __match_any_sync(am, bin);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&w.tidx_hist[kMaxTemplates + bin], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    w.seg_order[base + __popc(peers & ((1u << lane) - 1u))] = (int32_t)s;
+  }
+}
+
+// ---------------------------------------------------------------- kernels
 
 __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 2) k_main_records(LsimParams p, Tables tab, Workspace w, Grid g,
                                                                            int64_t n_rows) {
@@ -111,13 +167,13 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 2) k_main_records(Lsi
   MainSmem &ms = sms[threadIdx.x / kWarp];
   constexpr int nbp = kBinsPerPixel;
   int n_rec = 0;
-  int64_t s0, s1;
-  block_range(n_rows, &s0, &s1);
-  for (int64_t s = s0; s < s1; s += kMainBlockWarps) {
+  int64_t i0, i1;
+  block_range(w.counts->n_main_seg, &i0, &i1);
+  for (int64_t i = i0; i < i1; i += kMainBlockWarps) {
+    const int64_t s = w.seg_order[i];
     const SegFwd &f = w.segf[s];
     const float ne = f.ne;
     const int32_t key = w.key[s];
-    if (ne == 0.f || key < 0) continue;
     const float qa = f.qa, qb = f.qb, qc = f.qc;
     int lx, hx, ly, hy;
     axis_range(f.bx, nbp, &lx, &hx);
@@ -167,16 +223,13 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 3) k_main_adjoint(Lsi
   MainSmem &ms = sms[threadIdx.x / kWarp];
   const int L = p.signal_length;
   constexpr int nbp = kBinsPerPixel;
-  float th[LSIM_NPARAM];
-#pragma unroll
-  for (int i = 0; i < LSIM_NPARAM; ++i) th[i] = 0.f;
-  int64_t s0, s1;
-  block_range(n_rows, &s0, &s1);
-  for (int64_t s = s0; s < s1; s += kMainBlockWarps) {
+  int64_t i0, i1;
+  block_range(w.counts->n_main_seg, &i0, &i1);
+  for (int64_t i = i0; i < i1; i += kMainBlockWarps) {
+    const int64_t s = w.seg_order[i];
     const SegFwd &f = w.segf[s];
     const float ne = f.ne;
     const int32_t key = w.key[s];
-    if (ne == 0.f || key < 0) continue;
     const SegAdj &a = w.sega[s];
     const float qa = f.qa, qb = f.qb, qc = f.qc;
     float acc_ne = 0.f, acc_sig = 0.f, acc_a = 0.f, acc_b = 0.f, acc_c = 0.f;
@@ -227,34 +280,44 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 3) k_main_adjoint(Lsi
     // V and the boundary term carry n_e * W(sigma_T) * (a, b, c)(longdiff)
     const float sig = acc_sig * ne;
     const float lsum = (acc_a * a.dqa + acc_b * a.dqb + acc_c * a.dqc) * ne;
-    th[0] += acc_ne * a.dne[0];
-    th[1] += acc_ne * a.dne[1];
-    th[2] += acc_ne * a.dne[2] + sig * a.dsig[0] + lsum * a.dld[0];
-    th[3] += acc_ne * a.dne[3];
-    th[5] += lsum * a.dld[1];
-    th[6] += sig * a.dsig[1];
-    th[7] += acc_ne * a.dne[4];
-  }
+    float th[LSIM_NPARAM];
+    th[0] = acc_ne * a.dne[0];
+    th[1] = acc_ne * a.dne[1];
+    th[2] = acc_ne * a.dne[2] + sig * a.dsig[0] + lsum * a.dld[0];
+    th[3] = acc_ne * a.dne[3];
+    th[4] = 0.f;
+    th[5] = lsum * a.dld[1];
+    th[6] = sig * a.dsig[1];
+    th[7] = acc_ne * a.dne[4];
 #pragma unroll
-  for (int i = 0; i < LSIM_NPARAM; ++i) th[i] = warp_sum(th[i]);
-  if (lane == 0) {
-    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-    float *dst = w.main_out + gw * kPixRec;
-    dst[0] = 0.f;
+    for (int q = 0; q < LSIM_NPARAM; ++q)
+      if (q != 4) th[q] = warp_sum(th[q]);
+    if (lane == 0) {
+      float *dst = w.main_out + s * kPixRec;
 #pragma unroll
-    for (int i = 0; i < LSIM_NPARAM; ++i) dst[1 + i] = th[i];
+      for (int q = 0; q < LSIM_NPARAM; ++q) dst[1 + q] = th[q];
+    }
   }
 }
 
 int run_main_records(const AccumArgs &a, cudaStream_t st) {
-  if (cudaMemsetAsync(&a.w.counts->n_main_rec, 0, sizeof(int32_t), st) != cudaSuccess) return LSIM_ERR_CUDA;
+  if (cudaMemsetAsync(&a.w.counts->n_main_rec, 0, 2 * sizeof(int32_t), st) != cudaSuccess) return LSIM_ERR_CUDA;
   if (a.n_rows <= 0) return LSIM_OK;
+  if (a.p.n_templates > kMaxTemplates) return LSIM_ERR_UNSUPPORTED;
+  if (cudaMemsetAsync(a.w.tidx_hist, 0, sizeof(int32_t) * kMaxTemplates, st) != cudaSuccess) return LSIM_ERR_CUDA;
+  const unsigned nb = (unsigned)((a.n_rows + 255) / 256);
+  k_main_order_count<<<nb, 256, 0, st>>>(a.w, a.n_rows);
+  k_main_order_scan<<<1, kMaxTemplates, 0, st>>>(a.w);
+  k_main_order_scatter<<<nb, 256, 0, st>>>(a.w, a.n_rows);
   k_main_records<<<kMainWarps / kMainBlockWarps, kMainBlockWarps * kWarp, 0, st>>>(a.p, a.tab, a.w, a.g, a.n_rows);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 
 int run_main_adjoint(const AccumArgs &a, cudaStream_t st) {
-  // every warp writes its record, also when it owns no segment
+  // per-segment records; segments without main-bin records contribute zeros
+  if (cudaMemsetAsync(a.w.main_out, 0, sizeof(float) * kPixRec * (size_t)a.n_rows, st) != cudaSuccess)
+    return LSIM_ERR_CUDA;
+  if (a.n_rows <= 0) return LSIM_OK;
   k_main_adjoint<<<kMainWarps / kMainBlockWarps, kMainBlockWarps * kWarp, 0, st>>>(a.p, a.tab, a.w, a.g, a.n_rows);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
