@@ -93,7 +93,8 @@ typedef struct LsimCounts {
   int32_t work;         /* internal work counter */
   int32_t n_main_rec;   /* main-bin records written by the last LUT accumulation */
   int32_t n_main_seg;   /* segments with main-bin records in the last LUT accumulation */
-  int32_t reserved[7];
+  int32_t n_big_slots;  /* internal: pixel slots whose segment lists are sorted by a whole block */
+  int32_t reserved[6];
 } LsimCounts;
 
 int lsim_abi_version(void);

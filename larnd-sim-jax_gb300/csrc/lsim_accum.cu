@@ -729,17 +729,28 @@ __global__ void k_target_only(AccumArgs a, double *partials) {
   if (threadIdx.x == 0) partials[(size_t)blockIdx.x * 16] = sh[0];
 }
 
+// One block per output (0: loss, 1..8: gradient): fixed-order float64 sum
+// of the reduction partials.
 __global__ void k_grad_finalize(const double *partials, int n_rec_blocks, const double *tgt_partials,
                                 int n_tgt_blocks, float *loss_out, float *grad_out) {
-  const int q = threadIdx.x;   // 0: loss, 1..8: gradient
-  if (q > LSIM_NPARAM) return;
-  double s = 0.0;
-  for (int b = 0; b < n_rec_blocks; ++b) s += partials[(size_t)b * 16 + q];
-  if (q == 0) {
-    for (int b = 0; b < n_tgt_blocks; ++b) s += tgt_partials[(size_t)b * 16];
-    if (loss_out) loss_out[0] = (float)s;
-  } else if (grad_out) {
-    grad_out[q - 1] = (float)s;
+  __shared__ double sh[kRedThreads];
+  const int q = blockIdx.x;
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < n_rec_blocks; b += kRedThreads) acc += partials[(size_t)b * 16 + q];
+  if (q == 0)
+    for (int b = threadIdx.x; b < n_tgt_blocks; b += kRedThreads) acc += tgt_partials[(size_t)b * 16];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = kRedThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (q == 0) {
+      if (loss_out) loss_out[0] = (float)sh[0];
+    } else if (grad_out) {
+      grad_out[q - 1] = (float)sh[0];
+    }
   }
 }
 
@@ -828,7 +839,8 @@ int run_grad_finalize(const AccumArgs &a, float *loss_out, float *grad_out, cuda
     tb = kTgtBlocks;
     k_target_only<<<tb, kRedThreads, 0, st>>>(a, tgt_partials);
   }
-  k_grad_finalize<<<1, 32, 0, st>>>(rec_partials, kPixBlocks + kMainBlocks, tgt_partials, tb, loss_out, grad_out);
+  k_grad_finalize<<<1 + LSIM_NPARAM, kRedThreads, 0, st>>>(rec_partials, kPixBlocks + kMainBlocks, tgt_partials, tb,
+                                                         loss_out, grad_out);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 

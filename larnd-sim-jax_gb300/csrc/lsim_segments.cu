@@ -13,9 +13,9 @@ namespace lsim {
 
 __global__ void k_reset_counts(LsimCounts *c) {
   if (threadIdx.x == 0) {
-    c->n_valid = 0; c->n_em1 = 0; c->any_m1 = 0; c->status = 0; c->max_slot = 0;
-    c->bad_row = 0x7fffffff; c->work = 0;
-    for (int i = 0; i < 9; ++i) c->reserved[i] = 0;
+    c->n_valid = 0; c->n_em1 = 0; c->any_m1 = 0; c->status = 0; c->max_slot = 0; c->n_big_slots = 0;
+    c->bad_row = 0x7fffffff; c->work = 0; c->n_main_rec = 0; c->n_main_seg = 0;
+    for (int i = 0; i < (int)(sizeof(c->reserved) / sizeof(c->reserved[0])); ++i) c->reserved[i] = 0;
   }
 }
 
@@ -431,21 +431,84 @@ __global__ void k_scatter(const int32_t *__restrict__ key, int64_t n_rows, const
 }
 
 // Sort each slot's segment list ascending so accumulation order, and hence
-// every float32 result, is deterministic.
+// every float32 result, is deterministic.  Lists of up to kSortLocal
+// segments are sorted here by one thread; longer ones are queued for
+// k_sort_big_slots.
 __global__ void k_sort_slots(const int32_t *__restrict__ cnt, const int32_t *__restrict__ off, int64_t G,
-                             int32_t *__restrict__ seg_list, LsimCounts *counts) {
+                             int32_t *__restrict__ seg_list, int32_t *__restrict__ big_slots, LsimCounts *counts) {
   int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (slot >= G) return;
-  int c = cnt[slot];
+  const int c = slot < G ? cnt[slot] : 0;
+  // one atomic per warp for the largest slot (a shared counter is hot)
+  const int cmax = __reduce_max_sync(0xffffffffu, c);
+  if ((threadIdx.x % kWarp) == 0 && cmax > 1) {
+    atomicMax(&counts->max_slot, cmax);
+    if (cmax > kMaxSlotSegments) atomicCAS(&counts->status, 0, (int)LSIM_ERR_CAPACITY);
+  }
   if (c <= 1) return;
-  atomicMax(&counts->max_slot, c);
-  if (c > kMaxSlotSegments) atomicCAS(&counts->status, 0, (int)LSIM_ERR_CAPACITY);
   int32_t *l = seg_list + off[slot];
-  for (int i = 1; i < c; ++i) {
-    int32_t x = l[i];
-    int j = i - 1;
-    while (j >= 0 && l[j] > x) { l[j + 1] = l[j]; --j; }
-    l[j + 1] = x;
+  if (c > kSortLocal) {
+    big_slots[atomicAdd(&counts->n_big_slots, 1)] = (int32_t)slot;
+    return;
+  }
+  {
+    // short lists (nearly all): insertion sort in a thread-local copy
+    int32_t v[kSortLocal];
+    for (int i = 0; i < c; ++i) v[i] = l[i];
+    for (int i = 1; i < c; ++i) {
+      const int32_t x = v[i];
+      int j = i - 1;
+      while (j >= 0 && v[j] > x) { v[j + 1] = v[j]; --j; }
+      v[j + 1] = x;
+    }
+    for (int i = 0; i < c; ++i) l[i] = v[i];
+  }
+}
+
+// One block per queued long list: bitonic sort in shared memory for lists
+// up to kSortBig entries, a block-wide odd-even transposition sort in place
+// beyond (lists that long do not occur in practice).
+constexpr int kSortBig = 8192;
+constexpr int kSortThreads = 256;
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_big_slots(const int32_t *__restrict__ cnt,
+                                                                 const int32_t *__restrict__ off,
+                                                                 int32_t *__restrict__ seg_list,
+                                                                 const int32_t *__restrict__ big_slots,
+                                                                 const LsimCounts *counts) {
+  __shared__ int32_t sh[kSortBig];
+  const int nbig = counts->n_big_slots;
+  for (int b = blockIdx.x; b < nbig; b += gridDim.x) {
+    const int64_t slot = big_slots[b];
+    const int c = cnt[slot];
+    int32_t *l = seg_list + off[slot];
+    if (c <= kSortBig) {
+      int n2 = 1;
+      while (n2 < c) n2 <<= 1;
+      for (int i = threadIdx.x; i < n2; i += kSortThreads) sh[i] = i < c ? l[i] : INT32_MAX;
+      __syncthreads();
+      for (int k = 2; k <= n2; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+          for (int i = threadIdx.x; i < n2; i += kSortThreads) {
+            const int ij = i ^ j;
+            if (ij > i) {
+              const bool up = (i & k) == 0;
+              const int32_t a = sh[i], d = sh[ij];
+              if ((a > d) == up) { sh[i] = d; sh[ij] = a; }
+            }
+          }
+          __syncthreads();
+        }
+      for (int i = threadIdx.x; i < c; i += kSortThreads) l[i] = sh[i];
+    } else {
+      for (int phase = 0; phase < c; ++phase) {
+        for (int i = 2 * threadIdx.x + (phase & 1); i + 1 < c; i += 2 * kSortThreads) {
+          const int32_t a = l[i], d = l[i + 1];
+          if (a > d) { l[i] = d; l[i + 1] = a; }
+        }
+        __syncthreads();
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -485,7 +548,12 @@ int run_pixel_map(const LsimParams &p, const Workspace &w, const Grid &g, int64_
   }
   if (cudaMemsetAsync(w.cursor, 0, 4 * (size_t)g.G, st) != cudaSuccess) return LSIM_ERR_CUDA;
   if (n_rows > 0) k_scatter<<<(unsigned)((n_rows + 255) / 256), 256, 0, st>>>(w.key, n_rows, w.off, w.cursor, w.seg_list);
-  if (g.G > 0) k_sort_slots<<<(unsigned)((g.G + 255) / 256), 256, 0, st>>>(w.cnt, w.off, g.G, w.seg_list, w.counts);
+  if (g.G > 0) {
+    k_sort_slots<<<(unsigned)((g.G + 255) / 256), 256, 0, st>>>(w.cnt, w.off, g.G, w.seg_list, w.big_slots,
+                                                                 w.counts);
+    k_sort_big_slots<<<(unsigned)(device_sm_count() * 4), kSortThreads, 0, st>>>(w.cnt, w.off, w.seg_list,
+                                                                                w.big_slots, w.counts);
+  }
   return LSIM_OK;
 }
 
