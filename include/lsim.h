@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define LSIM_ABI_VERSION 1
+#define LSIM_ABI_VERSION 2
 
 enum {
   LSIM_OK = 0,
@@ -80,6 +80,10 @@ typedef struct LsimParams {
   /* adjoint: raw parameter values and d(vdrift)/d(eField) */
   float eField, lArDensity, dvdrift_deField;
   int32_t reserved[8];
+  /* electron mobility parametrisation (ELECTRON_MOBILITY_PARAMS) and the
+   * temperature factor (T/89)^-1.5 / 1000, for lsim_lut_stage1_theta */
+  double mobility[6];
+  double mobility_temp;
 } LsimParams;
 
 /* Device counters filled by the stage-1 calls (read after a sync). */
@@ -144,6 +148,30 @@ size_t lsim_workspace_bytes(const LsimParams *p, int64_t n_rows, int32_t n_event
  * (src/larndsim/sim_jax.py:715-725).  Writes an LsimCounts to counts_dev. */
 int lsim_lut_stage1(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,
                     int32_t n_events, void *ws, size_t ws_bytes, LsimCounts *counts_dev, void *stream);
+
+/* lsim_lut_stage1 with the fit parameters read from device memory:
+ * theta_dev[LSIM_NPARAM] = (Ab, kb, eField, lifetime, vdrift, long_diff,
+ * tran_diff, lArDensity) replace the matching LsimParams fields, and the
+ * quantities derived from them (eField*lArDensity, the drift velocity
+ * get_vdrift of src/larndsim/consts_jax.py:192-217 and its derivative) are
+ * recomputed on the device in float64 from p->mobility.  Every size the
+ * later stages use is read from device memory, so a whole fit step
+ * (this call, lsim_lut_grad, lsim_adam_step) can be captured once in a CUDA
+ * graph and replayed with theta updated in place.  Not part of the
+ * reference interface (the reference rebuilds its params pytree per step,
+ * optimize/fit_params.py:704-731). */
+int lsim_lut_stage1_theta(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,
+                          int32_t n_events, const float *theta_dev, void *ws, size_t ws_bytes,
+                          LsimCounts *counts_dev, void *stream);
+
+/* One Adam step on the fit parameters in place, in the reference's
+ * "divide" normalisation (optimize/fit_params.py:89-95, :872-895: the
+ * optimiser sees theta / scale and gradients * scale; optax.adam with
+ * eps = 1e-8): m, v and the step count live in state[2 * LSIM_NPARAM + 1];
+ * lr[i] = 0 freezes parameter i; a non-finite gradient skips the update
+ * (fit_params.py:873-876). */
+int lsim_adam_step(float *theta_dev, const float *grad_dev, const float *scale_dev, const float *lr_dev,
+                   float *state_dev, float beta1, float beta2, float eps, void *stream);
 
 /* Stage 2 of simulate_wfs: fill unique_pixels (p_pad rows: n_em1 negative
  * ids, n_m1 = p_pad - n_em1 - n_valid entries of -1, then the valid ids

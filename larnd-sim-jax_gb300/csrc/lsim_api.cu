@@ -137,7 +137,7 @@ size_t lsim_workspace_bytes(const LsimParams *p, int64_t n_rows, int32_t n_event
 
 static int stage1(bool param_mode, const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,
                   int32_t n_events, const float *normals, void *ws, size_t ws_bytes, LsimCounts *counts_dev,
-                  void *stream, const char *name) {
+                  void *stream, const char *name, const float *theta_dev = nullptr) {
   g_err.clear();
   int rc = check_params(p);
   if (!rc) rc = check_fields(f);
@@ -151,7 +151,7 @@ static int stage1(bool param_mode, const LsimParams *p, const LsimFieldMap *f, c
   Grid g = make_grid(*p, n_events);
   if (g.G > 0x7fffffff) return fail(LSIM_ERR_CAPACITY, "%s: pixel grid of %lld slots exceeds int32", name, (long long)g.G);
   cudaStream_t st = (cudaStream_t)stream;
-  rc = run_stage1(param_mode, *p, *f, tracks, normals, n_rows, n_events, w, st);
+  rc = run_stage1(param_mode, *p, *f, tracks, normals, n_rows, n_events, w, st, theta_dev);
   if (rc) return wrap(rc, name);
   if (counts_dev && cudaMemcpyAsync(counts_dev, w.counts, sizeof(LsimCounts), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
     return check_cuda(name);
@@ -161,6 +161,26 @@ static int stage1(bool param_mode, const LsimParams *p, const LsimFieldMap *f, c
 int lsim_lut_stage1(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows, int32_t n_events,
                     void *ws, size_t ws_bytes, LsimCounts *counts_dev, void *stream) {
   return stage1(false, p, f, tracks, n_rows, n_events, nullptr, ws, ws_bytes, counts_dev, stream, "lsim_lut_stage1");
+}
+
+int lsim_lut_stage1_theta(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,
+                          int32_t n_events, const float *theta_dev, void *ws, size_t ws_bytes,
+                          LsimCounts *counts_dev, void *stream) {
+  if (!theta_dev) {
+    g_err.clear();
+    return fail(LSIM_ERR_INVALID, "lsim_lut_stage1_theta: null theta");
+  }
+  return stage1(false, p, f, tracks, n_rows, n_events, nullptr, ws, ws_bytes, counts_dev, stream,
+                "lsim_lut_stage1_theta", theta_dev);
+}
+
+int lsim_adam_step(float *theta_dev, const float *grad_dev, const float *scale_dev, const float *lr_dev,
+                   float *state_dev, float beta1, float beta2, float eps, void *stream) {
+  g_err.clear();
+  if (!theta_dev || !grad_dev || !scale_dev || !lr_dev || !state_dev)
+    return fail(LSIM_ERR_INVALID, "lsim_adam_step: null pointer");
+  return wrap(run_adam(theta_dev, grad_dev, scale_dev, lr_dev, state_dev, beta1, beta2, eps, (cudaStream_t)stream),
+              "lsim_adam_step");
 }
 
 int lsim_param_stage1(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,

@@ -20,6 +20,7 @@ constexpr int kMaxSlotSegments = (1 << 23) - 1;   // segments sharing one princi
 constexpr int kWinSamples = 160;         // padded window samples k = -1 .. 158 (signal_length <= 158)
 constexpr int kScanTile = 2048;          // slots per scan block
 constexpr int kSortLocal = 64;           // slot lists up to this length are sorted by one thread
+constexpr int kThetaDerived = 16;
 constexpr int kScanThreads = 256;
 
 // --------------------------------------------------------------- records
@@ -106,6 +107,7 @@ struct Workspace {
   int32_t *cnt, *off, *cursor;
   int32_t *seg_list, *pix_slot, *em1_slot;
   int32_t *big_slots;       // slots with more than kSortLocal segments (sorted by a block each)
+  float *theta_derived;     // fit parameters and derived quantities for lsim_lut_stage1_theta (kThetaDerived)
   int32_t *scan_blocks;     // 3 ints per scan block (+1 block)
   float *pix_out;           // per valid pixel: [loss, 8 gradient terms] (kPixRec floats)
   double *red_partials;     // fixed-order reduction partials (kRedSlots * 16 doubles)
@@ -145,6 +147,7 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   size_t o_pixs = take(4 * (size_t)n_rows);
   size_t o_em1 = take(4 * (size_t)n_rows);
   size_t o_big = take(4 * ((size_t)n_rows / (kSortLocal + 1) + 1));
+  size_t o_theta = take(4 * (size_t)kThetaDerived);
   size_t o_scan = take(3 * 4 * (size_t)nscan);
   size_t o_pix = take(4 * (size_t)kPixRec * (size_t)n_rows);
   size_t o_red = take(8 * (size_t)kRedSlots * 16);
@@ -169,6 +172,7 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   w.pix_slot = (int32_t *)(b + o_pixs);
   w.em1_slot = (int32_t *)(b + o_em1);
   w.big_slots = (int32_t *)(b + o_big);
+  w.theta_derived = (float *)(b + o_theta);
   w.scan_blocks = (int32_t *)(b + o_scan);
   w.pix_out = (float *)(b + o_pix);
   w.red_partials = (double *)(b + o_red);

@@ -123,10 +123,51 @@ __device__ __forceinline__ void bin_integrals(const LsimParams &p, float x0, flo
 }
 
 // K1, LUT mode: one thread per track row.
+// Fit parameters from device memory (lsim_lut_stage1_theta): theta in the
+// gradient order, the derived quantities computed in float64 as
+// _abi.make_params does on the host (get_vdrift, consts_jax.py:192-217, and
+// its analytic derivative) and rounded once to float32.
+// out: Ab, kb, erho, vdrift, lifetime, long_diff, tran_diff, eField,
+// lArDensity, dvdrift/deField.
+__global__ void k_theta_derive(LsimParams p, const float *__restrict__ theta, float *out) {
+  if (threadIdx.x != 0) return;
+  const double e = theta[2], rho = theta[7];
+  const double *a = p.mobility;
+  const double se = sqrt(e);
+  const double num = a[0] + a[1] * e + a[2] * pow(e, 1.5) + a[3] * pow(e, 2.5);
+  const double den = 1.0 + (a[1] / a[0]) * e + a[4] * pow(e, 2.0) + a[5] * pow(e, 3.0);
+  const double mu = num / den * p.mobility_temp;
+  const double dnum = a[1] + 1.5 * a[2] * se + 2.5 * a[3] * pow(e, 1.5);
+  const double dden = (a[1] / a[0]) + 2.0 * a[4] * e + 3.0 * a[5] * e * e;
+  const double dmu = (dnum * den - num * dden) / (den * den) * p.mobility_temp;
+  out[0] = theta[0];
+  out[1] = theta[1];
+  out[2] = (float)(e * rho);
+  out[3] = (float)(mu * e);
+  out[4] = theta[3];
+  out[5] = theta[5];
+  out[6] = theta[6];
+  out[7] = theta[2];
+  out[8] = theta[7];
+  out[9] = (float)(dmu * e + mu);
+}
+
 __global__ void k_segments_lut(LsimParams p, LsimFieldMap f, const float *__restrict__ tracks, int64_t n_rows,
-                               int32_t n_events, Workspace w, Grid g) {
+                               int32_t n_events, Workspace w, Grid g, const float *__restrict__ derived) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= n_rows) return;
+  if (derived) {
+    p.Ab = derived[0];
+    p.kb = derived[1];
+    p.erho = derived[2];
+    p.vdrift = derived[3];
+    p.lifetime = derived[4];
+    p.long_diff = derived[5];
+    p.tran_diff = derived[6];
+    p.eField = derived[7];
+    p.lArDensity = derived[8];
+    p.dvdrift_deField = derived[9];
+  }
   TrackRow t = load_row(p, f, tracks, s);
   if (t.event < -1 || t.event >= n_events) {
     set_status(w.counts, LSIM_ERR_INVALID, (int)s);
@@ -558,16 +599,19 @@ int run_pixel_map(const LsimParams &p, const Workspace &w, const Grid &g, int64_
 }
 
 int run_stage1(bool param_mode, const LsimParams &p, const LsimFieldMap &f, const float *tracks,
-               const float *normals, int64_t n_rows, int32_t n_events, const Workspace &w, cudaStream_t st) {
+               const float *normals, int64_t n_rows, int32_t n_events, const Workspace &w, cudaStream_t st,
+               const float *theta_dev) {
   Grid g = make_grid(p, n_events);
   k_reset_counts<<<1, 32, 0, st>>>(w.counts);
+  if (theta_dev) k_theta_derive<<<1, 32, 0, st>>>(p, theta_dev, w.theta_derived);
   if (cudaMemsetAsync(w.cnt, 0, 4 * (size_t)g.G, st) != cudaSuccess) return LSIM_ERR_CUDA;
   if (n_rows > 0) {
     unsigned nb = (unsigned)((n_rows + 127) / 128);
     if (param_mode)
       k_segments_param<<<nb, 128, 0, st>>>(p, f, tracks, normals, n_rows, n_events, w, g);
     else
-      k_segments_lut<<<nb, 128, 0, st>>>(p, f, tracks, n_rows, n_events, w, g);
+      k_segments_lut<<<nb, 128, 0, st>>>(p, f, tracks, n_rows, n_events, w, g,
+                                         theta_dev ? w.theta_derived : nullptr);
   }
   return run_pixel_map(p, w, g, n_rows, st);
 }
@@ -584,6 +628,37 @@ int run_fill_unique(const LsimParams &p, const Workspace &w, const Grid &g, int6
       cudaMemsetAsync(wfs, 0, sizeof(float) * (size_t)n_garbage * (size_t)nt_out, st) != cudaSuccess)
     return LSIM_ERR_CUDA;
   return LSIM_OK;
+}
+
+// ---------------------------------------------------------------- optimiser
+
+// One Adam step over the LSIM_NPARAM fit parameters (one thread each) in
+// "divide" normalisation: the optimiser works on theta / scale with
+// gradients g * scale (optax.adam: bias-corrected moments, eps added to
+// sqrt(v_hat)).  state = m[8], v[8], step count; skipped when any gradient is
+// not finite.
+__global__ void k_adam(float *theta, const float *grad, const float *scale, const float *lr, float *state,
+                       float beta1, float beta2, float eps) {
+  const int i = threadIdx.x;
+  const float g = i < LSIM_NPARAM ? grad[i] * scale[i] : 0.f;
+  const bool bad = __any_sync(0xffffffffu, i < LSIM_NPARAM && !isfinite(g));
+  if (bad || i >= LSIM_NPARAM) return;
+  const float t = state[2 * LSIM_NPARAM] + 1.f;
+  const float m = beta1 * state[i] + (1.f - beta1) * g;
+  const float v = beta2 * state[LSIM_NPARAM + i] + (1.f - beta2) * g * g;
+  state[i] = m;
+  state[LSIM_NPARAM + i] = v;
+  const float mh = m / (1.f - powf(beta1, t)), vh = v / (1.f - powf(beta2, t));
+  const float xn = theta[i] / scale[i] - lr[i] * mh / (sqrtf(vh) + eps);
+  theta[i] = xn * scale[i];
+  __syncwarp(0xffu);
+  if (i == 0) state[2 * LSIM_NPARAM] = t;
+}
+
+int run_adam(float *theta, const float *grad, const float *scale, const float *lr, float *state, float beta1,
+             float beta2, float eps, cudaStream_t st) {
+  k_adam<<<1, 32, 0, st>>>(theta, grad, scale, lr, state, beta1, beta2, eps);
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 
 }  // namespace lsim

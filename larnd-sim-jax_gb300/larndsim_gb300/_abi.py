@@ -18,7 +18,7 @@ import numpy as np
 from . import consts
 
 LIB_PATH = Path(__file__).resolve().parent / "liblsim.so"
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_TPC, MAX_TEMPLATES, MAX_HITS, NPARAM = 2, 128, 16, 8
 GRAD_PARAMS = ("Ab", "kb", "eField", "lifetime", "vdrift", "long_diff", "tran_diff", "lArDensity")
 
@@ -57,6 +57,7 @@ class LsimParams(C.Structure):
         ("param_dt", C.c_float), ("param_ticks", C.c_float * 64),
         ("eField", C.c_float), ("lArDensity", C.c_float), ("dvdrift_deField", C.c_float),
         ("reserved", C.c_int32 * 8),
+        ("mobility", C.c_double * 6), ("mobility_temp", C.c_double),
     ]
 
 
@@ -78,6 +79,8 @@ _SIGNATURES = {
     "lsim_lut_prepare": (C.c_int, [_PP, _vp, _vp, _sz, _vp]),
     "lsim_workspace_bytes": (_sz, [_PP, _i64, _i32]),
     "lsim_lut_stage1": (C.c_int, [_PP, _PF, _vp, _i64, _i32, _vp, _sz, _vp, _vp]),
+    "lsim_lut_stage1_theta": (C.c_int, [_PP, _PF, _vp, _i64, _i32, _vp, _vp, _sz, _vp, _vp]),
+    "lsim_adam_step": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_float, C.c_float, C.c_float, _vp]),
     "lsim_lut_stage2": (C.c_int, [_PP, _vp, _vp, _i64, _i32, _i64, _i32, _i32, _vp, _vp, _vp]),
     "lsim_valid_pixels": (C.c_int, [_PP, _vp, _i64, _i32, _i32, _vp, _vp]),
     "lsim_lut_adc": (C.c_int, [_PP, _vp, _vp, _i64, _i32, _i32, _vp, _vp, _vp, _vp]),
@@ -250,4 +253,7 @@ def make_params(params, lut_shape=None) -> LsimParams:
         lp.param_ticks[i] = float(v)
     lp.eField, lp.lArDensity = _f32(params.eField), _f32(params.lArDensity)
     lp.dvdrift_deField = _f32(consts.get_vdrift_derivative(params))
+    for i, v in enumerate(params.ELECTRON_MOBILITY_PARAMS):
+        lp.mobility[i] = float(v)
+    lp.mobility_temp = pow(params.temperature / 89, -1.5) / 1000
     return lp

@@ -159,7 +159,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_library_abi_and_sizes(lib):
-    assert lib.lsim_abi_version() == 1
+    assert lib.lsim_abi_version() == _abi.ABI_VERSION == 2
     p = _abi.make_params(consts.Params(number_pix_neighbors=4), (100, 45, 45, 1950))
     assert lib.lsim_lut_tables_bytes(p) > 40e6
     assert lib.lsim_workspace_bytes(p, 1000, 2) > 1000 * 192
