@@ -110,6 +110,21 @@ class LUTChain:
         if given, bracket the lsim_lut_grad call (all gradient kernels)."""
         return self._grad(params, target=target, normals=normals, sync=False, events=events)
 
+    def capture(self, params, target: Target, normals=None):
+        """One loss-and-gradient step at fixed ``params`` (stage 1, forward,
+        adjoint) captured in a CUDA graph; returns (graph, output tensor
+        [loss, grads...] that every replay rewrites).  Nothing in the step
+        waits for the host, so replays run back to back."""
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self.loss_and_grad_device(params, target, normals=normals)
+        torch.cuda.current_stream().wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, capture_error_mode="thread_local"):
+            out = self.loss_and_grad_device(params, target, normals=normals)
+        return g, out
+
     def set_tracks(self, tracks):
         """Replace the batch (same shape); host tensors are copied asynchronously."""
         src = torch.as_tensor(tracks)
