@@ -41,32 +41,47 @@ __device__ __forceinline__ TrackRow load_row(const LsimParams &p, const LsimFiel
   return t;
 }
 
+// The parameter-dependent values the segment kernels use: from the
+// parameter block, or (lsim_lut_stage1_theta) from device memory.  Kept
+// apart from LsimParams so the large kernel-parameter block is never copied.
+struct Phys {
+  float Ab, kb, erho, vdrift, lifetime, long_diff, tran_diff, eField, lArDensity, dvdrift;
+};
+
+__device__ __forceinline__ Phys phys_of(const LsimParams &p, const float *__restrict__ derived) {
+  if (derived)
+    return Phys{derived[0], derived[1], derived[2], derived[3], derived[4],
+                derived[5], derived[6], derived[7], derived[8], derived[9]};
+  return Phys{p.Ab, p.kb, p.erho, p.vdrift, p.lifetime, p.long_diff, p.tran_diff, p.eField, p.lArDensity,
+              p.dvdrift_deField};
+}
+
 // Recombination factor and its derivatives d/d(Ab, kb, eField, lArDensity).
-__device__ __forceinline__ float recombination(const LsimParams &p, const TrackRow &t, float d[4]) {
+__device__ __forceinline__ float recombination(const LsimParams &p, const Phys &ph, const TrackRow &t, float d[4]) {
   d[0] = d[1] = d[2] = d[3] = 0.f;
   if (p.recombination_mode == LSIM_RECOMB_BIRKS) {
     // Ab / (1 + kb*dEdx/(eField*lArDensity)), quenching_jax.py:23-25
-    float X = __fdiv_rn(__fmul_rn(p.kb, t.dEdx), p.erho);
+    float X = __fdiv_rn(__fmul_rn(ph.kb, t.dEdx), ph.erho);
     float den = __fadd_rn(1.0f, X);
-    float R = __fdiv_rn(p.Ab, den);
+    float R = __fdiv_rn(ph.Ab, den);
     float r_den = R / den;
     d[0] = 1.0f / den;
-    d[1] = -r_den * (t.dEdx / p.erho);
-    d[2] = r_den * X / p.eField;
-    d[3] = r_den * X / p.lArDensity;
+    d[1] = -r_den * (t.dEdx / ph.erho);
+    d[2] = r_den * X / ph.eField;
+    d[3] = r_den * X / ph.lArDensity;
     return R;
   }
   float csi, denom;
   if (p.recombination_mode == LSIM_RECOMB_BOX) {
     // max(0, log(alpha + csi)/csi), quenching_jax.py:18-21
-    csi = __fdiv_rn(__fmul_rn(p.beta, t.dEdx), p.erho);
+    csi = __fdiv_rn(__fmul_rn(p.beta, t.dEdx), ph.erho);
     denom = csi;
   } else {
     // ellipsoid Box model, quenching_jax.py:30-35 and :55-66
     float cosphi = __fdiv_rn(fabsf(__fsub_rn(t.ze, t.zs)), __fadd_rn(t.dx, 1e-10f));
     float c2 = __fmul_rn(cosphi, cosphi);
     float b_phi = __fdiv_rn(p.beta, sqrtf(__fadd_rn(__fsub_rn(1.0f, c2), __fmul_rn(p.r_inv2, c2))));
-    csi = __fdiv_rn(__fmul_rn(b_phi, t.dEdx), p.erho);
+    csi = __fdiv_rn(__fmul_rn(b_phi, t.dEdx), ph.erho);
     denom = __fadd_rn(csi, 1e-10f);
   }
   float lg = logf(__fadd_rn(p.alpha, csi));
@@ -75,8 +90,8 @@ __device__ __forceinline__ float recombination(const LsimParams &p, const TrackR
   // jnp.maximum(0, f) passes 1 for f > 0, 0.5 at a tie
   float gate = f > 0.f ? 1.0f : (f == 0.f ? 0.5f : 0.0f);
   float dRdcsi = gate * (1.0f / ((p.alpha + csi) * denom) - lg / (denom * denom));
-  d[2] = dRdcsi * (-csi / p.eField);
-  d[3] = dRdcsi * (-csi / p.lArDensity);
+  d[2] = dRdcsi * (-csi / ph.eField);
+  d[3] = dRdcsi * (-csi / ph.lArDensity);
   return R;
 }
 
@@ -156,18 +171,7 @@ __global__ void k_segments_lut(LsimParams p, LsimFieldMap f, const float *__rest
                                int32_t n_events, Workspace w, Grid g, const float *__restrict__ derived) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= n_rows) return;
-  if (derived) {
-    p.Ab = derived[0];
-    p.kb = derived[1];
-    p.erho = derived[2];
-    p.vdrift = derived[3];
-    p.lifetime = derived[4];
-    p.long_diff = derived[5];
-    p.tran_diff = derived[6];
-    p.eField = derived[7];
-    p.lArDensity = derived[8];
-    p.dvdrift_deField = derived[9];
-  }
+  const Phys ph = phys_of(p, derived);
   TrackRow t = load_row(p, f, tracks, s);
   if (t.event < -1 || t.event >= n_events) {
     set_status(w.counts, LSIM_ERR_INVALID, (int)s);
@@ -175,20 +179,20 @@ __global__ void k_segments_lut(LsimParams p, LsimFieldMap f, const float *__rest
   }
   // quench (quenching_jax.py:73-74)
   float dR[4];
-  float R = recombination(p, t, dR);
+  float R = recombination(p, ph, t, dR);
   float ne0 = __fmul_rn(__fmul_rn(R, t.dE), p.mev_to_electrons);
   // drift (drifting_jax.py:34-50)
   bool mask;
   int plane = tpc_plane(p, t.x, t.y, t.z, &mask);
   float z_anode = border(p, plane, 2, 0);
   float dist = __fadd_rn(fabsf(__fsub_rn(t.z, z_anode)), 1e-6f);
-  const float v = p.vdrift;
+  const float v = ph.vdrift;
   float tdr = __fdiv_rn(dist, v);
-  float red = expf(__fdiv_rn(-tdr, p.lifetime));
+  float red = expf(__fdiv_rn(-tdr, ph.lifetime));
   float mf = mask ? 1.0f : 0.0f;
   float ne = __fmul_rn(__fmul_rn(ne0, red), mf);
-  float sigL = sqrtf(__fmul_rn(__fmul_rn(tdr, 2.0f), p.long_diff));
-  float sigT = sqrtf(__fmul_rn(__fmul_rn(tdr, 2.0f), p.tran_diff));
+  float sigL = sqrtf(__fmul_rn(__fmul_rn(tdr, 2.0f), ph.long_diff));
+  float sigT = sqrtf(__fmul_rn(__fmul_rn(tdr, 2.0f), ph.tran_diff));
   // binning (get_bin_shifts, detsim_jax.py:505-510; sim_jax.py:405-409)
   float bx0 = border(p, plane, 0, 0), by0 = border(p, plane, 1, 0);
   float relx = __fsub_rn(t.x, bx0), rely = __fsub_rn(t.y, by0);
@@ -232,17 +236,17 @@ __global__ void k_segments_lut(LsimParams p, LsimFieldMap f, const float *__rest
   r.t0 = t0;
   r.ld = ld;
   // ---- adjoint partials (parameter order: Ab kb eField lifetime vdrift long_diff tran_diff lArDensity)
-  const float dv = p.dvdrift_deField;
+  const float dv = ph.dvdrift;
   float dtdE = -tdr * dv / v;
   float k = t.dE * p.mev_to_electrons * red * mf;
   a.dne[0] = dR[0] * k;
   a.dne[1] = dR[1] * k;
-  a.dne[2] = dR[2] * k + ne * (-1.0f / p.lifetime) * dtdE;
-  a.dne[3] = ne * tdr / (p.lifetime * p.lifetime);
+  a.dne[2] = dR[2] * k + ne * (-1.0f / ph.lifetime) * dtdE;
+  a.dne[3] = ne * tdr / (ph.lifetime * ph.lifetime);
   a.dne[4] = dR[3] * k;
-  a.dsig[0] = (p.tran_diff / sigT) * dtdE;
+  a.dsig[0] = (ph.tran_diff / sigT) * dtdE;
   a.dsig[1] = tdr / sigT;
-  a.dld[0] = ((p.long_diff / sigL) * dtdE / v - sigL * dv / (v * v)) / p.t_sampling;
+  a.dld[0] = ((ph.long_diff / sigL) * dtdE / v - sigL * dv / (v * v)) / p.t_sampling;
   a.dld[1] = (tdr / sigL) / v / p.t_sampling;
   a.dt0 = -t0 * dv / v;
   a.dqa = (l1 + l2) / d01;
@@ -274,6 +278,7 @@ __global__ void k_segments_lut(LsimParams p, LsimFieldMap f, const float *__rest
 __global__ void k_segments_param(LsimParams p, LsimFieldMap f, const float *__restrict__ tracks,
                                  const float *__restrict__ normals, int64_t n_rows, int32_t n_events,
                                  Workspace w, Grid g) {
+  const Phys ph = phys_of(p, nullptr);
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= n_rows) return;
   TrackRow t = load_row(p, f, tracks, s);
@@ -282,18 +287,18 @@ __global__ void k_segments_param(LsimParams p, LsimFieldMap f, const float *__re
     t.event = -1;
   }
   float dR[4];
-  float R = recombination(p, t, dR);
+  float R = recombination(p, ph, t, dR);
   float ne0 = __fmul_rn(__fmul_rn(R, t.dE), p.mev_to_electrons);
   bool mask;
   int plane = tpc_plane(p, t.x, t.y, t.z, &mask);
   float z_anode = border(p, plane, 2, 0);
   float dist = __fadd_rn(fabsf(__fsub_rn(t.z, z_anode)), 1e-6f);
-  const float v = p.vdrift;
+  const float v = ph.vdrift;
   float tdr = __fdiv_rn(dist, v);
-  float red = expf(__fdiv_rn(-tdr, p.lifetime));
+  float red = expf(__fdiv_rn(-tdr, ph.lifetime));
   float ne = __fmul_rn(__fmul_rn(ne0, red), mask ? 1.0f : 0.0f);
-  float sigL = sqrtf(__fmul_rn(__fmul_rn(tdr, 2.0f), p.long_diff));
-  float sigT = sqrtf(__fmul_rn(__fmul_rn(tdr, 2.0f), p.tran_diff));
+  float sigL = sqrtf(__fmul_rn(__fmul_rn(tdr, 2.0f), ph.long_diff));
+  float sigT = sqrtf(__fmul_rn(__fmul_rn(tdr, 2.0f), ph.tran_diff));
   // generate_electrons (detsim_jax.py:390-399)
   float nx = normals ? normals[3 * s + 0] : 0.f;
   float ny = normals ? normals[3 * s + 1] : 0.f;
