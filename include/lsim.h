@@ -205,6 +205,18 @@ int lsim_lut_grad(const LsimParams *p, const void *tables, const void *ws, int64
                   const int32_t *tgt_pids, const float *tgt_adc, int64_t n_tgt, float *loss_out,
                   float *grad_out, float *adc_out, void *stream);
 
+/* The store-the-waveforms variant of lsim_lut_grad: instead of recomputing
+ * the waveforms, the adjoint reads the rows that lsim_lut_stage2 wrote to
+ * wfs (P_pad x (n_ticks - 1), valid rows last) with the same workspace, and
+ * reuses that pass's main-bin records.  Same outputs as lsim_lut_grad; it
+ * trades the forward recomputation for P_pad x (n_ticks - 1) x 4 bytes of
+ * stored waveforms (the reference keeps the forward's materialised arrays
+ * for its backward pass, src/larndsim/sim_jax.py:141-286). */
+int lsim_lut_grad_stored(const LsimParams *p, const void *tables, const void *ws, int64_t n_rows, int32_t n_events,
+                         const float *wfs, int64_t p_pad, int32_t n_valid, const float *normals, const float *g_adc,
+                         const int32_t *tgt_pids, const float *tgt_adc, int64_t n_tgt, float *loss_out,
+                         float *grad_out, float *adc_out, void *stream);
+
 /* ---------------------------------------------------------------- FEE + hits */
 
 /* Self-trigger FEE + digitize on waveforms wfs[n_pix][n_t]: ADC values and

@@ -551,7 +551,7 @@ __device__ __forceinline__ int32_t slot_pid(const LsimParams &p, const Grid &g, 
 
 template <int MODE>
 __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a) {
-  constexpr bool GRAD = (MODE == kModeGrad);
+  constexpr bool GRAD = (MODE == kModeGrad || MODE == kModeGradStored);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x % kWarp, wid = threadIdx.x / kWarp;
   unsigned char *wbase = smem_raw + (size_t)wid * a.warp_smem;
@@ -589,11 +589,19 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a
     float4 *b4 = reinterpret_cast<float4 *>(sm.buf);
     for (int i = lane; i < kRowFloats / 4; i += kWarp) b4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     build_list(a.g, a.w.cnt, a.w.off, slot, sm.list, lane);
-    // ---- forward: neighbour parts, then main-bin parts
-    neigh_forward(p, a.tab, a.w, sm.list, sm.nb, row, lane);
-    main_batches<false>(p, a.w, sm.list, sm.nb, lane,
-                        [&](int m) { main_rec_forward(p, a.w.mrec, sm.nb, m, row, lane); });
-    __syncwarp();
+    if (MODE == kModeGradStored) {
+      // the waveform stored by a preceding simulate_wfs pass (columns 1..T)
+      const float4 *src = reinterpret_cast<const float4 *>(a.wfs + (a.row_offset + r) * (int64_t)T);
+      float4 *dst = reinterpret_cast<float4 *>(row + 1);
+      for (int i = lane; i < T / 4; i += kWarp) dst[i] = __ldg(src + i);
+      __syncwarp();
+    } else {
+      // ---- forward: neighbour parts, then main-bin parts
+      neigh_forward(p, a.tab, a.w, sm.list, sm.nb, row, lane);
+      main_batches<false>(p, a.w, sm.list, sm.nb, lane,
+                          [&](int m) { main_rec_forward(p, a.w.mrec, sm.nb, m, row, lane); });
+      __syncwarp();
+    }
     if (MODE == kModeWfs) {
       float4 *dst = reinterpret_cast<float4 *>(a.wfs + (a.row_offset + r) * (int64_t)T);
       const float4 *src = reinterpret_cast<const float4 *>(row + 1);
@@ -761,7 +769,7 @@ __global__ void k_grad_finalize(const double *partials, int n_rec_blocks, const 
 // workspace, one kFeeMaskWords block per warp).
 template <int MODE>
 static size_t warp_smem_bytes(const LsimParams &) {
-  return (sizeof(WarpSmem<MODE == kModeGrad>) + 15) & ~size_t(15);
+  return (sizeof(WarpSmem<MODE == kModeGrad || MODE == kModeGradStored>) + 15) & ~size_t(15);
 }
 
 // Persistent grid: every SM filled to its occupancy limit.
@@ -812,7 +820,9 @@ int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st) {
   // descriptor packing: LUT rows in 15 bits, window origins within +-16384
   if (a.p.lut_nx * a.p.lut_ny > kPackRowMask + 1 || a.p.lut_nt >= kPackCbBias || a.p.signal_length >= kPackCbBias)
     return LSIM_ERR_UNSUPPORTED;
-  int rc = run_main_records(a, st);
+  // the stored-waveform adjoint reuses the records (and their template
+  // order) of the simulate_wfs pass that wrote the waveforms
+  int rc = mode == kModeGradStored ? LSIM_OK : run_main_records(a, st);
   if (rc != LSIM_OK) return rc;
   switch (mode) {
     case kModeWfs: return launch_mode<kModeWfs>(a, st);
@@ -823,6 +833,13 @@ int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st) {
         if (cudaGetLastError() != cudaSuccess) return LSIM_ERR_CUDA;
       }
       rc = launch_mode<kModeGrad>(a, st);
+      return rc != LSIM_OK ? rc : run_main_adjoint(a, st);
+    case kModeGradStored:
+      if (!a.g_adc && a.n_tgt > 0 && a.n_rows > 0) {
+        k_target_index<<<(unsigned)((a.n_rows + 255) / 256), 256, 0, st>>>(a);
+        if (cudaGetLastError() != cudaSuccess) return LSIM_ERR_CUDA;
+      }
+      rc = launch_mode<kModeGradStored>(a, st);
       return rc != LSIM_OK ? rc : run_main_adjoint(a, st);
   }
   return LSIM_ERR_INVALID;

@@ -265,6 +265,32 @@ int lsim_lut_grad(const LsimParams *p, const void *tables, const void *ws, int64
   return wrap(run_grad_finalize(a, loss_out, grad_out, st), "lsim_lut_grad");
 }
 
+int lsim_lut_grad_stored(const LsimParams *p, const void *tables, const void *ws, int64_t n_rows, int32_t n_events,
+                         const float *wfs, int64_t p_pad, int32_t n_valid, const float *normals, const float *g_adc,
+                         const int32_t *tgt_pids, const float *tgt_adc, int64_t n_tgt, float *loss_out,
+                         float *grad_out, float *adc_out, void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (!tables || !ws || !grad_out || !wfs) return fail(LSIM_ERR_INVALID, "lsim_lut_grad_stored: null pointer");
+  if (!g_adc && n_tgt > 0 && (!tgt_pids || !tgt_adc)) return fail(LSIM_ERR_INVALID, "lsim_lut_grad_stored: null target");
+  if (n_valid < 0 || p_pad < n_valid) return fail(LSIM_ERR_CAPACITY, "lsim_lut_grad_stored: p_pad < n_valid");
+  cudaStream_t st = (cudaStream_t)stream;
+  AccumArgs a = make_args(p, tables, ws, n_rows, n_events);
+  a.n_valid = n_valid;
+  a.row_offset = p_pad - n_valid;
+  a.wfs = const_cast<float *>(wfs);
+  a.normals = normals;
+  a.g_adc = g_adc;
+  a.tgt_pids = tgt_pids;
+  a.tgt_adc = tgt_adc;
+  a.n_tgt = g_adc ? 0 : n_tgt;
+  a.adc_out = adc_out;
+  rc = run_accum(kModeGradStored, a, st);
+  if (rc) return wrap(rc, "lsim_lut_grad_stored");
+  return wrap(run_grad_finalize(a, loss_out, grad_out, st), "lsim_lut_grad_stored");
+}
+
 int lsim_fee(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, const float *normals, float *adc_out,
              float *tick_out, float *integral_out, void *stream) {
   g_err.clear();

@@ -15,7 +15,7 @@ int run_fill_unique(const LsimParams &p, const Workspace &w, const Grid &g, int6
                     int32_t n_valid, int32_t *unique_pixels, float *wfs, int32_t nt_out, cudaStream_t st);
 
 // lsim_accum.cu
-enum AccumMode { kModeWfs = 0, kModeAdc = 1, kModeGrad = 2 };
+enum AccumMode { kModeWfs = 0, kModeAdc = 1, kModeGrad = 2, kModeGradStored = 3 };
 struct AccumArgs {
   LsimParams p;
   int64_t n_rows;           // segments (rows of the track table)
@@ -24,7 +24,7 @@ struct AccumArgs {
   Grid g;
   int32_t n_valid;
   int64_t row_offset;       // output row of valid row 0 (wfs mode)
-  float *wfs;               // [rows][n_ticks-1] (wfs mode)
+  float *wfs;               // [rows][n_ticks-1] (wfs mode: written; stored-gradient mode: read)
   const float *normals;     // [n_valid][1+3H] or null
   float *adc_out, *tick_out;  // [n_valid][H] (adc/grad modes, optional in grad)
   const float *g_adc;       // [n_valid][H] cotangent (grad mode) or null

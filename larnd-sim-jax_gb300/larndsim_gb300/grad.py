@@ -104,6 +104,29 @@ class LUTChain:
         vals = out.cpu().numpy()
         return float(vals[0]), dict(zip(GRAD_PARAMS, vals[1:].tolist()))
 
+    def loss_and_grad_stored(self, params, target: Target, normals=None):
+        """``loss_and_grad`` through the store-the-waveforms variant: a
+        simulate_wfs pass writes the (n_valid, n_ticks - 1) waveforms, and
+        the adjoint reads them back instead of recomputing them.  Returns
+        (loss, gradient dict, waveforms)."""
+        st = self.stage1(params)
+        n_valid = self._check(st)
+        dev = self.tracks.device
+        T = int(st.lp.n_ticks) - 1
+        wfs = torch.empty((n_valid, T), dtype=torch.float32, device=dev)
+        unique = torch.empty((n_valid,), dtype=torch.int32, device=dev)
+        s = sim._stream()
+        _abi.check(self.lib, self.lib.lsim_lut_stage2(st.lp, sim._ptr(self.lut.tables), sim._ptr(st.ws), st.n_rows,
+                                                      st.n_events, n_valid, 0, n_valid, sim._ptr(wfs),
+                                                      sim._ptr(unique), s))
+        out = torch.empty(1 + _abi.NPARAM, dtype=torch.float32, device=dev)
+        _abi.check(self.lib, self.lib.lsim_lut_grad_stored(
+            st.lp, sim._ptr(self.lut.tables), sim._ptr(st.ws), st.n_rows, st.n_events, sim._ptr(wfs), n_valid,
+            n_valid, sim._ptr(normals), None, sim._ptr(target.pids), sim._ptr(target.adc), target.pids.shape[0],
+            sim._ptr(out), sim._ptr(out[1:]), None, s))
+        vals = out.cpu().numpy()
+        return float(vals[0]), dict(zip(GRAD_PARAMS, vals[1:].tolist())), wfs
+
     def loss_and_grad_device(self, params, target: Target, normals=None, events=None):
         """Like ``loss_and_grad`` but returns the device tensor [loss, grads...]
         without a host synchronisation.  ``events`` (start, end) CUDA events,

@@ -144,3 +144,14 @@ def test_loss_zero_at_target_params(cuda):
     loss, g = chain.loss_and_grad(p, target)
     assert loss == 0.0
     assert all(v == 0.0 for v in g.values())
+
+
+def test_stored_waveform_variant_matches_recompute(cuda):
+    """The store-the-waveforms adjoint gives the recomputing adjoint's
+    loss and gradient bit for bit."""
+    p, tmpl, tracks, fields, chain, target = _setup(n_neighbors=2, seed=5, n_tracks=2, shower=300)
+    pp = _perturbed(p)
+    a = chain.loss_and_grad(pp, target)
+    loss, g, wfs = chain.loss_and_grad_stored(pp, target)
+    assert wfs.shape[0] == chain._stage.n_valid
+    assert (loss, g) == a
