@@ -178,6 +178,9 @@ def run_ours(args):
     seg_rec = st.ws[256:256 + 96 * n_seg].view(torch.int32).view(n_seg, 24).cpu().numpy()
     ne = seg_rec[:, 0].view(np.float32)
     active = int((ne > 0).sum())
+    # ---- launch shapes picked by the autotuner for this device and batch
+    from larndsim_gb300 import tune
+    tuned, _ = tune.autotune(step, key=("bench", n_seg, N_NEIGH))
     # ---- the pixel kernel alone, CUDA events around its launch (eager steps)
     kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
     for e in kev:
@@ -266,7 +269,8 @@ def run_ours(args):
                                "SSE-ADC loss vs nominal target, params perturbed N(0,5%)",
                    "segments": n_seg, "active_segments": active, "pixels": n_pix, "events": n_events,
                    "l2": "flushed between timed steps (512 MiB write)", "parallelism": f"replicas x{world}",
-                   "step": "stage 1 + forward + adjoint replayed as one captured CUDA graph"},
+                   "step": "stage 1 + forward + adjoint replayed as one captured CUDA graph",
+                   "launch_shapes": tuned},
         "e2e": {"value": n_seg * world / e2e_s, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
                 "h2d_bytes_per_step": int(tracks.nbytes), "d2h_bytes_per_step": 4 * (1 + 8)},
         "roofline": {"bound": "hbm", "kernel": "k_lut_pixels<grad> (pixel-major forward + front end + loss + adjoint)",

@@ -108,6 +108,19 @@ const char *lsim_last_error(void);
  * binding can check its structure layout against the library. */
 void lsim_struct_sizes(size_t *params, size_t *fields, size_t *counts);
 
+/* Launch shapes of the LUT kernels, chosen by the Python autotuner
+ * (larndsim_gb300/tune.py) per device and workload; zero fields keep the
+ * defaults (pixel kernel: as many 128-thread blocks per SM as fit; main-bin
+ * kernels: 1024 blocks of 8 warps).  Applies to the calling thread's later
+ * calls.  Not part of the reference interface. */
+typedef struct LsimTuning {
+  int32_t pixel_blocks_per_sm;  /* persistent pixel-kernel blocks per SM, 1..occupancy limit */
+  int32_t main_blocks;          /* blocks of the segment-major main-bin kernels */
+  int32_t main_block_warps;     /* warps per main-bin block: 4 or 8 */
+  int32_t reserved[5];
+} LsimTuning;
+void lsim_set_tuning(const LsimTuning *t);
+
 /* Profiling hook: when both are non-null, the calling thread's subsequent
  * lsim_lut_stage2 / lsim_lut_adc / lsim_lut_grad calls record start/stop
  * (cudaEvent_t handles) on their stream around the pixel-accumulation

@@ -784,6 +784,8 @@ static int grid_blocks(const LsimParams &p, int *blocks, size_t *smem_out) {
       cudaSuccess)
     return LSIM_ERR_CUDA;
   if (per_sm < 1) per_sm = 1;
+  const LsimTuning tu = tuning();
+  if (tu.pixel_blocks_per_sm > 0 && tu.pixel_blocks_per_sm < per_sm) per_sm = tu.pixel_blocks_per_sm;
   *blocks = min(device_sm_count() * per_sm, kMaxPixelWarps / kAccWarps);
   *smem_out = smem;
   return LSIM_OK;

@@ -81,6 +81,9 @@ void kernel_events(cudaEvent_t *start, cudaEvent_t *stop) {
   *stop = g_ev_stop;
 }
 
+static thread_local LsimTuning g_tuning = {0, 0, 0, {0, 0, 0, 0, 0}};
+LsimTuning tuning() { return g_tuning; }
+
 }  // namespace lsim
 
 using namespace lsim;
@@ -88,6 +91,14 @@ using namespace lsim;
 extern "C" {
 
 int lsim_abi_version(void) { return LSIM_ABI_VERSION; }
+
+void lsim_set_tuning(const LsimTuning *t) {
+  if (t) {
+    lsim::g_tuning = *t;
+  } else {
+    lsim::g_tuning = LsimTuning{0, 0, 0, {0, 0, 0, 0, 0}};
+  }
+}
 
 void lsim_set_kernel_events(void *start, void *stop) {
   const bool on = start != nullptr && stop != nullptr;

@@ -61,6 +61,8 @@ int device_sm_count();
 
 // profiling events around the pixel-accumulation kernel (lsim_set_kernel_events)
 void kernel_events(cudaEvent_t *start, cudaEvent_t *stop);
+// launch shapes set by lsim_set_tuning (zero fields: defaults)
+LsimTuning tuning();
 
 // lsim_api.cu: thread-local error message shared by all entry points
 int set_error(int code, const char *msg);

@@ -25,7 +25,6 @@
 
 namespace lsim {
 
-constexpr int kMainBlockWarps = 8;
 
 // Grouped LUT sub-positions of one (segment, pixel) pair: row offset
 // (tidx*5 + u)*5 + v into the window tables, W, dW/dsigma_T, the
@@ -103,6 +102,13 @@ __device__ __forceinline__ void block_range(int64_t n, int64_t *i0, int64_t *i1)
   *i1 = min(n, (int64_t)blockIdx.x * chunk + chunk);
 }
 
+// Launch shape of the main-bin kernels: tuned or the default 1024 x 8 warps.
+static void main_shape(int *blocks, int *warps) {
+  const LsimTuning tu = tuning();
+  *warps = tu.main_block_warps == 4 ? 4 : 8;
+  *blocks = tu.main_blocks > 0 ? min(tu.main_blocks, kMainWarps / *warps) : 1024;
+}
+
 // ---------------------------------------------------------------- order
 
 // Segments with main-bin records (n_e != 0 and a grid slot), grouped by
@@ -160,7 +166,8 @@ __global__ void k_main_order_scatter(Workspace w, int64_t n_rows) {
 
 // ---------------------------------------------------------------- kernels
 
-__global__ void __launch_bounds__(kMainBlockWarps * kWarp, 2) k_main_records(LsimParams p, Tables tab, Workspace w, Grid g,
+template <int kMainBlockWarps>
+__global__ void __launch_bounds__(kMainBlockWarps * kWarp, 16 / kMainBlockWarps) k_main_records(LsimParams p, Tables tab, Workspace w, Grid g,
                                                                            int64_t n_rows) {
   __shared__ MainSmem sms[kMainBlockWarps];
   const int lane = threadIdx.x % kWarp;
@@ -216,7 +223,8 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 2) k_main_records(Lsi
   if (lane == 0 && n_rec) atomicAdd(&w.counts->n_main_rec, n_rec);
 }
 
-__global__ void __launch_bounds__(kMainBlockWarps * kWarp, 3) k_main_adjoint(LsimParams p, Tables tab, Workspace w, Grid g,
+template <int kMainBlockWarps>
+__global__ void __launch_bounds__(kMainBlockWarps * kWarp, 24 / kMainBlockWarps) k_main_adjoint(LsimParams p, Tables tab, Workspace w, Grid g,
                                                                            int64_t n_rows) {
   __shared__ MainSmem sms[kMainBlockWarps];
   const int lane = threadIdx.x % kWarp;
@@ -309,7 +317,12 @@ int run_main_records(const AccumArgs &a, cudaStream_t st) {
   k_main_order_count<<<nb, 256, 0, st>>>(a.w, a.n_rows);
   k_main_order_scan<<<1, kMaxTemplates, 0, st>>>(a.w);
   k_main_order_scatter<<<nb, 256, 0, st>>>(a.w, a.n_rows);
-  k_main_records<<<kMainWarps / kMainBlockWarps, kMainBlockWarps * kWarp, 0, st>>>(a.p, a.tab, a.w, a.g, a.n_rows);
+  int blocks, warps;
+  main_shape(&blocks, &warps);
+  if (warps == 4)
+    k_main_records<4><<<blocks, 4 * kWarp, 0, st>>>(a.p, a.tab, a.w, a.g, a.n_rows);
+  else
+    k_main_records<8><<<blocks, 8 * kWarp, 0, st>>>(a.p, a.tab, a.w, a.g, a.n_rows);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 
@@ -318,7 +331,12 @@ int run_main_adjoint(const AccumArgs &a, cudaStream_t st) {
   if (cudaMemsetAsync(a.w.main_out, 0, sizeof(float) * kPixRec * (size_t)a.n_rows, st) != cudaSuccess)
     return LSIM_ERR_CUDA;
   if (a.n_rows <= 0) return LSIM_OK;
-  k_main_adjoint<<<kMainWarps / kMainBlockWarps, kMainBlockWarps * kWarp, 0, st>>>(a.p, a.tab, a.w, a.g, a.n_rows);
+  int blocks, warps;
+  main_shape(&blocks, &warps);
+  if (warps == 4)
+    k_main_adjoint<4><<<blocks, 4 * kWarp, 0, st>>>(a.p, a.tab, a.w, a.g, a.n_rows);
+  else
+    k_main_adjoint<8><<<blocks, 8 * kWarp, 0, st>>>(a.p, a.tab, a.w, a.g, a.n_rows);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 

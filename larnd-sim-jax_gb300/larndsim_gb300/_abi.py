@@ -74,6 +74,7 @@ _SIGNATURES = {
     "lsim_last_error": (C.c_char_p, []),
     "lsim_struct_sizes": (None, [C.POINTER(_sz)] * 3),
     "lsim_set_kernel_events": (None, [_vp, _vp]),
+    "lsim_set_tuning": (None, [_vp]),
     "lsim_lut_build_templates": (C.c_int, [_vp, _i32, _i32, _i32, _vp, _i32, _i32, _vp, _vp]),
     "lsim_lut_tables_bytes": (_sz, [_PP]),
     "lsim_lut_prepare": (C.c_int, [_PP, _vp, _vp, _sz, _vp]),

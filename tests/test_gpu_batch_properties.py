@@ -101,3 +101,28 @@ def test_large_shower_event_runs_deterministically(cuda):
     assert a == b
     assert a[0] > 0 and np.isfinite(a[0]) and all(np.isfinite(v) for v in a[1].values())
     assert chain._stage.n_valid > 1000
+
+
+def test_launch_shapes_do_not_change_results(cuda):
+    """Every launch shape the autotuner may pick gives bit-identical loss
+    and gradient."""
+    from larndsim_gb300 import grad, tune, workloads
+    from oracle import reference_np as R
+    p = small_params(n_neighbors=2)
+    tmpl = torch.from_numpy(R.load_lut_templates(workloads.synthetic_response(seed=0, nx=25, ny=25), p)).cuda()
+    tracks, fields = _batch(seed=60)
+    chain = grad.LUTChain(p, tmpl, tracks, fields)
+    target = chain.target(p)
+    pp = p.replace(eField=0.52, lifetime=2000.0, tran_diff=9e-6)
+    results = set()
+    try:
+        for cfg in tune.DEFAULT_CANDIDATES:
+            tune.set_tuning(cfg)
+            loss, g = chain.loss_and_grad(pp, target)
+            results.add((loss,) + tuple(g.values()))
+        cfg, times = tune.autotune(lambda: chain.loss_and_grad_device(pp, target), reps=1, warmup=0)
+        assert set(times) == {tuple(c[k] for k in tune.FIELDS) for c in tune.DEFAULT_CANDIDATES}
+        assert cfg in tune.DEFAULT_CANDIDATES
+    finally:
+        tune.set_tuning(None)
+    assert len(results) == 1
