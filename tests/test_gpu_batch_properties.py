@@ -126,3 +126,28 @@ def test_launch_shapes_do_not_change_results(cuda):
     finally:
         tune.set_tuning(None)
     assert len(results) == 1
+
+
+def test_parametrised_batch_rows_equal_single_event_rows(cuda):
+    """Parametrised mode (number_pix_neighbors = 0, Monte-Carlo diffusion
+    draws supplied per segment): the same batch invariance."""
+    from larndsim_gb300 import sim
+    from oracle import reference_np as R
+    p = small_params(n_neighbors=0, mc_diff=True)
+    tracks, fields = _batch(seed=80)
+    col = fields.index("eventID")
+    offsets = np.random.default_rng(3).standard_normal((tracks.shape[0], 3)).astype(np.float32)
+    sim.reset_size_history()
+    wfs, unique = sim.simulate_parametrized_wfs(p, tracks, fields, offsets=torch.from_numpy(offsets).cuda())
+    wfs, unique = wfs.cpu().numpy(), unique.cpu().numpy()
+    ev_b = np.where(unique >= 0, R.id2pixel(p, np.maximum(unique, 0))[3], -9)
+    for e in range(4):
+        m = tracks[:, col] == e
+        one = tracks[m].copy()
+        one[:, col] = 0
+        sim.reset_size_history()
+        w1, u1 = sim.simulate_parametrized_wfs(p, one, fields, offsets=torch.from_numpy(offsets[m]).cuda())
+        w1, u1 = w1.cpu().numpy(), u1.cpu().numpy()
+        rows_1 = w1[u1 >= 0]
+        assert rows_1.shape[0] > 10
+        np.testing.assert_array_equal(wfs[ev_b == e], rows_1)
