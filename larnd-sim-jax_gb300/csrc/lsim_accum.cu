@@ -262,15 +262,18 @@ __device__ __forceinline__ void neigh_vjp_one(const NDesc &d, const float v[kChu
   float sA = 0.f, sB = 0.f, gA0 = 0.f, gB0 = 0.f;   // sum v gA, sum v gB
   if (!(pk & kPackEdge)) {
     // interior window: every column in range (columns past cb + L + 1 hold
-    // zeros of the row padding and meet zero samples)
+    // zeros of the row padding and meet zero samples); the two sums advance
+    // together in one packed FMA per chunk
+    float2 sAB = make_float2(0.f, 0.f);
 #pragma unroll
     for (int c = 0; c < kChunks; ++c) {
       const int c1 = cb + c * kWarp + lane;
-      const float gA = grow[c1], gB = grow[c1 + 1];
-      sA = fmaf(v[c], gA, sA);
-      sB = fmaf(v[c], gB, sB);
-      if (c == 0) { gA0 = gA; gB0 = gB; }
+      const float2 g = make_float2(grow[c1], grow[c1 + 1]);
+      sAB = __ffma2_rn(make_float2(v[c], v[c]), g, sAB);
+      if (c == 0) { gA0 = g.x; gB0 = g.y; }
     }
+    sA = sAB.x;
+    sB = sAB.y;
   } else {
 #pragma unroll
     for (int c = 0; c < kChunks; ++c) {

@@ -263,14 +263,15 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 24 / kMainBlockWarps)
 #pragma unroll 1
         for (int e = 0; e < n; ++e) {
           const float4 *src = tab.wmp + (size_t)ms.off[e] * kWinSamples + lane;
-          float sx = 0.f, sy = 0.f, sz = 0.f;
+          float2 sxy = make_float2(0.f, 0.f);
+          float sz = 0.f;
 #pragma unroll
           for (int j = 0; j < kChunks; ++j) {
             const float4 t = __ldg(src + j * kWarp);
-            sx = fmaf(d[j], t.x, sx);
-            sy = fmaf(d[j], t.y, sy);
+            sxy = __ffma2_rn(make_float2(d[j], d[j]), make_float2(t.x, t.y), sxy);
             sz = fmaf(d[j], t.z, sz);
           }
+          const float sx = sxy.x, sy = sxy.y;
           const float W = ms.W[e], dW = ms.dW[e];
           const float sB = (sy * qb + sx * qa) + sz * qc;
           acc_ne = fmaf(W, sB, acc_ne);
