@@ -154,14 +154,27 @@ __device__ __noinline__ void window_apply_edge(float U0, float U1, float U2, flo
 // L + 1 add exact zeros.
 __device__ __forceinline__ void window_apply_interior(const float U[kChunks], int cb, int rl, float a, float b,
                                                       float *row, int lane) {
+  float P[kChunks];
   float sprev = 0.f;
 #pragma unroll
   for (int j = 0; j < kChunks; ++j) {
     const float sh = __shfl_sync(0xffffffffu, U[j], (lane + kWarp - 1) & (kWarp - 1));
-    const float prev = rl == 0 ? sprev : sh;
+    P[j] = rl == 0 ? sprev : sh;
     sprev = sh;
-    float &x = row[cb + rl + j * kWarp];
-    x = fmaf(U[j], b, fmaf(prev, a, x));
+  }
+  // chunk pairs advance in packed f32x2 FMAs
+  float *x = row + cb + rl;
+  const float2 aa = make_float2(a, a), bb = make_float2(b, b);
+#pragma unroll
+  for (int j = 0; j + 1 < kChunks; j += 2) {
+    float2 v = make_float2(x[j * kWarp], x[(j + 1) * kWarp]);
+    v = __ffma2_rn(make_float2(U[j], U[j + 1]), bb, __ffma2_rn(make_float2(P[j], P[j + 1]), aa, v));
+    x[j * kWarp] = v.x;
+    x[(j + 1) * kWarp] = v.y;
+  }
+  if (kChunks & 1) {
+    constexpr int j = kChunks - 1;
+    x[j * kWarp] = fmaf(U[j], b, fmaf(P[j], a, x[j * kWarp]));
   }
 }
 
