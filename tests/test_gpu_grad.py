@@ -55,7 +55,8 @@ def _check(g_gpu, g_fd, theta):
 
 
 @pytest.mark.parametrize("case", [dict(n_neighbors=1), dict(n_neighbors=2, seed=5, n_tracks=2, shower=300),
-                                  dict(n_neighbors=0, seed=6, n_tracks=2, shower=300)])
+                                  dict(n_neighbors=0, seed=6, n_tracks=2, shower=300),
+                                  dict(n_neighbors=4, seed=7, n_tracks=2, shower=200)])
 def test_loss_and_grad_vs_fp64_adjoint(cuda, case):
     from oracle import grad64 as G
     p, tmpl, tracks, fields, chain, target = _setup(**case)
