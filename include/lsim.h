@@ -98,7 +98,8 @@ typedef struct LsimCounts {
   int32_t n_main_rec;   /* main-bin records written by the last LUT accumulation */
   int32_t n_main_seg;   /* segments with main-bin records in the last LUT accumulation */
   int32_t n_big_slots;  /* internal: pixel slots whose segment lists are sorted by a whole block */
-  int32_t reserved[6];
+  int32_t n_heavy;      /* internal: pixels handed out first by the accumulation kernel */
+  int32_t reserved[5];
 } LsimCounts;
 
 int lsim_abi_version(void);

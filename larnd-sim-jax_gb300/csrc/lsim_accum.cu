@@ -582,12 +582,21 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a
   const int T = NT - 1;
   const int H = p.max_adc_values;
   const int n_valid = a.w.counts->n_valid;
+  const int n_heavy = a.w.counts->n_heavy;
   const bool early_exit = (a.normals == nullptr) && p.threshold > 0.f;
   for (;;) {
     int r = 0;
     if (lane == 0) r = atomicAdd(&a.w.counts->work, 1);
     r = __shfl_sync(0xffffffffu, r, 0);
-    if (r >= n_valid) break;
+    // work items: the heavy pixels first, then all pixels in grid order
+    // (skipping the heavy ones), so the grid does not end on a few long rows
+    if (r >= n_valid + n_heavy) break;
+    if (r < n_heavy) {
+      r = a.w.heavy[r];
+    } else {
+      r -= n_heavy;
+      if (n_heavy > 0 && a.w.heavy_flag[r]) continue;
+    }
     const int64_t slot = a.w.pix_slot[r];
     // adjoint mode: this lane's hit cotangent, or the target ADC of the
     // pixel (digitize(0) where the target has no such pixel), loaded early
@@ -778,6 +787,31 @@ __global__ void k_grad_finalize(const double *partials, int n_rec_blocks, const 
   }
 }
 
+// ---------------------------------------------------------------- work order
+
+// Pixels whose (2h+1)^2 neighbourhood holds more than kHeavyPixel segments
+// (contributions) are listed so that the persistent kernel starts with them.
+constexpr int kHeavyPixel = 2048;
+
+__global__ void k_heavy_pixels(Grid g, Workspace w) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= w.counts->n_valid) return;
+  const int64_t slot = w.pix_slot[r];
+  int cost = 0;
+  for (int dy = -g.h; dy <= g.h; ++dy)
+    for (int dx = -g.h; dx <= g.h; ++dx) cost += __ldg(w.cnt + slot - (int64_t)dy * g.nxe - dx);
+  const bool heavy = cost > kHeavyPixel;
+  w.heavy_flag[r] = heavy ? 1 : 0;
+  if (heavy) w.heavy[atomicAdd(&w.counts->n_heavy, 1)] = (int32_t)r;
+}
+
+static int run_heavy_pixels(const AccumArgs &a, cudaStream_t st) {
+  if (cudaMemsetAsync(&a.w.counts->n_heavy, 0, sizeof(int32_t), st) != cudaSuccess) return LSIM_ERR_CUDA;
+  if (a.n_rows <= 0) return LSIM_OK;
+  k_heavy_pixels<<<(unsigned)((a.n_rows + 255) / 256), 256, 0, st>>>(a.g, a.w);
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
 // ---------------------------------------------------------------- launch
 
 // Persistent grid: every SM filled to its occupancy limit.
@@ -841,6 +875,7 @@ int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st) {
   // the stored-waveform adjoint reuses the records (and their template
   // order) of the simulate_wfs pass that wrote the waveforms
   int rc = mode == kModeGradStored ? LSIM_OK : run_main_records(a, st);
+  if (rc == LSIM_OK) rc = run_heavy_pixels(a, st);
   if (rc != LSIM_OK) return rc;
   switch (mode) {
     case kModeWfs: return launch_mode<kModeWfs>(a, st);

@@ -108,6 +108,8 @@ struct Workspace {
   int32_t *seg_list, *pix_slot, *em1_slot;
   int32_t *big_slots;       // slots with more than kSortLocal segments (sorted by a block each)
   float *theta_derived;     // fit parameters and derived quantities for lsim_lut_stage1_theta (kThetaDerived)
+  int32_t *heavy;           // pixels with many contributions, handed out first (count in counts->reserved[0])
+  uint8_t *heavy_flag;      // per valid pixel: 1 if it is in the heavy list
   int32_t *scan_blocks;     // 3 ints per scan block (+1 block)
   float *pix_out;           // per valid pixel: [loss, 8 gradient terms] (kPixRec floats)
   double *red_partials;     // fixed-order reduction partials (kRedSlots * 16 doubles)
@@ -148,6 +150,8 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   size_t o_em1 = take(4 * (size_t)n_rows);
   size_t o_big = take(4 * ((size_t)n_rows / (kSortLocal + 1) + 1));
   size_t o_theta = take(4 * (size_t)kThetaDerived);
+  size_t o_heavy = take(4 * (size_t)n_rows);
+  size_t o_hflag = take((size_t)n_rows);
   size_t o_scan = take(3 * 4 * (size_t)nscan);
   size_t o_pix = take(4 * (size_t)kPixRec * (size_t)n_rows);
   size_t o_red = take(8 * (size_t)kRedSlots * 16);
@@ -173,6 +177,8 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   w.em1_slot = (int32_t *)(b + o_em1);
   w.big_slots = (int32_t *)(b + o_big);
   w.theta_derived = (float *)(b + o_theta);
+  w.heavy = (int32_t *)(b + o_heavy);
+  w.heavy_flag = (uint8_t *)(b + o_hflag);
   w.scan_blocks = (int32_t *)(b + o_scan);
   w.pix_out = (float *)(b + o_pix);
   w.red_partials = (double *)(b + o_red);

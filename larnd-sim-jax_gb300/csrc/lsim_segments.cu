@@ -14,7 +14,7 @@ namespace lsim {
 __global__ void k_reset_counts(LsimCounts *c) {
   if (threadIdx.x == 0) {
     c->n_valid = 0; c->n_em1 = 0; c->any_m1 = 0; c->status = 0; c->max_slot = 0; c->n_big_slots = 0;
-    c->bad_row = 0x7fffffff; c->work = 0; c->n_main_rec = 0; c->n_main_seg = 0;
+    c->bad_row = 0x7fffffff; c->work = 0; c->n_main_rec = 0; c->n_main_seg = 0; c->n_heavy = 0;
     for (int i = 0; i < (int)(sizeof(c->reserved) / sizeof(c->reserved[0])); ++i) c->reserved[i] = 0;
   }
 }

@@ -63,7 +63,7 @@ class LsimParams(C.Structure):
 
 class LsimCounts(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("n_valid", "n_em1", "any_m1", "status", "max_slot", "bad_row", "work",
-                                         "n_main_rec", "n_main_seg", "n_big_slots")] + [("reserved", C.c_int32 * 6)]
+                                         "n_main_rec", "n_main_seg", "n_big_slots", "n_heavy")] + [("reserved", C.c_int32 * 5)]
 
 
 _vp, _i64, _i32, _sz = C.c_void_p, C.c_int64, C.c_int32, C.c_size_t
