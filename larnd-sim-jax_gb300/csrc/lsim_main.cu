@@ -166,6 +166,13 @@ __global__ void k_main_order_scatter(Workspace w, int64_t n_rows) {
 
 // ---------------------------------------------------------------- kernels
 
+// L1 prefetch of the next segment's records (segments come in template
+// order, so their records are scattered; the next one's lines are fetched
+// while this one is processed).
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 template <int kMainBlockWarps>
 __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 16 / kMainBlockWarps) k_main_records(LsimParams p, Tables tab, Workspace w, Grid g,
                                                                            int64_t n_rows) {
@@ -178,6 +185,8 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 16 / kMainBlockWarps)
   block_range(w.counts->n_main_seg, &i0, &i1);
   for (int64_t i = i0; i < i1; i += kMainBlockWarps) {
     const int64_t s = w.seg_order[i];
+    if (lane < 2 && i + kMainBlockWarps < i1)
+      prefetch_l1(reinterpret_cast<const char *>(w.segf + w.seg_order[i + kMainBlockWarps]) + 64 * lane);
     const SegFwd &f = w.segf[s];
     const float ne = f.ne;
     const int32_t key = w.key[s];
@@ -235,6 +244,12 @@ __global__ void __launch_bounds__(kMainBlockWarps * kWarp, 24 / kMainBlockWarps)
   block_range(w.counts->n_main_seg, &i0, &i1);
   for (int64_t i = i0; i < i1; i += kMainBlockWarps) {
     const int64_t s = w.seg_order[i];
+    if (i + kMainBlockWarps < i1) {
+      const int64_t sn = w.seg_order[i + kMainBlockWarps];
+      if (lane < 2) prefetch_l1(reinterpret_cast<const char *>(w.segf + sn) + 64 * lane);
+      else if (lane < 4) prefetch_l1(reinterpret_cast<const char *>(w.sega + sn) + 64 * (lane - 2));
+      else if (lane < 4 + 21) prefetch_l1(w.mrec + (size_t)sn * kRecPerSeg * kRecFloats + 32 * (lane - 4));
+    }
     const SegFwd &f = w.segf[s];
     const float ne = f.ne;
     const int32_t key = w.key[s];
