@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--events", type=int, default=N_EVENTS, help="events per batch (profiling runs use fewer)")
+    ap.add_argument("--path", choices=["grad", "chop"], default="grad",
+                    help="grad: the fwd+bwd step (default); chop: on-device chop_tracks of one 500k-segment event")
     return ap.parse_args()
 
 
@@ -405,9 +407,136 @@ def run_reference(args):
     print(json.dumps(rec), flush=True)
 
 
+# ---------------------------------------------------------------- chop_tracks
+
+CHOP_SEGMENTS, CHOP_PRECISION, CHOP_CPU_TRACKS = 500_000, 0.001, 20_000
+
+
+def run_chop(args):
+    """On-device chop_tracks (optimize/dataio.py:63-106) of one 500k-segment
+    shower event at the reference's default step of 0.001 cm (about 50M
+    output rows, 5.2 GB).  value: output rows/s of lsim_chop_tracks with the
+    tracks in HBM and the output allocated (one count-and-fill call);
+    e2e: dataio.chop_tracks on pinned host tracks (copy in, count, read the
+    count, allocate, fill)."""
+    import torch
+    from larndsim_gb300 import _abi, dataio, sim, workloads
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _abi.load()
+    tracks, fields = workloads.large_shower_event(seed=2, n_segments=CHOP_SEGMENTS, n_subtracks=40)
+    t = torch.from_numpy(tracks).to(dev)
+    fm = _abi.field_map(fields)
+    n = t.shape[0]
+    ws = torch.empty(lib.lsim_chop_workspace_bytes(n), dtype=torch.uint8, device=dev)
+    cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    s = sim._stream()
+    _abi.check(lib, lib.lsim_chop_tracks(fm, t.data_ptr(), n, CHOP_PRECISION, None, 0, cnt.data_ptr(),
+                                         ws.data_ptr(), ws.numel(), s))
+    rows = int(cnt.item())
+    out = torch.empty((rows, len(fields)), dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        _abi.check(lib, lib.lsim_chop_tracks(fm, t.data_ptr(), n, CHOP_PRECISION, out.data_ptr(), rows,
+                                             cnt.data_ptr(), ws.data_ptr(), ws.numel(), s))
+
+    for _ in range(args.warmup):
+        step()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(torch.cuda.current_device())
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        starts[i].record()
+        step()
+        ends[i].record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in zip(starts, ends)]))
+    value = rows / (ms * 1e-3)
+    host = torch.from_numpy(tracks).pin_memory()
+    for _ in range(2):
+        dataio.chop_tracks(host, fields, CHOP_PRECISION)
+    torch.cuda.synchronize()
+    del out
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        r = dataio.chop_tracks(host, fields, CHOP_PRECISION)
+        del r
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    algo = 4 * len(fields) * (n + rows)          # read the tracks, write the steps
+    achieved = algo / (ms * 1e-3) / 1e9
+    rec = {"metric": "chop_tracks steps/s", "value": value, "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 (float64 step positions)", "data": "synthetic (seeded tracks)",
+           "config": {"workload": f"chop_tracks of one {n}-segment shower event (40 sub-tracks) at "
+                                  f"{CHOP_PRECISION} cm", "tracks": n, "steps_out": rows, "columns": len(fields),
+                      "l2": "flushed between timed steps (512 MiB write); output 5 GB >> L2"},
+           "e2e": {"value": rows / e2e_s, "unit": "steps/s", "ms_per_step": e2e_s * 1e3,
+                   "h2d_bytes_per_step": int(tracks.nbytes), "d2h_bytes_per_step": 8},
+           "roofline": {"bound": "hbm", "kernel": "lsim_chop_tracks (count, scan, offsets, fill; timed together)",
+                        "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "algorithmic_bytes": algo,
+                        "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None},
+           "gpu_launches": 4 * args.steps, "clocks": clk}
+    if not args.no_cpu_baseline:
+        from oracle import reference_np as R
+        sample = tracks[:CHOP_CPU_TRACKS]
+        t0 = time.perf_counter()
+        ref = R.chop_tracks(sample, fields, CHOP_PRECISION)
+        dt = time.perf_counter() - t0
+        rec["cpu_baseline"] = {"value": ref.shape[0] / dt, "unit": "steps/s", "cores": 1, "kind": "port",
+                               "sample": f"first {CHOP_CPU_TRACKS} tracks ({ref.shape[0]} steps), vectorised "
+                                         f"numpy restatement, {dt:.2f} s"}
+    print(json.dumps(rec), flush=True)
+
+
+def run_chop_reference(args):
+    """CPU arm of --path chop: the numpy restatement of chop_tracks, one
+    bounded sample (the first 20k tracks of the same event) per step."""
+    if dist_env()[0] != 0:
+        return
+    from larndsim_gb300 import workloads
+    from oracle import reference_np as R
+    tracks, fields = workloads.large_shower_event(seed=2, n_segments=CHOP_SEGMENTS, n_subtracks=40)
+    sample = tracks[:CHOP_CPU_TRACKS]
+    times, rows = [], 0
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        rows = R.chop_tracks(sample, fields, CHOP_PRECISION).shape[0]
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    ms = float(np.mean(times)) * 1e3
+    value = rows / (ms * 1e-3)
+    print(json.dumps({"metric": "chop_tracks steps/s", "value": value, "unit": "steps/s", "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
+                      "data": "synthetic (seeded tracks)",
+                      "config": {"workload": f"chop_tracks at {CHOP_PRECISION} cm, first {CHOP_CPU_TRACKS} "
+                                             "tracks of the 500k-segment shower event", "steps_out": rows},
+                      "cpu_baseline": {"value": value, "unit": "steps/s", "cores": 1, "kind": "port",
+                                       "sample": f"{CHOP_CPU_TRACKS} tracks, {rows} steps per step"},
+                      "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.path == "chop":
+        if args.impl == "reference":
+            run_chop_reference(args)
+        else:
+            run_chop(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -275,6 +275,27 @@ int lsim_hits_noalloc(const LsimParams *p, const float *adc, const float *ticks,
                       float *out_z, float *out_ticks, float *out_hit_prob, int32_t *out_event,
                       int32_t *out_pixels, int32_t *nb_valid_dev, void *stream);
 
+/* ---------------------------------------------------------------- input side */
+
+/* Workspace bytes of lsim_chop_tracks for n_rows input tracks. */
+size_t lsim_chop_workspace_bytes(int64_t n_rows);
+
+/* Cut each of the n_rows tracks (float32 rows of f->n_fields <= 96 columns)
+ * into max(ceil(length / precision), 1) steps: step k starts at
+ * start + k * precision * direction, every step has dx = precision and
+ * dE = dE * precision / length except the last, which ends at the track's
+ * end and takes the remaining dx and dE; x, y, z become the step midpoints
+ * and every other column is copied.  Output rows follow the input order.
+ * Replaces chop_tracks, optimize/dataio.py:63-106, with its float32/float64
+ * arithmetic (NumPy 2 promotion) reproduced bit for bit.
+ * The number of output rows goes to *n_out_dev (int64, device memory), or
+ * -1 when some track length is not finite (the reference's integer cast
+ * fails there); the first min(n_out, out_capacity) rows are written to out.
+ * A caller that does not know the count calls once with out = NULL and
+ * out_capacity = 0, reads *n_out_dev, and calls again. */
+int lsim_chop_tracks(const LsimFieldMap *f, const float *tracks, int64_t n_rows, double precision, float *out,
+                     int64_t out_capacity, int64_t *n_out_dev, void *ws, size_t ws_bytes, void *stream);
+
 /* ---------------------------------------------------------------- parametrised mode */
 
 /* Stage 1 of simulate_parametrized: shift, quench, drift, Monte-Carlo

@@ -311,6 +311,23 @@ int lsim_fee(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, 
   return wrap(run_fee(*p, wfs, n_pix, n_t, normals, adc_out, tick_out, integral_out, (cudaStream_t)stream), "lsim_fee");
 }
 
+size_t lsim_chop_workspace_bytes(int64_t n_rows) { return n_rows < 0 ? 0 : chop_workspace_bytes(n_rows); }
+
+int lsim_chop_tracks(const LsimFieldMap *f, const float *tracks, int64_t n_rows, double precision, float *out,
+                     int64_t out_capacity, int64_t *n_out_dev, void *ws, size_t ws_bytes, void *stream) {
+  g_err.clear();
+  int rc = check_fields(f);
+  if (rc) return rc;
+  if (n_rows < 0 || out_capacity < 0 || !n_out_dev || (n_rows > 0 && !tracks) || (out_capacity > 0 && !out))
+    return fail(LSIM_ERR_INVALID, "lsim_chop_tracks: bad arguments");
+  if (!(precision > 0) || !(precision < 1e30)) return fail(LSIM_ERR_INVALID, "lsim_chop_tracks: precision %g", precision);
+  if (!ws || ws_bytes < chop_workspace_bytes(n_rows))
+    return fail(LSIM_ERR_CAPACITY, "lsim_chop_tracks: workspace %zu < %zu bytes", ws_bytes,
+                chop_workspace_bytes(n_rows));
+  return wrap(run_chop(*f, tracks, n_rows, precision, out, out_capacity, n_out_dev, ws, (cudaStream_t)stream),
+              "lsim_chop_tracks");
+}
+
 size_t lsim_hits_workspace_bytes(int64_t n_pix, int32_t max_adc_values) {
   return hits_ws_bytes(n_pix * (int64_t)max_adc_values);
 }

@@ -57,6 +57,11 @@ int run_build_templates(const float *response, int nx, int ny, int nt, const flo
                         int extent, float *out, cudaStream_t st);
 int run_prepare_tables(const LsimParams &p, const float *templates, void *tables, cudaStream_t st);
 
+// lsim_chop.cu
+size_t chop_workspace_bytes(int64_t n_rows);
+int run_chop(const LsimFieldMap &f, const float *tracks, int64_t n_rows, double precision, float *out,
+             int64_t capacity, int64_t *n_out, void *ws, cudaStream_t st);
+
 int device_sm_count();
 
 // profiling events around the pixel-accumulation kernel (lsim_set_kernel_events)

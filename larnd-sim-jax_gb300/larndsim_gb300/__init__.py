@@ -1,7 +1,8 @@
 """GB300-native (sm_103a) implementation of larnd-sim-jax's simulate path.
 
 Drop-in functions with the reference's names (src/larndsim/sim_jax.py,
-consts_jax.py, fee_jax.py, losses_jax.py, optimize/strategies.py), backed by
+consts_jax.py, fee_jax.py, losses_jax.py, optimize/strategies.py,
+optimize/dataio.py), backed by
 hand-written CUDA kernels in ``liblsim.so`` (C ABI: include/lsim.h).
 """
 
@@ -11,9 +12,10 @@ from .sim import (get_adc_values, load_lut, pad_size, prepare_lut, simulate_para
                   simulate_stochastic, simulate_wfs)
 from .fee import digitize  # noqa: F401
 from .losses import adc2charge  # noqa: F401
+from .dataio import chop_tracks  # noqa: F401
 
 __all__ = [
     "Params", "RecombinationMode", "build_params_class", "default_params", "get_vdrift",
     "load_detector_properties", "get_adc_values", "load_lut", "pad_size", "prepare_lut",
-    "simulate_parametrized", "simulate_stochastic", "simulate_wfs", "digitize", "adc2charge",
+    "simulate_parametrized", "simulate_stochastic", "simulate_wfs", "digitize", "adc2charge", "chop_tracks",
 ]

@@ -648,3 +648,53 @@ def load_lut_templates(response, params):
         out[i] = conv.reshape(r.shape).astype(np.float32)
     out[0] = np.asarray(response, np.float32)
     return out
+
+
+# ---------------------------------------------------------------- input side
+
+def chop_tracks(tracks, fields, precision=0.001):
+    """optimize/dataio.py:63-106: cut every track into steps of length
+    ``precision`` (the last step takes the remainder), vectorised.
+
+    Arithmetic follows NumPy 2 promotion of the reference's expressions:
+    the length (left-to-right float32 sum of squares, float32 sqrt), the
+    direction, the step count and the per-step dE are float32; the step
+    positions ``start + k*precision*direction`` and the last step's dE and
+    dx are float64 and rounded once when stored; midpoints are float32.
+    """
+    t = np.asarray(tracks, F32)
+    col = {k: fields.index(k) for k in ("x_start", "y_start", "z_start", "x_end", "y_end", "z_end",
+                                           "x", "y", "z", "dE", "dx")}
+    start = t[:, [col["x_start"], col["y_start"], col["z_start"]]]
+    end = t[:, [col["x_end"], col["y_end"], col["z_end"]]]
+    seg = (end - start).astype(F32)
+    sq = (seg * seg).astype(F32)
+    length = ((sq[:, 0] + sq[:, 1]).astype(F32) + sq[:, 2]).astype(F32)
+    length = np.sqrt(length).astype(F32)                                   # dataio.py:98
+    lpe = (length + F32(1e-10)).astype(F32)
+    direction = (seg / lpe[:, None]).astype(F32)                           # :100
+    nsteps = np.maximum(np.ceil((length / F32(precision)).astype(F32)), F32(1))
+    if not np.all(np.isfinite(nsteps)):
+        raise ValueError("chop_tracks: non-finite track length")
+    nsteps = nsteps.astype(np.int64)                                       # :101
+    src = np.repeat(np.arange(t.shape[0]), nsteps)
+    first = np.concatenate([[0], np.cumsum(nsteps)[:-1]]).astype(np.int64)
+    k = np.arange(src.shape[0], dtype=np.int64) - first[src]
+    last = k == nsteps[src] - 1
+    out = t[src].copy()
+    out[:, col["dE"]] = ((t[src, col["dE"]] * F32(precision)).astype(F32) / lpe[src]).astype(F32)   # :67
+    p = float(precision)
+    for a, (cs, ce) in enumerate((("x_start", "x_end"), ("y_start", "y_end"), ("z_start", "z_end"))):
+        s0 = t[src, col[cs]].astype(np.float64)
+        d = direction[src, a].astype(np.float64)
+        out[:, col[cs]] = (s0 + (k * p) * d).astype(F32)                   # :70-72
+        out[:, col[ce]] = np.where(last, t[src, col[ce]], (s0 + (p * (k + 1)) * d).astype(F32))   # :74-76, :80-82
+    out[:, col["dx"]] = F32(p)                                             # :77
+    n1 = (nsteps[src] - 1).astype(np.float64)
+    de_last = (t[src, col["dE"]].astype(np.float64) * (1 - p * n1 / lpe[src].astype(np.float64))).astype(F32)
+    dx_last = (length[src].astype(np.float64) - p * n1).astype(F32)
+    out[:, col["dE"]] = np.where(last, de_last, out[:, col["dE"]])         # :83
+    out[:, col["dx"]] = np.where(last, dx_last, out[:, col["dx"]])         # :84
+    for cm, cs, ce in (("x", "x_start", "x_end"), ("y", "y_start", "y_end"), ("z", "z_start", "z_end")):
+        out[:, col[cm]] = (F32(0.5) * (out[:, col[cs]] + out[:, col[ce]]).astype(F32)).astype(F32)   # :87-89
+    return out
