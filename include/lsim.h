@@ -296,6 +296,33 @@ size_t lsim_chop_workspace_bytes(int64_t n_rows);
 int lsim_chop_tracks(const LsimFieldMap *f, const float *tracks, int64_t n_rows, double precision, float *out,
                      int64_t out_capacity, int64_t *n_out_dev, void *ws, size_t ws_bytes, void *stream);
 
+/* ---------------------------------------------------------------- probabilistic front end */
+
+/* Pixel centres, plane and event of each pixel id (any of the outputs may
+ * be NULL).  Replaces id2pixel + get_pixel_coordinates,
+ * src/larndsim/detsim_jax.py:264-306, as simulate_probabilistic uses them
+ * (src/larndsim/sim_jax.py:807-811). */
+int lsim_pixel_coords(const LsimParams *p, const int32_t *unique_pixels, int64_t n_pix, float *x_out, float *y_out,
+                      int32_t *plane_out, int32_t *event_out, void *stream);
+
+/* Workspace bytes of lsim_fee_prob (one flag per hit step). */
+size_t lsim_fee_prob_workspace_bytes(const LsimParams *p);
+
+/* Probabilistic self-trigger front end on waveforms wfs[n_pix][n_t]
+ * (n_t <= 2048): the beam search over n_paths (fee_paths_scaling <= 32)
+ * paths and p->max_adc_values hit steps of
+ * get_adc_values_average_noise_vmap, src/larndsim/fee_jax.py:386-461
+ * (step _find_one_hit_step :334-384, log_diff_ndtr :33-53), with noise
+ * sigma p->reset_noise (> 0) and the whole batch stopped once no pixel keeps
+ * a total path probability above stop_threshold.  Outputs, each optional:
+ * log_prob_out and charge_out [n_pix][H][n_t - 1] (the reference's two
+ * outputs after its moveaxis), and the reductions of get_average_hit_values
+ * (fee_jax.py:463-480) applied to exp(log_prob) and digitize(charge):
+ * exp_tick_out, exp_adc_out, lambda_out [n_pix][H] (all three or none). */
+int lsim_fee_prob(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, int32_t n_paths,
+                  float stop_threshold, float *log_prob_out, float *charge_out, float *exp_tick_out,
+                  float *exp_adc_out, float *lambda_out, void *ws, size_t ws_bytes, void *stream);
+
 /* ---------------------------------------------------------------- parametrised mode */
 
 /* Stage 1 of simulate_parametrized: shift, quench, drift, Monte-Carlo

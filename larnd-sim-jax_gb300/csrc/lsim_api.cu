@@ -311,6 +311,39 @@ int lsim_fee(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, 
   return wrap(run_fee(*p, wfs, n_pix, n_t, normals, adc_out, tick_out, integral_out, (cudaStream_t)stream), "lsim_fee");
 }
 
+int lsim_pixel_coords(const LsimParams *p, const int32_t *unique_pixels, int64_t n_pix, float *x_out, float *y_out,
+                      int32_t *plane_out, int32_t *event_out, void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (n_pix < 0 || (n_pix > 0 && !unique_pixels)) return fail(LSIM_ERR_INVALID, "lsim_pixel_coords: bad arguments");
+  return wrap(run_pixel_coords(*p, unique_pixels, n_pix, x_out, y_out, plane_out, event_out, (cudaStream_t)stream),
+              "lsim_pixel_coords");
+}
+
+size_t lsim_fee_prob_workspace_bytes(const LsimParams *p) {
+  return p ? fee_prob_workspace_bytes(p->max_adc_values) : 0;
+}
+
+int lsim_fee_prob(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, int32_t n_paths,
+                  float stop_threshold, float *log_prob_out, float *charge_out, float *exp_tick_out,
+                  float *exp_adc_out, float *lambda_out, void *ws, size_t ws_bytes, void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (n_pix < 0 || (n_pix > 0 && !wfs)) return fail(LSIM_ERR_INVALID, "lsim_fee_prob: bad waveform arguments");
+  const bool any_red = exp_tick_out || exp_adc_out || lambda_out;
+  if (any_red && !(exp_tick_out && exp_adc_out && lambda_out))
+    return fail(LSIM_ERR_INVALID, "lsim_fee_prob: give all three of exp_tick, exp_adc, lambda or none");
+  if (!(stop_threshold > 0.0f)) return fail(LSIM_ERR_INVALID, "lsim_fee_prob: stop_threshold %g", stop_threshold);
+  if (!ws || ws_bytes < fee_prob_workspace_bytes(p->max_adc_values))
+    return fail(LSIM_ERR_CAPACITY, "lsim_fee_prob: workspace %zu < %zu bytes", ws_bytes,
+                fee_prob_workspace_bytes(p->max_adc_values));
+  return wrap(run_fee_prob(*p, wfs, n_pix, n_t, n_paths, stop_threshold, log_prob_out, charge_out, exp_tick_out,
+                           exp_adc_out, lambda_out, ws, (cudaStream_t)stream),
+              "lsim_fee_prob");
+}
+
 size_t lsim_chop_workspace_bytes(int64_t n_rows) { return n_rows < 0 ? 0 : chop_workspace_bytes(n_rows); }
 
 int lsim_chop_tracks(const LsimFieldMap *f, const float *tracks, int64_t n_rows, double precision, float *out,

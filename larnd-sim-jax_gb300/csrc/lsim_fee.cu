@@ -150,6 +150,26 @@ __global__ void k_hits_write(LsimParams p, const float *adc, const float *ticks,
   out_pixels[o] = pid;
 }
 
+// Per-pixel id2pixel + get_pixel_coordinates (detsim_jax.py:264-306), the
+// same centre arithmetic as the hit compaction above.
+__global__ void k_pixel_coords(LsimParams p, const int32_t *unique_pixels, int64_t n, float *x, float *y,
+                               int32_t *plane, int32_t *event) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PixelGeo g = id2pixel(p, unique_pixels[i]);
+  if (x) x[i] = __fadd_rn(__fmaf_rn((float)g.px, p.pixel_pitch, border(p, g.plane, 0, 0)), p.half_pitch);
+  if (y) y[i] = __fadd_rn(__fmaf_rn((float)g.py, p.pixel_pitch, border(p, g.plane, 1, 0)), p.half_pitch);
+  if (plane) plane[i] = g.plane;
+  if (event) event[i] = g.event;
+}
+
+int run_pixel_coords(const LsimParams &p, const int32_t *unique_pixels, int64_t n, float *x, float *y,
+                     int32_t *plane, int32_t *event, cudaStream_t st) {
+  if (n <= 0) return LSIM_OK;
+  k_pixel_coords<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, unique_pixels, n, x, y, plane, event);
+  return LSIM_OK;
+}
+
 size_t hits_ws_bytes(int64_t n) { return align256(4 * (size_t)((n + kHitTile - 1) / kHitTile + 1)); }
 
 int run_hits(const LsimParams &p, const float *adc, const float *ticks, const int32_t *unique_pixels, int64_t n_pix,

@@ -57,6 +57,15 @@ int run_build_templates(const float *response, int nx, int ny, int nt, const flo
                         int extent, float *out, cudaStream_t st);
 int run_prepare_tables(const LsimParams &p, const float *templates, void *tables, cudaStream_t st);
 
+int run_pixel_coords(const LsimParams &p, const int32_t *unique_pixels, int64_t n, float *x, float *y,
+                     int32_t *plane, int32_t *event, cudaStream_t st);
+
+// lsim_fee_prob.cu
+size_t fee_prob_workspace_bytes(int32_t max_adc_values);
+int run_fee_prob(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, int32_t n_paths,
+                 float stop_threshold, float *log_prob, float *charge, float *e_tick, float *e_adc, float *lam,
+                 void *ws, cudaStream_t st);
+
 // lsim_chop.cu
 size_t chop_workspace_bytes(int64_t n_rows);
 int run_chop(const LsimFieldMap &f, const float *tracks, int64_t n_rows, double precision, float *out,

@@ -5,7 +5,8 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from .sim import get_adc_values  # noqa: F401  (fee_jax.get_adc_values)
+from .sim import (average_hit_values, get_adc_values, get_adc_values_average_noise_vmap,  # noqa: F401
+                  get_average_hit_values)
 
 
 def digitize(params, integral_list):

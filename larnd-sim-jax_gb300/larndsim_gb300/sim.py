@@ -342,3 +342,81 @@ def simulate_parametrized(params, tracks, fields, rngseed=0, offsets=None, norma
     wfs, unique = simulate_parametrized_wfs(params, tracks, fields, rngseed, offsets)
     out, _ = _fee_and_hits(params, wfs, unique, wfs.shape[1] + 1 - 3, rngseed + 1, normals)
     return (out, wfs, unique) if return_wfs else out
+
+
+# ---------------------------------------------------------------- probabilistic front end
+
+def _fee_prob(params, wfs, stop_threshold, distributions, reductions):
+    lib = _abi.load()
+    w = torch.as_tensor(wfs).to(device=_device(), dtype=torch.float32).contiguous()
+    if w.dim() != 2:
+        raise ValueError(f"wfs must be (n_pixels, n_ticks), got {tuple(w.shape)}")
+    if not params.RESET_NOISE_CHARGE > 0:
+        raise ValueError("the probabilistic front end needs RESET_NOISE_CHARGE > 0 (its noise width)")
+    P, T = w.shape
+    H = int(params.MAX_ADC_VALUES)
+    lp = _abi.make_params(params)
+    ws = torch.empty(lib.lsim_fee_prob_workspace_bytes(lp), dtype=torch.uint8, device=w.device)
+    f = dict(dtype=torch.float32, device=w.device)
+    log_prob = torch.empty((P, H, T - 1), **f) if distributions else None
+    charge = torch.empty((P, H, T - 1), **f) if distributions else None
+    red = [torch.empty((P, H), **f) for _ in range(3)] if reductions else [None] * 3
+    _abi.check(lib, lib.lsim_fee_prob(lp, _ptr(w), P, T, int(params.fee_paths_scaling), float(stop_threshold),
+                                      _ptr(log_prob), _ptr(charge), *(_ptr(r) for r in red), _ptr(ws),
+                                      ws.numel(), _stream()))
+    return log_prob, charge, red
+
+
+def get_adc_values_average_noise_vmap(params, wfs, stop_threshold=1e-9):
+    """Probabilistic self-trigger front end (fee_jax.py:386-461): a beam
+    search over ``fee_paths_scaling`` paths and MAX_ADC_VALUES hits with
+    noise width RESET_NOISE_CHARGE.  Returns (log_prob, charge), each
+    (P, MAX_ADC_VALUES, T - 1): the log-probability that hit h is read at
+    each tick and the expected charge if it is."""
+    log_prob, charge, _ = _fee_prob(params, wfs, stop_threshold, True, False)
+    return log_prob, charge
+
+
+def average_hit_values(params, wfs, stop_threshold=1e-9):
+    """get_average_hit_values (fee_jax.py:463-480) of the probabilistic
+    front end's output, fused into the beam search so the (P, H, T - 1)
+    distributions are never stored: (expected_ticks, expected_adcs,
+    lambda), each (P, MAX_ADC_VALUES)."""
+    _, _, (e_tick, e_adc, lam) = _fee_prob(params, wfs, stop_threshold, False, True)
+    return e_tick, e_adc, lam
+
+
+def get_average_hit_values(ticks_prob, adcs_distrib):
+    """fee_jax.py:463-480 on given distributions (probabilities, not logs):
+    (expected_ticks, expected_adcs, lambda) per (pixel, hit)."""
+    tp = torch.as_tensor(ticks_prob, dtype=torch.float32)
+    ad = torch.as_tensor(adcs_distrib, dtype=torch.float32, device=tp.device)
+    lam = tp.sum(dim=2)
+    ticks = torch.arange(tp.shape[2], dtype=torch.float32, device=tp.device)
+    den = torch.clamp(lam, min=1e-10)
+    return (ticks * tp).sum(dim=2) / den, (ad * tp).sum(dim=2) / den, lam
+
+
+def pixel_coordinates(params, unique_pixels):
+    """(pixel_x, pixel_y, plane, event) of each pixel id: id2pixel +
+    get_pixel_coordinates (detsim_jax.py:264-306)."""
+    lib = _abi.load()
+    u = torch.as_tensor(unique_pixels).to(device=_device(), dtype=torch.int32).contiguous()
+    n = u.shape[0]
+    x = torch.empty(n, dtype=torch.float32, device=u.device)
+    y = torch.empty(n, dtype=torch.float32, device=u.device)
+    plane = torch.empty(n, dtype=torch.int32, device=u.device)
+    event = torch.empty(n, dtype=torch.int32, device=u.device)
+    _abi.check(lib, lib.lsim_pixel_coords(_abi.make_params(params), _ptr(u), n, _ptr(x), _ptr(y), _ptr(plane),
+                                          _ptr(event), _stream()))
+    return x, y, plane, event
+
+
+def simulate_probabilistic(params, wfs, unique_pixels):
+    """sim_jax.py:771-813: (adcs_distrib, pixel_x, pixel_y, ticks_prob,
+    event); ticks_prob holds the log-probabilities of the beam search and
+    adcs_distrib the digitised expected charges, both (P, H, T - 1)."""
+    from .fee import digitize
+    log_prob, charge = get_adc_values_average_noise_vmap(params, wfs)
+    x, y, _, event = pixel_coordinates(params, unique_pixels)
+    return digitize(params, charge), x, y, log_prob, event

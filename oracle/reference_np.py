@@ -698,3 +698,185 @@ def chop_tracks(tracks, fields, precision=0.001):
     for cm, cs, ce in (("x", "x_start", "x_end"), ("y", "y_start", "y_end"), ("z", "z_start", "z_end")):
         out[:, col[cm]] = (F32(0.5) * (out[:, col[cs]] + out[:, col[ce]]).astype(F32)).astype(F32)   # :87-89
     return out
+
+
+# ---------------------------------------------------------------- probabilistic front end
+
+# jax.scipy.special.log_ndtr (the third-party arithmetic this path calls;
+# JAX is not vendored with the reference and is unpinned): for float32 the
+# published piecewise form switches to -ndtr(-x) above x = 5 and to the
+# order-3 asymptotic series below x = -10.
+LOG_NDTR_LOWER32, LOG_NDTR_UPPER32 = -10.0, 5.0
+
+
+def ndtr32(x):
+    """Standard normal CDF as jax.scipy.special.ndtr evaluates it (erf near
+    zero, erfc in the tails), float32."""
+    x = np.asarray(x, F32)
+    hs2 = F32(0.5 * np.sqrt(2.0))
+    w = (x * hs2).astype(F32)
+    z = np.abs(w)
+    y = np.where(z < hs2, F32(1) + special.erf(w).astype(F32),
+                 np.where(w > 0, F32(2) - special.erfc(z).astype(F32), special.erfc(z).astype(F32)))
+    return (F32(0.5) * y.astype(F32)).astype(F32)
+
+
+def log_ndtr32(x):
+    """log of the standard normal CDF, float32, piecewise as above."""
+    x = np.asarray(x, F32)
+    lo, hi = F32(LOG_NDTR_LOWER32), F32(LOG_NDTR_UPPER32)
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        upper = -ndtr32(-x)
+        mid = np.log(ndtr32(np.maximum(x, lo))).astype(F32)
+        xl = np.minimum(x, lo)
+        x2 = (xl * xl).astype(F32)
+        log_scale = ((-(x2 / F32(2))) - np.log(-xl).astype(F32) - F32(0.5 * np.log(2 * np.pi))).astype(F32)
+        # 1 + even - odd with the terms (2n-1)!! / x^(2n), n = 1, 2, 3
+        x4 = (x2 * x2).astype(F32)
+        x6 = (x4 * x2).astype(F32)
+        odd = (F32(1) / x2 + F32(15) / x6).astype(F32)
+        even = (F32(3) / x4).astype(F32)
+        series = ((F32(1) + even) - odd).astype(F32)
+        lower = (log_scale + np.log(series).astype(F32)).astype(F32)
+    return np.where(x > hi, upper, np.where(x > lo, mid, lower)).astype(F32)
+
+
+def softplus32(y):
+    """jax.nn.softplus = logaddexp(y, 0) = max(y, 0) + log1p(exp(-|y|))."""
+    y = np.asarray(y, F32)
+    with np.errstate(over="ignore"):
+        return (np.maximum(y, F32(0)) + np.log1p(np.exp(-np.abs(y))).astype(F32)).astype(F32)
+
+
+def sigmoid32(x):
+    x = np.asarray(x, F32)
+    with np.errstate(over="ignore"):
+        return (F32(1) / (F32(1) + np.exp(-x).astype(F32))).astype(F32)
+
+
+def soft_max32(x, lo, sharpness):
+    """fee_jax.py:13-20: lo + softplus((x - lo) * s) / s."""
+    s = F32(sharpness)
+    return (F32(lo) + softplus32(((np.asarray(x, F32) - F32(lo)) * s).astype(F32)) / s).astype(F32)
+
+
+def soft_where32(cond, true_val, false_val, sharpness):
+    """fee_jax.py:23-30: w * true + (1 - w) * false, w = sigmoid(cond * s)."""
+    w = sigmoid32((np.asarray(cond, F32) * F32(sharpness)).astype(F32))
+    return ((w * np.asarray(true_val, F32)).astype(F32) + ((F32(1) - w) * F32(false_val)).astype(F32)).astype(F32)
+
+
+def log_diff_ndtr32(a, b, la=None, lb=None):
+    """fee_jax.py:33-53: log(Phi(a) - Phi(b)) with the smooth clamps."""
+    a = np.asarray(a, F32)
+    b = np.asarray(b, F32)
+    la = log_ndtr32(a) if la is None else la
+    lb = log_ndtr32(b) if lb is None else lb
+    safe = np.where(a > b, (lb - la).astype(F32), F32(-1))
+    neg = (-np.expm1(safe)).astype(F32)
+    neg_safe = soft_max32(neg, 1e-30, 1e10)
+    with np.errstate(divide="ignore"):
+        lt = np.log(neg_safe).astype(F32)
+    lts = soft_max32(lt, -100.0, 10.0)
+    lp = (la + lts).astype(F32)
+    return soft_where32((a - b).astype(F32), lp, -1000.0, 1000.0)
+
+
+def logsumexp32(x, axis):
+    x = np.asarray(x, F32)
+    m = np.max(x, axis=axis, keepdims=True)
+    m = np.where(np.isfinite(m), m, F32(0)).astype(F32)
+    s = np.sum(np.exp((x - m).astype(F32)).astype(F32), axis=axis, keepdims=True, dtype=F32)
+    with np.errstate(divide="ignore"):
+        return (np.log(s).astype(F32) + m).astype(F32).squeeze(axis)
+
+
+def top_k_indices(x, k):
+    """lax.top_k indices: largest first, equal values in index order."""
+    return np.argsort(-np.asarray(x, np.float64), axis=-1, kind="stable")[..., :k]
+
+
+def find_one_hit_step(q_sum, charges, log_probs, sigma, threshold, interval, n_values):
+    """fee_jax.py:334-384 for P pixels at once: q_sum (P, T), charges and
+    log_probs (P, K).  Returns (charges', log_probs') and the step outputs
+    (log_total_hit_dist_tick (P, T-1), esperance_value (P, T-1))."""
+    P, T = q_sum.shape
+    z = F32(1.0 / sigma)
+    thr = F32(threshold)
+    sh = np.clip(np.arange(T - 1) + interval + 1, 0, T - 1)
+    Q = (q_sum[:, None, :] - charges[:, :, None]).astype(F32)                       # (P, K, T)
+    qmax = np.maximum.accumulate(Q, axis=2)
+    zm = ((qmax - thr) * z).astype(F32)
+    lm = log_ndtr32(zm)
+    log_guess = log_diff_ndtr32(zm[..., 1:], zm[..., :-1], lm[..., 1:], lm[..., :-1])
+    zq = ((Q - thr) * z).astype(F32)
+    lq = log_ndtr32(zq)
+    lpe = log_diff_ndtr32(zq[..., sh], zq[..., :-1], lq[..., sh], lq[..., :-1])
+    lpe = np.minimum(lpe, log_guess)
+    lpe = soft_max32(lpe, -1000.0, 1.0)
+    esp = ((q_sum[:, sh] + thr).astype(F32) - (F32(0.5) * (q_sum[:, 1:] + q_sum[:, :-1]).astype(F32))).astype(F32)
+    lpe = soft_where32((esp - thr).astype(F32)[:, None, :], lpe, -1000.0, 10.0)
+    lp = log_probs[:, :, None]
+    hit = logsumexp32((lpe + lp).astype(F32), axis=1)
+    dist = logsumexp32((log_guess + lp).astype(F32), axis=1)
+    next_q = Q[:, :, np.clip(sh + 1, 0, T - 1)]
+    maxfut = np.maximum.accumulate(Q[:, :, ::-1], axis=2)[:, :, ::-1]
+    fe = np.clip(sh + interval + 1, 0, T - 1)
+    lf = log_ndtr32((((maxfut[:, :, fe] - next_q).astype(F32) - thr) * z).astype(F32))
+    sel = logsumexp32(((log_guess + lf).astype(F32) + lp).astype(F32), axis=1)
+    top = top_k_indices(sel, n_values)                                              # (P, K)
+    new_lp = np.take_along_axis(dist, top, axis=1)
+    best = np.clip(sh[top] + 1, 0, T - 1)
+    new_c = np.take_along_axis(q_sum, best, axis=1)
+    return (new_c.astype(F32), new_lp.astype(F32)), (hit, esp)
+
+
+def get_adc_values_average_noise(params, wfs, stop_threshold=1e-9):
+    """fee_jax.py:386-461: beam search over MAX_ADC_VALUES hits with
+    fee_paths_scaling paths, stopped for the whole batch once no pixel keeps
+    a total path probability above stop_threshold.  Returns
+    (log_prob (P, H, T-1), charge (P, H, T-1))."""
+    wfs = np.asarray(wfs, F32)
+    P, T = wfs.shape
+    K = int(params.fee_paths_scaling)
+    H = int(params.MAX_ADC_VALUES)
+    interval = fee_interval(params)
+    q_sum = np.cumsum((wfs * F32(params.t_sampling)).astype(F32), axis=1, dtype=F32)
+    c = np.zeros((P, K), F32)
+    lp = np.full((P, K), F32(-1000))
+    lp[:, 0] = 0
+    log_stop = np.log(F32(stop_threshold)).astype(F32)
+    out_lp = np.full((P, H, T - 1), F32(-1000))
+    out_q = np.zeros((P, H, T - 1), F32)
+    active = True
+    for h in range(H):
+        if not active:
+            break
+        (c, lp), (hit, esp) = find_one_hit_step(q_sum, c, lp, params.RESET_NOISE_CHARGE,
+                                                 params.DISCRIMINATION_THRESHOLD, interval, K)
+        out_lp[:, h] = hit
+        out_q[:, h] = esp
+        active = bool(np.any(logsumexp32(lp, axis=1) > log_stop))
+    return out_lp, out_q
+
+
+def get_average_hit_values(ticks_prob, adcs_distrib):
+    """fee_jax.py:463-480: per (pixel, hit) the total probability, the
+    expected tick and the expected ADC."""
+    tp = np.asarray(ticks_prob, F32)
+    lam = tp.sum(axis=2, dtype=F32)
+    ticks = np.arange(tp.shape[2], dtype=F32)
+    den = np.maximum(lam, F32(1e-10))
+    e_tick = ((ticks[None, None, :] * tp).sum(axis=2, dtype=F32) / den).astype(F32)
+    e_adc = ((np.asarray(adcs_distrib, F32) * tp).sum(axis=2, dtype=F32) / den).astype(F32)
+    return e_tick, e_adc, lam
+
+
+def simulate_probabilistic(params, wfs, unique_pixels):
+    """sim_jax.py:771-813: (adcs_distrib, pixel_x, pixel_y, ticks_prob, event)
+    with ticks_prob the log-probabilities of the beam search."""
+    log_prob, charge = get_adc_values_average_noise(params, wfs)
+    adcs = digitize(params, charge)
+    px, py, plane, event = id2pixel(params, np.asarray(unique_pixels))
+    pc = get_pixel_coordinates(params, px, py, plane)
+    return adcs, pc[:, 0], pc[:, 1], log_prob, event
