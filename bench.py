@@ -64,8 +64,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--events", type=int, default=N_EVENTS, help="events per batch (profiling runs use fewer)")
-    ap.add_argument("--path", choices=["grad", "chop"], default="grad",
-                    help="grad: the fwd+bwd step (default); chop: on-device chop_tracks of one 500k-segment event")
+    ap.add_argument("--path", choices=["grad", "chop", "prob"], default="grad",
+                    help="grad: the fwd+bwd step (default); chop: on-device chop_tracks of one 500k-segment event; "
+                         "prob: the probabilistic front end on the waveforms of 8 events")
     return ap.parse_args()
 
 
@@ -500,6 +501,85 @@ def run_chop(args):
     print(json.dumps(rec), flush=True)
 
 
+# ---------------------------------------------------------------- probabilistic front end
+
+PROB_EVENTS, PROB_CPU_PIXELS = 8, 16
+
+
+def _prob_workload(seed=0):
+    """Waveforms (valid rows) of the first 8 events of the batched
+    workload, LUT mode n_neighbors = 4, L = 150, noise width 900 e-."""
+    from larndsim_gb300 import sim, workloads
+    params = nominal_params().replace(RESET_NOISE_CHARGE=900.0)
+    tmpl, params = sim.load_lut(workloads.synthetic_response(seed=0), params)
+    tracks, fields = workload(0, seed, n_events=PROB_EVENTS)
+    wfs, unique = sim.simulate_wfs(params, tmpl, tracks, fields)
+    return params, wfs[unique >= 0].contiguous()
+
+
+def run_prob(args):
+    """The beam search of get_adc_values_average_noise_vmap
+    (fee_jax.py:386-461) with the reductions of get_average_hit_values
+    fused in (lsim_fee_prob), on every simulated pixel of 8 events.
+    value: pixels/s with the waveforms in HBM; e2e: pinned host waveforms
+    in, the three (P, H) reductions out."""
+    import torch
+    from larndsim_gb300 import sim
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    params, wfs = _prob_workload(args.seed)
+    P = wfs.shape[0]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=wfs.device)
+    for _ in range(args.warmup):
+        sim.average_hit_values(params, wfs)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(torch.cuda.current_device())
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        starts[i].record()
+        sim.average_hit_values(params, wfs)
+        ends[i].record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in zip(starts, ends)]))
+    host = wfs.cpu().pin_memory()
+    e2e_steps = max(3, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        out = [t.cpu() for t in sim.average_hit_values(params, host)]
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    H = int(params.MAX_ADC_VALUES)
+    rec = {"metric": "probabilistic FEE pixels/s", "value": P / (ms * 1e-3), "unit": "pixels/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tracks and LUT)",
+           "config": {"workload": f"beam search (fee_paths_scaling={int(params.fee_paths_scaling)}, H={H}, "
+                                  f"RESET_NOISE_CHARGE=900) on the {P} simulated pixels of {PROB_EVENTS} events of "
+                                  "the batched LUT workload (n_neighbors=4, L=150), expected tick / ADC / hit "
+                                  "probability fused", "pixels": P, "ticks": int(wfs.shape[1]),
+                      "l2": "flushed between timed steps (512 MiB write)"},
+           "e2e": {"value": P / e2e_s, "unit": "pixels/s", "ms_per_step": e2e_s * 1e3,
+                   "h2d_bytes_per_step": int(host.numel() * 4), "d2h_bytes_per_step": int(3 * P * H * 4)},
+           "roofline": {"bound": "issue", "kernel": "k_fee_prob",
+                        "note": "transcendental-function bound (erf/erfc, log, exp, expm1 per path and tick); "
+                                "HBM traffic is the waveform read only"},
+           "gpu_launches": 2 * args.steps, "clocks": clk}
+    if not args.no_cpu_baseline:
+        from oracle import reference_np as R
+        sample = wfs[:PROB_CPU_PIXELS].cpu().numpy()
+        t0 = time.perf_counter()
+        R.get_average_hit_values(*(lambda lp, q: (np.exp(lp), R.digitize(params, q)))(
+            *R.get_adc_values_average_noise(params, sample)))
+        dt = time.perf_counter() - t0
+        rec["cpu_baseline"] = {"value": PROB_CPU_PIXELS / dt, "unit": "pixels/s", "cores": 1, "kind": "port",
+                               "sample": f"first {PROB_CPU_PIXELS} pixels, float32 numpy restatement, {dt:.1f} s"}
+    print(json.dumps(rec), flush=True)
+
+
 def run_chop_reference(args):
     """CPU arm of --path chop: the numpy restatement of chop_tracks, one
     bounded sample (the first 20k tracks of the same event) per step."""
@@ -531,6 +611,13 @@ def run_chop_reference(args):
 
 def main():
     args = parse()
+    if args.path == "prob":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "prob path: its CPU arm is the cpu_baseline of "
+                                                                  "--path prob (the numpy restatement)"}))
+        else:
+            run_prob(args)
+        return
     if args.path == "chop":
         if args.impl == "reference":
             run_chop_reference(args)

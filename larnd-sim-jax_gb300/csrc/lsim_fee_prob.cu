@@ -8,10 +8,12 @@
 // maximum in shared memory; because max(x - c) = max(x) - c holds exactly
 // in floating point, the per-path running maxima of q - c are read from the
 // two shared arrays instead of being rescanned for each of the K paths.
-// For each of the H hit steps the block walks the K paths; per path it
-// tabulates log Phi of (q - c - thr)/sigma and of the running maximum over
-// all ticks, then every thread folds its 8 ticks into three online
-// log-sum-exp accumulators (hit, total, selection).  A block top-K over the
+// Ticks whose inputs are bit-identical to the previous tick's are grouped
+// into classes (one evaluation per class; flat stretches of a waveform
+// collapse).  For each of the H hit steps the block walks the K paths and
+// every thread folds its classes into three online log-sum-exp
+// accumulators (hit, total, selection), with no barrier between paths.  A
+// block top-K over the
 // selection values (largest first, lower tick first on ties, as lax.top_k)
 // gives the next K paths.  The reference stops the whole batch once no pixel
 // keeps a total path probability above stop_threshold; the step kernel
@@ -23,11 +25,13 @@
 namespace lsim {
 namespace {
 
-constexpr int kProbThreads = 256;
-constexpr int kProbTicks = 8;   // ticks per thread: up to 2048 ticks
+constexpr int kProbThreads = 512;
+constexpr int kProbTicks = 4;   // ticks per thread: up to 2048 ticks
 constexpr int kProbMaxT = kProbThreads * kProbTicks;
 constexpr int kProbMaxPaths = 32;
-constexpr int kProbArrays = 7;  // q, running max, suffix max, esperance, soft-where weight, log Phi(q), log Phi(max)
+constexpr int kProbArrays = 10;  // q, running max, suffix max, esperance, soft-where weight, 3 class values, class, representative
+// plus 6 partial sums per thread and the per-warp top-K candidates (value, index)
+constexpr int kProbExtraFloats = 6 * kProbThreads + 2 * (kProbThreads / 32) * kProbMaxPaths;
 constexpr float kProbFloor = -1000.0f;
 
 // ---------------------------------------------------------------- special functions
@@ -44,6 +48,8 @@ __device__ __forceinline__ float ndtr_f(float x) {
 }
 
 __device__ __forceinline__ float log_ndtr_f(float x) {
+  // above 15, erfc(x / sqrt 2) < 1e-50 is 0 in float32: -ndtr(-x) = -0
+  if (x > 15.0f) return -0.0f;
   if (x > 5.0f) return -ndtr_f(-x);
   if (x > -10.0f) return logf(ndtr_f(x));
   const float x2 = x * x;
@@ -64,34 +70,72 @@ __device__ __forceinline__ float softplus_f(float y) {
 
 __device__ __forceinline__ float sigmoid_f(float x) { return 1.0f / (1.0f + expf(-x)); }
 
-// log(Phi(a) - Phi(b)) with the reference's smooth clamps; la, lb = log_ndtr(a), log_ndtr(b)
-__device__ __forceinline__ float log_diff_ndtr_f(float a, float b, float la, float lb) {
-  const float safe = a > b ? lb - la : -1.0f;
+// The clamped log(1 - exp(safe)) term of log_diff_ndtr.
+__device__ __forceinline__ float ldn_log_term(float safe) {
   const float neg = -expm1f(safe);
   const float neg_safe = 1e-30f + softplus_f((neg - 1e-30f) * 1e10f) / 1e10f;
   // neg_safe >= 1e-30, so lt >= -69.1 and the clamp's softplus argument
   // (lt + 100) * 10 >= 309: softplus is the identity there
   const float lt = logf(neg_safe);
-  const float lts = -100.0f + ((lt + 100.0f) * 10.0f) / 10.0f;
+  return -100.0f + ((lt + 100.0f) * 10.0f) / 10.0f;
+}
+
+// log(Phi(a) - Phi(b)) with the reference's smooth clamps; la, lb =
+// log_ndtr(a), log_ndtr(b); term_m1 = ldn_log_term(-1), the value every
+// a <= b takes (safe = -1 there), so flat stretches (a == b, w = 1/2 exactly)
+// need no transcendental function at all.
+__device__ __forceinline__ float log_diff_ndtr_f(float a, float b, float la, float lb, float term_m1) {
+  if (a == b) return 0.5f * (la + term_m1) + 0.5f * kProbFloor;
+  const float lts = a > b ? ldn_log_term(lb - la) : term_m1;
   const float lp = la + lts;
   const float w = sigmoid_f((a - b) * 1000.0f);
   return w * lp + (1.0f - w) * kProbFloor;
 }
 
 // online log-sum-exp: m = running maximum, s = sum of exp(x - m)
+// (exp of arguments below -110 is 0 in float32 and is skipped)
 __device__ __forceinline__ void lse_add(float &m, float &s, float x) {
   if (x > m) {
-    s = s * expf(m - x) + 1.0f;
+    s = m - x > -110.0f ? s * expf(m - x) + 1.0f : 1.0f;
     m = x;
-  } else {
+  } else if (x - m > -110.0f) {
     s += expf(x - m);
   }
 }
 
 __device__ __forceinline__ float lse_final(float m, float s) { return logf(s) + m; }
 
+// merge a partial (m2, s2) into (m, s)
+__device__ __forceinline__ void lse_merge(float &m, float &s, float m2, float s2) {
+  if (!(s2 > 0.0f)) return;
+  if (!(s > 0.0f)) {
+    m = m2;
+    s = s2;
+    return;
+  }
+  if (m2 > m) {
+    s = (m - m2 > -110.0f ? s * expf(m - m2) : 0.0f) + s2;
+    m = m2;
+  } else if (m2 - m > -110.0f) {
+    s += s2 * expf(m2 - m);
+  }
+}
+
 __device__ __forceinline__ bool better(float va, int ia, float vb, int ib) {
   return va > vb || (va == vb && ia < ib);
+}
+
+// warp-wide best (value, index) under better(); every lane gets the result
+__device__ __forceinline__ void warp_best(float &bv, int &bi) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (better(ov, oi, bv, bi)) {
+      bv = ov;
+      bi = oi;
+    }
+  }
 }
 
 // ---------------------------------------------------------------- block scans over a pixel row
@@ -162,20 +206,31 @@ struct ProbArgs {
   int32_t *step_active;   // [H]: some pixel kept a total path probability above the stop level after step h
 };
 
-__global__ void __launch_bounds__(kProbThreads, 3) k_fee_prob(ProbArgs a) {
+// The per-tick work of a step reads, for tick t, only the running maximum
+// at t and t+1, q at t, t+1, s = shifted(t) and s+1, and the suffix maximum
+// at the selection window end.  Ticks whose 7 values are bit-identical to
+// those of the tick before give bit-identical results, so the block
+// evaluates one representative per run of equal ticks (a "class") and
+// expands the class values back to ticks; flat stretches of a waveform
+// (no charge arriving) collapse to a handful of classes.
+__global__ void __launch_bounds__(kProbThreads, 2) k_fee_prob(ProbArgs a) {
   extern __shared__ __align__(16) float sm[];
   float *qs = sm, *cm = qs + kProbMaxT, *cr = cm + kProbMaxT, *esp = cr + kProbMaxT, *sw = esp + kProbMaxT;
-  float *LQ = sw + kProbMaxT, *LM = LQ + kProbMaxT;
+  float *vh = sw + kProbMaxT, *vd = vh + kProbMaxT, *vs = vd + kProbMaxT;
+  int *cls = reinterpret_cast<int *>(vs + kProbMaxT), *rep = cls + kProbMaxT;
+  float *part = reinterpret_cast<float *>(rep + kProbMaxT);   // [kProbThreads][6] partial sums of path groups
+  float *cand_v = part + 6 * kProbThreads;                     // [warps][K] per-warp top-K candidates
+  int *cand_i = reinterpret_cast<int *>(cand_v + (kProbThreads / 32) * kProbMaxPaths);
   __shared__ float red[kProbThreads / 32];
-  __shared__ float red_v[kProbThreads / 32];
-  __shared__ int red_i[kProbThreads / 32];
   __shared__ float pc[kProbMaxPaths], plp[kProbMaxPaths], nc[kProbMaxPaths], nlp[kProbMaxPaths];
   __shared__ int pskip[kProbMaxPaths];
-  __shared__ int top_t;
+  __shared__ int n_cls;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 
   const LsimParams &p = a.p;
   const int T = a.T, K = a.K, H = p.max_adc_values, tid = threadIdx.x;
   const float z = a.z, thr = a.thr;
+  const float term_m1 = ldn_log_term(-1.0f);
   auto shifted = [&](int t) { return min(t + a.interval + 1, T - 1); };
 
   for (int64_t pix = blockIdx.x; pix < a.n_pix; pix += gridDim.x) {
@@ -187,25 +242,51 @@ __global__ void __launch_bounds__(kProbThreads, 3) k_fee_prob(ProbArgs a) {
     __syncthreads();
     block_scan_row<kScanMax>(cm, T, red);
     block_scan_row<kScanSuffixMax>(cr, T, red);
+    // esperance values, soft-where weights and the tick classes
     for (int t = tid; t < T - 1; t += kProbThreads) {
-      const float e = (qs[shifted(t)] + thr) - 0.5f * (qs[t + 1] + qs[t]);
+      const int s = shifted(t);
+      const float e = (qs[s] + thr) - 0.5f * (qs[t + 1] + qs[t]);
       esp[t] = e;
       sw[t] = sigmoid_f((e - thr) * 10.0f);
+      bool head = t == 0;
+      if (!head) {
+        const int sp = shifted(t - 1);
+        const int s1 = min(s + 1, T - 1), sp1 = min(sp + 1, T - 1);
+        const int fe = min(s + a.interval + 1, T - 1), fep = min(sp + a.interval + 1, T - 1);
+        auto ne = [](float x, float y) { return __float_as_uint(x) != __float_as_uint(y); };
+        head = ne(cm[t], cm[t - 1]) || ne(cm[t + 1], cm[t]) || ne(qs[t], qs[t - 1]) || ne(qs[t + 1], qs[t]) ||
+               ne(qs[s], qs[sp]) || ne(qs[s1], qs[sp1]) || ne(cr[fe], cr[fep]);
+      }
+      vh[t] = head ? 1.0f : 0.0f;
+    }
+    __syncthreads();
+    block_scan_row<kScanSum>(vh, T - 1, red);   // integer counts, exact in float32
+    for (int t = tid; t < T - 1; t += kProbThreads) {
+      const int u = (int)vh[t] - 1;
+      cls[t] = u;
+      if (t == 0 || (int)vh[t - 1] != u + 1) rep[u] = t;
+      if (t == T - 2) n_cls = u + 1;
     }
     if (tid < K) {
       pc[tid] = 0.0f;
       plp[tid] = tid == 0 ? 0.0f : kProbFloor;
     }
     __syncthreads();
+    const int U = n_cls;
+    // with few classes, G groups of threads share a class and split the paths
+    const int G = U <= kProbThreads / 2 ? min(8, kProbThreads / U) : 1;
+    const int grp = G > 1 ? tid / U : 0;
+    const int n_own = G > 1 ? (grp < G ? 1 : 0) : kProbTicks;
+    const int r0 = G > 1 ? tid - grp * U : tid;
 
     for (int h = 0; h < H; ++h) {
       // paths whose charge repeats that of a path more than 110 log units
       // likelier add exp(< -110) = 0 to every float32 log-sum-exp: skip them
       if (tid < K) {
-        int s = 0;
+        int sk = 0;
         for (int j = 0; j < K; ++j)
-          if (j != tid && pc[j] == pc[tid] && plp[j] > plp[tid] + 110.0f) s = 1;
-        pskip[tid] = s;
+          if (j != tid && pc[j] == pc[tid] && plp[j] > plp[tid] + 110.0f) sk = 1;
+        pskip[tid] = sk;
       }
       float hm[kProbTicks], hs[kProbTicks], dm[kProbTicks], ds[kProbTicks], sm_[kProbTicks], ss[kProbTicks];
 #pragma unroll
@@ -214,23 +295,23 @@ __global__ void __launch_bounds__(kProbThreads, 3) k_fee_prob(ProbArgs a) {
         hs[i] = ds[i] = ss[i] = 0.0f;
       }
       __syncthreads();
-      for (int k = 0; k < K; ++k) {
+      for (int k = grp; n_own > 0 && k < K; k += G) {
         if (pskip[k]) continue;
         const float c = pc[k], lp = plp[k];
-        for (int t = tid; t < T; t += kProbThreads) {
-          LQ[t] = log_ndtr_f(((qs[t] - c) - thr) * z);
-          LM[t] = log_ndtr_f(((cm[t] - c) - thr) * z);
-        }
-        __syncthreads();
 #pragma unroll
         for (int i = 0; i < kProbTicks; ++i) {
-          const int t = tid + i * kProbThreads;
-          if (t < T - 1) {
+          const int r = r0 + i * kProbThreads;
+          if (i < n_own && r < U) {
+            const int t = rep[r];
             const int s = shifted(t);
             const float zm0 = ((cm[t] - c) - thr) * z, zm1 = ((cm[t + 1] - c) - thr) * z;
-            const float lg = log_diff_ndtr_f(zm1, zm0, LM[t + 1], LM[t]);
+            const float LM0 = log_ndtr_f(zm0);
+            const float LM1 = zm1 == zm0 ? LM0 : log_ndtr_f(zm1);
+            const float lg = log_diff_ndtr_f(zm1, zm0, LM1, LM0, term_m1);
             const float zq0 = ((qs[t] - c) - thr) * z, zqs = ((qs[s] - c) - thr) * z;
-            float le = log_diff_ndtr_f(zqs, zq0, LQ[s], LQ[t]);
+            const float LQ0 = log_ndtr_f(zq0);
+            const float LQs = zqs == zq0 ? LQ0 : log_ndtr_f(zqs);
+            float le = log_diff_ndtr_f(zqs, zq0, LQs, LQ0, term_m1);
             le = fminf(le, lg);
             le = kProbFloor + softplus_f(le - kProbFloor);
             le = sw[t] * le + (1.0f - sw[t]) * kProbFloor;
@@ -241,18 +322,45 @@ __global__ void __launch_bounds__(kProbThreads, 3) k_fee_prob(ProbArgs a) {
             lse_add(sm_[i], ss[i], (lg + log_ndtr_f(x)) + lp);
           }
         }
-        __syncthreads();
       }
+      if (G > 1) {
+        // merge the path groups' partial log-sum-exps into group 0
+        if (grp > 0 && grp < G) {
+          float *q = part + 6 * tid;
+          q[0] = hm[0], q[1] = hs[0], q[2] = dm[0], q[3] = ds[0], q[4] = sm_[0], q[5] = ss[0];
+        }
+        __syncthreads();
+        if (grp == 0) {
+          for (int g2 = 1; g2 < G; ++g2) {
+            const float *q = part + 6 * (g2 * U + tid);
+            lse_merge(hm[0], hs[0], q[0], q[1]);
+            lse_merge(dm[0], ds[0], q[2], q[3]);
+            lse_merge(sm_[0], ss[0], q[4], q[5]);
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kProbTicks; ++i) {
+        const int r = r0 + i * kProbThreads;
+        if (i < n_own && grp == 0 && r < U) {
+          vh[r] = lse_final(hm[i], hs[i]);
+          vd[r] = lse_final(dm[i], ds[i]);
+          vs[r] = lse_final(sm_[i], ss[i]);
+        }
+      }
+      __syncthreads();
       // step outputs and the per-hit reductions
       float l_sum = 0.0f, t_sum = 0.0f, a_sum = 0.0f;
+      float selv[kProbTicks];
       const int64_t row = (pix * H + h) * (int64_t)(T - 1);
 #pragma unroll
       for (int i = 0; i < kProbTicks; ++i) {
         const int t = tid + i * kProbThreads;
+        selv[i] = -INFINITY;
         if (t < T - 1) {
-          const float hit = lse_final(hm[i], hs[i]);
-          dm[i] = lse_final(dm[i], ds[i]);
-          sm_[i] = lse_final(sm_[i], ss[i]);
+          const int u = cls[t];
+          const float hit = vh[u];
+          selv[i] = vs[u];
           if (a.log_prob) a.log_prob[row + t] = hit;
           if (a.charge) a.charge[row + t] = esp[t];
           const float pr = expf(hit);
@@ -272,71 +380,77 @@ __global__ void __launch_bounds__(kProbThreads, 3) k_fee_prob(ProbArgs a) {
           a.e_adc[pix * H + h] = As / den;
         }
       }
-      // top-K ticks by selection value -> next paths
-      unsigned taken = 0;
-      for (int r = 0; r < K; ++r) {
-        float bv = -INFINITY;
-        int bi = 0x7fffffff;
+      // top-K ticks by selection value -> next paths: each warp keeps the K
+      // best of its ticks (largest first, lower tick first on ties), then
+      // warp 0 takes the K best of those candidates
+      {
+        unsigned taken = 0;
+        for (int r = 0; r < K; ++r) {
+          float bv = -INFINITY;
+          int bi = 0x7fffffff;
 #pragma unroll
-        for (int i = 0; i < kProbTicks; ++i) {
-          const int t = tid + i * kProbThreads;
-          if (t < T - 1 && !(taken >> i & 1u) && better(sm_[i], t, bv, bi)) {
-            bv = sm_[i];
-            bi = t;
-          }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-          if (better(ov, oi, bv, bi)) {
-            bv = ov;
-            bi = oi;
-          }
-        }
-        if ((tid & 31) == 0) {
-          red_v[tid >> 5] = bv;
-          red_i[tid >> 5] = bi;
-        }
-        __syncthreads();
-        if (tid == 0) {
-          float v = red_v[0];
-          int ix = red_i[0];
-          for (int w2 = 1; w2 < kProbThreads / 32; ++w2)
-            if (better(red_v[w2], red_i[w2], v, ix)) {
-              v = red_v[w2];
-              ix = red_i[w2];
+          for (int i = 0; i < kProbTicks; ++i) {
+            const int t = tid + i * kProbThreads;
+            if (t < T - 1 && !(taken >> i & 1u) && better(selv[i], t, bv, bi)) {
+              bv = selv[i];
+              bi = t;
             }
-          top_t = ix;
+          }
+          warp_best(bv, bi);
+          if (bi != 0x7fffffff && (bi % kProbThreads) == tid) taken |= 1u << (bi / kProbThreads);
+          if (lane == 0) {
+            cand_v[wid * kProbMaxPaths + r] = bv;
+            cand_i[wid * kProbMaxPaths + r] = bi;
+          }
         }
-        __syncthreads();
-        const int tt = top_t;
-        if (tt >= 0 && tt < T - 1 && (tt % kProbThreads) == tid) {
-          const int ii = tt / kProbThreads;
-          float d = 0.0f;
-#pragma unroll
-          for (int i = 0; i < kProbTicks; ++i)
-            if (i == ii) d = dm[i];
-          taken |= 1u << ii;
-          nlp[r] = d;
-          nc[r] = qs[min(shifted(tt) + 1, T - 1)];
-        }
-        __syncthreads();
       }
+      __syncthreads();
+      if (wid == 0) {
+        constexpr int kCand = (kProbThreads / 32) * kProbMaxPaths / 32;   // candidates per lane
+        float cv[kCand];
+        int ci[kCand];
+#pragma unroll
+        for (int j = 0; j < kCand; ++j) {
+          const int e = lane + 32 * j, w2 = e / kProbMaxPaths, r2 = e % kProbMaxPaths;
+          cv[j] = r2 < K ? cand_v[w2 * kProbMaxPaths + r2] : -INFINITY;
+          ci[j] = r2 < K ? cand_i[w2 * kProbMaxPaths + r2] : 0x7fffffff;
+        }
+        unsigned taken = 0;
+        for (int r = 0; r < K; ++r) {
+          float bv = -INFINITY;
+          int bi = 0x7fffffff, bj = -1;
+#pragma unroll
+          for (int j = 0; j < kCand; ++j)
+            if (!(taken >> j & 1u) && better(cv[j], ci[j], bv, bi)) {
+              bv = cv[j];
+              bi = ci[j];
+              bj = j;
+            }
+          const int mine = bi;
+          warp_best(bv, bi);
+          if (bj >= 0 && mine == bi) taken |= 1u << bj;
+          if (lane == r) {
+            const int tt = bi >= 0 && bi < T - 1 ? bi : T - 2;
+            nlp[r] = vd[cls[tt]];
+            nc[r] = qs[min(shifted(tt) + 1, T - 1)];
+          }
+        }
+      }
+      __syncthreads();
       if (tid < 32) {
         const float v = tid < K ? nlp[tid] : -INFINITY;
         float m = v;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
         const float mm = isfinite(m) ? m : 0.0f;
-        float s = tid < K ? expf(v - mm) : 0.0f;
+        float sum = tid < K ? expf(v - mm) : 0.0f;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
         if (tid < K) {
           pc[tid] = nc[tid];
           plp[tid] = nlp[tid];
         }
-        if (tid == 0 && logf(s) + mm > a.log_stop && !*(volatile int32_t *)(a.step_active + h))
+        if (tid == 0 && logf(sum) + mm > a.log_stop && !*(volatile int32_t *)(a.step_active + h))
           atomicOr(a.step_active + h, 1);
       }
       __syncthreads();
@@ -403,7 +517,7 @@ int run_fee_prob(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n
   a.step_active = static_cast<int32_t *>(ws);
   if (cudaMemsetAsync(a.step_active, 0, sizeof(int32_t) * p.max_adc_values, st) != cudaSuccess) return LSIM_ERR_CUDA;
   if (n_pix == 0) return LSIM_OK;
-  const size_t smem = sizeof(float) * kProbArrays * kProbMaxT;
+  const size_t smem = sizeof(float) * (kProbArrays * kProbMaxT + kProbExtraFloats);
   if (cudaFuncSetAttribute(k_fee_prob, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return LSIM_ERR_CUDA;
   int per_sm = 0;
