@@ -323,6 +323,26 @@ int lsim_fee_prob(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t 
                   float stop_threshold, float *log_prob_out, float *charge_out, float *exp_tick_out,
                   float *exp_adc_out, float *lambda_out, void *ws, size_t ws_bytes, void *stream);
 
+/* ---------------------------------------------------------------- fit losses */
+
+/* Workspace bytes of lsim_mse_adc for n_hits predicted and n_ref reference hits. */
+size_t lsim_mse_adc_workspace_bytes(int64_t n_hits, int64_t n_ref);
+
+/* The hit-level loss mse_adc, src/larndsim/losses_jax.py:60-79 (with
+ * rbf_kernel and mmd, :13-39): the weighted maximum mean discrepancy with a
+ * Gaussian kernel of width sigma between the predicted hits (x, y, z,
+ * event, weight w = Q * hit_prob) and the reference hits, on the stacked
+ * coordinates (x + event * 1e5, y, z), plus lambda_q times the squared
+ * relative difference of the total weights.  out[0..2] = loss, MMD term,
+ * charge term (device floats).  grad_w and grad_z (optional, [n_hits]) get
+ * dL/dw and dL/dz of the predicted hits; x, y and the events carry no
+ * gradient.  Hits of different events never interact (their kernel value
+ * is 0 in float32); inputs ordered by event run fastest. */
+int lsim_mse_adc(const float *x, const float *y, const float *z, const int32_t *event, const float *w, int64_t n_hits,
+                 const float *ref_x, const float *ref_y, const float *ref_z, const int32_t *ref_event,
+                 const float *ref_w, int64_t n_ref, float sigma, float lambda_q, float *out, float *grad_w,
+                 float *grad_z, void *ws, size_t ws_bytes, void *stream);
+
 /* ---------------------------------------------------------------- parametrised mode */
 
 /* Stage 1 of simulate_parametrized: shift, quench, drift, Monte-Carlo

@@ -344,6 +344,28 @@ int lsim_fee_prob(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t 
               "lsim_fee_prob");
 }
 
+size_t lsim_mse_adc_workspace_bytes(int64_t n_hits, int64_t n_ref) {
+  return n_hits < 0 || n_ref < 0 ? 0 : mse_adc_workspace_bytes(n_hits, n_ref);
+}
+
+int lsim_mse_adc(const float *x, const float *y, const float *z, const int32_t *event, const float *w, int64_t n_hits,
+                 const float *ref_x, const float *ref_y, const float *ref_z, const int32_t *ref_event,
+                 const float *ref_w, int64_t n_ref, float sigma, float lambda_q, float *out, float *grad_w,
+                 float *grad_z, void *ws, size_t ws_bytes, void *stream) {
+  g_err.clear();
+  if (n_hits < 0 || n_ref < 0 || !out) return fail(LSIM_ERR_INVALID, "lsim_mse_adc: bad arguments");
+  if (n_hits > 0 && (!x || !y || !z || !event || !w)) return fail(LSIM_ERR_INVALID, "lsim_mse_adc: null hit array");
+  if (n_ref > 0 && (!ref_x || !ref_y || !ref_z || !ref_event || !ref_w))
+    return fail(LSIM_ERR_INVALID, "lsim_mse_adc: null reference array");
+  if (!(sigma > 0.0f)) return fail(LSIM_ERR_INVALID, "lsim_mse_adc: sigma %g", sigma);
+  if (!ws || ws_bytes < mse_adc_workspace_bytes(n_hits, n_ref))
+    return fail(LSIM_ERR_CAPACITY, "lsim_mse_adc: workspace %zu < %zu bytes", ws_bytes,
+                mse_adc_workspace_bytes(n_hits, n_ref));
+  return wrap(run_mse_adc(x, y, z, event, w, n_hits, ref_x, ref_y, ref_z, ref_event, ref_w, n_ref, sigma, lambda_q,
+                          out, grad_w, grad_z, ws, (cudaStream_t)stream),
+              "lsim_mse_adc");
+}
+
 size_t lsim_chop_workspace_bytes(int64_t n_rows) { return n_rows < 0 ? 0 : chop_workspace_bytes(n_rows); }
 
 int lsim_chop_tracks(const LsimFieldMap *f, const float *tracks, int64_t n_rows, double precision, float *out,

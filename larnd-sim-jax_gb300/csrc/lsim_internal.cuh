@@ -66,6 +66,12 @@ int run_fee_prob(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n
                  float stop_threshold, float *log_prob, float *charge, float *e_tick, float *e_adc, float *lam,
                  void *ws, cudaStream_t st);
 
+// lsim_losses.cu
+size_t mse_adc_workspace_bytes(int64_t n, int64_t m);
+int run_mse_adc(const float *x, const float *y, const float *z, const int32_t *event, const float *w, int64_t n,
+                const float *rx, const float *ry, const float *rz, const int32_t *revent, const float *rw, int64_t m,
+                float sigma, float lambda_q, float *out, float *grad_w, float *grad_z, void *ws, cudaStream_t st);
+
 // lsim_chop.cu
 size_t chop_workspace_bytes(int64_t n_rows);
 int run_chop(const LsimFieldMap &f, const float *tracks, int64_t n_rows, double precision, float *out,

@@ -96,6 +96,9 @@ _SIGNATURES = {
     "lsim_pixel_coords": (C.c_int, [_PP, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
     "lsim_fee_prob_workspace_bytes": (_sz, [_PP]),
     "lsim_fee_prob": (C.c_int, [_PP, _vp, _i64, _i32, _i32, C.c_float, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "lsim_mse_adc_workspace_bytes": (_sz, [_i64, _i64]),
+    "lsim_mse_adc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, C.c_float, C.c_float,
+                               _vp, _vp, _vp, _vp, _sz, _vp]),
     "lsim_chop_workspace_bytes": (_sz, [_i64]),
     "lsim_chop_tracks": (C.c_int, [_PF, _vp, _i64, C.c_double, _vp, _i64, _vp, _vp, _sz, _vp]),
     "lsim_param_stage1": (C.c_int, [_PP, _PF, _vp, _i64, _i32, _vp, _vp, _sz, _vp, _vp]),

@@ -202,3 +202,52 @@ def adc_fn(theta: torch.Tensor, chain: LUTChain, params, normals=None):
     """Differentiable (ADC, ticks, pixel ids) of the LUT chain as a function
     of ``theta`` = the 8 parameter values (order ``GRAD_PARAMS``)."""
     return _AdcFn.apply(theta, chain, params, normals)
+
+
+def _hit_z(params, theta, ticks, plane):
+    """get_hit_z (detsim_jax.py:309-319) with the drift velocity of theta's
+    eField: z_anode + tick * t_sampling * v * sign(z_high - z_anode); the
+    value uses get_vdrift in float64 rounded to float32, the derivative
+    d v / d eField (the reference differentiates get_vdrift)."""
+    from .consts import get_vdrift, get_vdrift_derivative
+    e = theta[GRAD_PARAMS.index("eField")]
+    pe = params.replace(eField=float(e.detach()))
+    v = torch.tensor(np.float32(get_vdrift(pe)), dtype=torch.float32, device=ticks.device)
+    v = v + (e - e.detach()).to(torch.float32) * float(get_vdrift_derivative(pe))
+    b = torch.as_tensor(np.asarray(params.tpc_borders, np.float32), device=ticks.device)[plane.long()]
+    za, zh = b[:, 2, 0], b[:, 2, 1]
+    return za + ticks * (np.float32(params.t_sampling) * v) * torch.sign(zh - za)
+
+
+def predicted_hits(theta, chain, params, normals=None):
+    """The accepted hits of the LUT chain at theta (simulate_stochastic's
+    compaction, sim_jax.py:757-769 and :619-647), differentiable in theta:
+    (Q, x, y, z, ticks, hit_prob, event)."""
+    from . import losses
+    from .consts import n_ticks
+    adc, ticks, pids = adc_fn(theta, chain, params, normals)
+    T = n_ticks(params) - 1
+    keep = (ticks < T - 3).reshape(-1)
+    H = adc.shape[1]
+    x, y, plane, event = sim.pixel_coordinates(params, pids)
+    rep = lambda t: t.repeat_interleave(H)[keep]   # noqa: E731
+    t_k = ticks.reshape(-1)[keep]
+    z = _hit_z(params, theta, t_k, rep(plane))
+    Q = losses.adc2charge(adc.reshape(-1)[keep], params)
+    return Q, rep(x), rep(y), z, t_k, torch.ones_like(t_k), rep(event)
+
+
+def params_loss(params, chain, ref, loss_fn=None, theta=None, normals=None, **loss_kwargs):
+    """params_loss (losses_jax.py:385-398) for the LUT chain with a hit-level
+    loss: simulate at ``theta`` (default: params' values), build the hits,
+    and evaluate ``loss_fn`` (default mse_adc) against ``ref`` = (ref_Q,
+    ref_x, ref_y, ref_z, ref_ticks, ref_hit_prob, ref_event).  Returns
+    (loss, aux, theta); ``loss.backward()`` fills theta.grad through the
+    loss kernel, the hit z and the LUT adjoint."""
+    from . import losses
+    loss_fn = losses.mse_adc if loss_fn is None else loss_fn
+    if theta is None:
+        theta = theta_of(params, device=chain.tracks.device).requires_grad_(True)
+    Q, x, y, z, t, hp, ev = predicted_hits(theta, chain, params, normals)
+    loss, aux = loss_fn(params, Q, x, y, z, t, hp, ev, *ref, **loss_kwargs)
+    return loss, aux, theta
