@@ -343,6 +343,36 @@ int lsim_mse_adc(const float *x, const float *y, const float *z, const int32_t *
                  const float *ref_w, int64_t n_ref, float sigma, float lambda_q, float *out, float *grad_w,
                  float *grad_z, void *ws, size_t ws_bytes, void *stream);
 
+/* Workspace bytes of lsim_nll_loss / lsim_chamfer_3d. */
+size_t lsim_nll_workspace_bytes(int64_t n_hits, int64_t n_ref);
+size_t lsim_chamfer_workspace_bytes(int64_t n_hits, int64_t n_ref);
+
+/* nll_loss, src/larndsim/losses_jax.py:329-359: the Poisson-process
+ * negative log-likelihood sum(hit_prob) - sum_j [ref_hit_prob_j > 0.5]
+ * log(lambda_j + 1e-10), lambda_j = sum_i hit_prob_i exp(-|p_i - r_j|^2 /
+ * (2 sigma^2)) on the 4-d points (x + event * 1e9, y, z, q) with
+ * q = Q / adc_norm given by the caller.  out[0..2] = loss, sum(hit_prob),
+ * the log-likelihood sum; optional gradients [n_hits] with respect to q, z
+ * and hit_prob.  (The reference's padding rows at -1e9 with zero
+ * probabilities add nothing and are not needed.) */
+int lsim_nll_loss(const float *x, const float *y, const float *z, const float *q, const int32_t *event,
+                  const float *hit_prob, int64_t n_hits, const float *ref_x, const float *ref_y, const float *ref_z,
+                  const float *ref_q, const int32_t *ref_event, const float *ref_hit_prob, int64_t n_ref, float sigma,
+                  float *out, float *grad_q, float *grad_z, float *grad_hit_prob, void *ws, size_t ws_bytes,
+                  void *stream);
+
+/* chamfer_distance_3d_og as chamfer_3d calls it, src/larndsim/losses_jax.py:
+ * 181-229: nearest neighbours both ways on (x + event * 1e9, y, z) in
+ * float32 (first index on ties); loss = sum over hits closer than 1e4 of
+ * min distance x own weight x neighbour weight.  The caller passes the
+ * weights Q / adc_norm and the padded rows (zeros, event 0) the reference
+ * appends.  out[0] = loss; optional gradients [n_hits] with respect to w
+ * and z (the neighbour choices carry none).  At most 2^31 - 1 hits a side. */
+int lsim_chamfer_3d(const float *x, const float *y, const float *z, const int32_t *event, const float *w,
+                    int64_t n_hits, const float *ref_x, const float *ref_y, const float *ref_z,
+                    const int32_t *ref_event, const float *ref_w, int64_t n_ref, float *out, float *grad_w,
+                    float *grad_z, void *ws, size_t ws_bytes, void *stream);
+
 /* ---------------------------------------------------------------- parametrised mode */
 
 /* Stage 1 of simulate_parametrized: shift, quench, drift, Monte-Carlo

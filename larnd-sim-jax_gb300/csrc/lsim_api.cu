@@ -366,6 +366,52 @@ int lsim_mse_adc(const float *x, const float *y, const float *z, const int32_t *
               "lsim_mse_adc");
 }
 
+size_t lsim_nll_workspace_bytes(int64_t n_hits, int64_t n_ref) {
+  return n_hits < 0 || n_ref < 0 ? 0 : nll_workspace_bytes(n_hits, n_ref);
+}
+
+int lsim_nll_loss(const float *x, const float *y, const float *z, const float *q, const int32_t *event,
+                  const float *hit_prob, int64_t n_hits, const float *ref_x, const float *ref_y, const float *ref_z,
+                  const float *ref_q, const int32_t *ref_event, const float *ref_hit_prob, int64_t n_ref, float sigma,
+                  float *out, float *grad_q, float *grad_z, float *grad_hit_prob, void *ws, size_t ws_bytes,
+                  void *stream) {
+  g_err.clear();
+  if (n_hits < 0 || n_ref < 0 || !out) return fail(LSIM_ERR_INVALID, "lsim_nll_loss: bad arguments");
+  if (n_hits > 0 && (!x || !y || !z || !q || !event || !hit_prob))
+    return fail(LSIM_ERR_INVALID, "lsim_nll_loss: null hit array");
+  if (n_ref > 0 && (!ref_x || !ref_y || !ref_z || !ref_q || !ref_event || !ref_hit_prob))
+    return fail(LSIM_ERR_INVALID, "lsim_nll_loss: null reference array");
+  if (!(sigma > 0.0f)) return fail(LSIM_ERR_INVALID, "lsim_nll_loss: sigma %g", sigma);
+  if (!ws || ws_bytes < nll_workspace_bytes(n_hits, n_ref))
+    return fail(LSIM_ERR_CAPACITY, "lsim_nll_loss: workspace %zu < %zu bytes", ws_bytes,
+                nll_workspace_bytes(n_hits, n_ref));
+  return wrap(run_nll(x, y, z, q, event, hit_prob, n_hits, ref_x, ref_y, ref_z, ref_q, ref_event, ref_hit_prob, n_ref,
+                      sigma, out, grad_q, grad_z, grad_hit_prob, ws, (cudaStream_t)stream),
+              "lsim_nll_loss");
+}
+
+size_t lsim_chamfer_workspace_bytes(int64_t n_hits, int64_t n_ref) {
+  return n_hits < 0 || n_ref < 0 ? 0 : chamfer_workspace_bytes(n_hits, n_ref);
+}
+
+int lsim_chamfer_3d(const float *x, const float *y, const float *z, const int32_t *event, const float *w,
+                    int64_t n_hits, const float *ref_x, const float *ref_y, const float *ref_z,
+                    const int32_t *ref_event, const float *ref_w, int64_t n_ref, float *out, float *grad_w,
+                    float *grad_z, void *ws, size_t ws_bytes, void *stream) {
+  g_err.clear();
+  if (n_hits < 0 || n_ref < 0 || !out || n_hits > INT32_MAX || n_ref > INT32_MAX)
+    return fail(LSIM_ERR_INVALID, "lsim_chamfer_3d: bad arguments");
+  if (n_hits > 0 && (!x || !y || !z || !event || !w)) return fail(LSIM_ERR_INVALID, "lsim_chamfer_3d: null hit array");
+  if (n_ref > 0 && (!ref_x || !ref_y || !ref_z || !ref_event || !ref_w))
+    return fail(LSIM_ERR_INVALID, "lsim_chamfer_3d: null reference array");
+  if (!ws || ws_bytes < chamfer_workspace_bytes(n_hits, n_ref))
+    return fail(LSIM_ERR_CAPACITY, "lsim_chamfer_3d: workspace %zu < %zu bytes", ws_bytes,
+                chamfer_workspace_bytes(n_hits, n_ref));
+  return wrap(run_chamfer(x, y, z, event, w, n_hits, ref_x, ref_y, ref_z, ref_event, ref_w, n_ref, out, grad_w,
+                          grad_z, ws, (cudaStream_t)stream),
+              "lsim_chamfer_3d");
+}
+
 size_t lsim_chop_workspace_bytes(int64_t n_rows) { return n_rows < 0 ? 0 : chop_workspace_bytes(n_rows); }
 
 int lsim_chop_tracks(const LsimFieldMap *f, const float *tracks, int64_t n_rows, double precision, float *out,

@@ -72,6 +72,16 @@ int run_mse_adc(const float *x, const float *y, const float *z, const int32_t *e
                 const float *rx, const float *ry, const float *rz, const int32_t *revent, const float *rw, int64_t m,
                 float sigma, float lambda_q, float *out, float *grad_w, float *grad_z, void *ws, cudaStream_t st);
 
+size_t nll_workspace_bytes(int64_t n, int64_t m);
+int run_nll(const float *x, const float *y, const float *z, const float *q, const int32_t *event, const float *hp,
+            int64_t n, const float *rx, const float *ry, const float *rz, const float *rq, const int32_t *revent,
+            const float *rhp, int64_t m, float sigma, float *out, float *g_q, float *g_z, float *g_hp, void *ws,
+            cudaStream_t st);
+size_t chamfer_workspace_bytes(int64_t n, int64_t m);
+int run_chamfer(const float *x, const float *y, const float *z, const int32_t *event, const float *w, int64_t n,
+                const float *rx, const float *ry, const float *rz, const int32_t *revent, const float *rw, int64_t m,
+                float *out, float *g_w, float *g_z, void *ws, cudaStream_t st);
+
 // lsim_chop.cu
 size_t chop_workspace_bytes(int64_t n_rows);
 int run_chop(const LsimFieldMap &f, const float *tracks, int64_t n_rows, double precision, float *out,

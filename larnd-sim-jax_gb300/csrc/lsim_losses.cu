@@ -198,6 +198,277 @@ __global__ void k_mse_adc_grad(HitSet pred, const float *__restrict__ a, const f
   }
 }
 
+// ---------------------------------------------------------------- nll_loss and chamfer_3d
+// Both stack (x + event * 1e9, y, z[, Q / adc_norm]) (losses_jax.py:221-222,
+// :337-338); hits of different events are 1e9 apart and never interact.
+
+struct HitSet4 {
+  const float *x, *y, *z, *q, *w;   // q: 4th coordinate (nll) or null
+  const int32_t *event;
+  int64_t n;
+};
+
+__device__ __forceinline__ float stacked_x9(const HitSet4 &h, int64_t i) {
+  return __fadd_rn(h.x[i], __fmul_rn((float)h.event[i], 1e9f));
+}
+
+// block-wide event range of the row tile into (lo, hi)
+__device__ __forceinline__ void tile_event_range(bool ok, int ev, int *lo_s, int *hi_s, int &lo, int &hi) {
+  int a = ok ? ev : 0x7fffffff, b = ok ? ev : -0x7fffffff - 1;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a = min(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  if (threadIdx.x == 0) {
+    *lo_s = 0x7fffffff;
+    *hi_s = -0x7fffffff - 1;
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(lo_s, a);
+    atomicMax(hi_s, b);
+  }
+  __syncthreads();
+  lo = *lo_s;
+  hi = *hi_s;
+}
+
+// nll_loss sums: s[i] = sum_j w_j K_ij, sz[i] = sum_j w_j K_ij (z_i - z_j),
+// sq[i] = sum_j w_j K_ij (q_i - q_j), K = exp(-|4-d difference|^2 / (2 sigma^2))
+__global__ void __launch_bounds__(kRbfRows) k_gauss4_rows(HitSet4 rows, HitSet4 cols,
+                                                          const int2 *__restrict__ col_ranges, float two_sigma2,
+                                                          float *__restrict__ s, float *__restrict__ sz,
+                                                          float *__restrict__ sq) {
+  __shared__ float cx[kRbfChunk], cy[kRbfChunk], cz[kRbfChunk], cq[kRbfChunk], cw[kRbfChunk];
+  __shared__ int lo_s, hi_s;
+  const int64_t i = (int64_t)blockIdx.x * kRbfRows + threadIdx.x;
+  const bool ok = i < rows.n;
+  float xi = 0.f, yi = 0.f, zi = 0.f, qi = 0.f;
+  int ev = 0;
+  if (ok) {
+    xi = stacked_x9(rows, i);
+    yi = rows.y[i];
+    zi = rows.z[i];
+    qi = rows.q[i];
+    ev = rows.event[i];
+  }
+  int lo, hi;
+  tile_event_range(ok, ev, &lo_s, &hi_s, lo, hi);
+  float acc = 0.f, accz = 0.f, accq = 0.f;
+  const int64_t n_chunks = (cols.n + kRbfChunk - 1) / kRbfChunk;
+  for (int64_t c = 0; c < n_chunks; ++c) {
+    const int2 r = col_ranges[c];
+    if (r.y < lo || r.x > hi) continue;
+    const int64_t j0 = c * kRbfChunk;
+    const int cnt = cols.n - j0 < kRbfChunk ? (int)(cols.n - j0) : kRbfChunk;
+    __syncthreads();
+    for (int k = threadIdx.x; k < cnt; k += kRbfRows) {
+      cx[k] = stacked_x9(cols, j0 + k);
+      cy[k] = cols.y[j0 + k];
+      cz[k] = cols.z[j0 + k];
+      cq[k] = cols.q[j0 + k];
+      cw[k] = cols.w[j0 + k];
+    }
+    __syncthreads();
+    if (ok) {
+      for (int k = 0; k < cnt; ++k) {
+        const float dx = __fsub_rn(xi, cx[k]), dy = __fsub_rn(yi, cy[k]), dz = __fsub_rn(zi, cz[k]);
+        const float dq = __fsub_rn(qi, cq[k]);
+        const float d = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)),
+                                  __fmul_rn(dq, dq));
+        const float kv = expf(__fdiv_rn(-d, two_sigma2)) * cw[k];
+        acc += kv;
+        accz = fmaf(kv, dz, accz);
+        accq = fmaf(kv, dq, accq);
+      }
+    }
+  }
+  if (ok) {
+    s[i] = acc;
+    if (sz) sz[i] = accz;
+    if (sq) sq[i] = accq;
+  }
+}
+
+// column weights of the second nll pass: (ref_hit_prob > 0.5) / (lambda + 1e-10)
+__global__ void k_nll_colw(const float *__restrict__ ref_hp, const float *__restrict__ lam, int64_t m,
+                           float *__restrict__ c) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < m) c[j] = ref_hp[j] > 0.5f ? 1.0f / (lam[j] + 1e-10f) : 0.0f;
+}
+
+__global__ void k_nll_reduce(const float *__restrict__ hp, int64_t n, const float *__restrict__ ref_hp,
+                             const float *__restrict__ lam, int64_t m, float *out) {
+  __shared__ double red[2][32];
+  double t2 = 0, t1 = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) t2 += hp[i];
+  for (int64_t j = threadIdx.x; j < m; j += blockDim.x)
+    if (ref_hp[j] > 0.5f) t1 += (double)logf(lam[j] + 1e-10f);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+    t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = t2;
+    red[1][threadIdx.x >> 5] = t1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      a += red[0][k];
+      b += red[1][k];
+    }
+    out[0] = (float)(a - b);
+    out[1] = (float)a;
+    out[2] = (float)b;
+  }
+}
+
+__global__ void k_nll_grad(const float *__restrict__ hp, int64_t n, const float *__restrict__ s,
+                           const float *__restrict__ sz, const float *__restrict__ sq, float inv_sigma2,
+                           float *__restrict__ g_hp, float *__restrict__ g_z, float *__restrict__ g_q) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (g_hp) g_hp[i] = 1.0f - s[i];
+  if (g_z) g_z[i] = hp[i] * inv_sigma2 * sz[i];
+  if (g_q) g_q[i] = hp[i] * inv_sigma2 * sq[i];
+}
+
+// chamfer: nearest column of every row (first index on ties) and its
+// squared distance; rows with no column in their events get (inf, -1)
+__global__ void __launch_bounds__(kRbfRows) k_nn_rows(HitSet4 rows, HitSet4 cols, const int2 *__restrict__ col_ranges,
+                                                      float *__restrict__ dmin, int32_t *__restrict__ amin) {
+  __shared__ float cx[kRbfChunk], cy[kRbfChunk], cz[kRbfChunk];
+  __shared__ int lo_s, hi_s;
+  const int64_t i = (int64_t)blockIdx.x * kRbfRows + threadIdx.x;
+  const bool ok = i < rows.n;
+  float xi = 0.f, yi = 0.f, zi = 0.f;
+  int ev = 0;
+  if (ok) {
+    xi = stacked_x9(rows, i);
+    yi = rows.y[i];
+    zi = rows.z[i];
+    ev = rows.event[i];
+  }
+  int lo, hi;
+  tile_event_range(ok, ev, &lo_s, &hi_s, lo, hi);
+  float best = INFINITY;
+  int64_t arg = -1;
+  const int64_t n_chunks = (cols.n + kRbfChunk - 1) / kRbfChunk;
+  for (int64_t c = 0; c < n_chunks; ++c) {
+    const int2 r = col_ranges[c];
+    if (r.y < lo || r.x > hi) continue;   // 1e9 apart: never the nearest when the row's event has columns
+    const int64_t j0 = c * kRbfChunk;
+    const int cnt = cols.n - j0 < kRbfChunk ? (int)(cols.n - j0) : kRbfChunk;
+    __syncthreads();
+    for (int k = threadIdx.x; k < cnt; k += kRbfRows) {
+      cx[k] = stacked_x9(cols, j0 + k);
+      cy[k] = cols.y[j0 + k];
+      cz[k] = cols.z[j0 + k];
+    }
+    __syncthreads();
+    if (ok) {
+      for (int k = 0; k < cnt; ++k) {
+        const float dx = __fsub_rn(xi, cx[k]), dy = __fsub_rn(yi, cy[k]), dz = __fsub_rn(zi, cz[k]);
+        const float d = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+        if (d < best) {
+          best = d;
+          arg = j0 + k;
+        }
+      }
+    }
+  }
+  if (ok) {
+    dmin[i] = best;
+    amin[i] = (int32_t)arg;
+  }
+}
+
+// chamfer gradient gathers for predicted row i over the reference hits j
+// whose nearest predicted hit is i: sum of mb_j wb_j and of wb_j 2 (z_i - z_j)
+__global__ void __launch_bounds__(kRbfRows) k_chamfer_back(HitSet4 rows, HitSet4 cols,
+                                                           const int2 *__restrict__ col_ranges,
+                                                           const float *__restrict__ col_dmin,
+                                                           const int32_t *__restrict__ col_amin,
+                                                           float *__restrict__ acc_w, float *__restrict__ acc_z) {
+  __shared__ float cz[kRbfChunk], cw[kRbfChunk], cd[kRbfChunk];
+  __shared__ int ca[kRbfChunk];
+  __shared__ int lo_s, hi_s;
+  const int64_t i = (int64_t)blockIdx.x * kRbfRows + threadIdx.x;
+  const bool ok = i < rows.n;
+  const int ev = ok ? rows.event[i] : 0;
+  const float zi = ok ? rows.z[i] : 0.f;
+  int lo, hi;
+  tile_event_range(ok, ev, &lo_s, &hi_s, lo, hi);
+  double aw = 0.0, az = 0.0;
+  const int64_t n_chunks = (cols.n + kRbfChunk - 1) / kRbfChunk;
+  for (int64_t c = 0; c < n_chunks; ++c) {
+    const int2 r = col_ranges[c];
+    if (r.y < lo || r.x > hi) continue;
+    const int64_t j0 = c * kRbfChunk;
+    const int cnt = cols.n - j0 < kRbfChunk ? (int)(cols.n - j0) : kRbfChunk;
+    __syncthreads();
+    for (int k = threadIdx.x; k < cnt; k += kRbfRows) {
+      cz[k] = cols.z[j0 + k];
+      cw[k] = cols.w[j0 + k];
+      cd[k] = col_dmin[j0 + k];
+      ca[k] = col_amin[j0 + k];
+    }
+    __syncthreads();
+    if (ok) {
+      for (int k = 0; k < cnt; ++k) {
+        if (ca[k] == (int)i && cd[k] < 1e4f) {
+          aw += (double)cd[k] * (double)cw[k];
+          az += (double)cw[k] * 2.0 * (double)__fsub_rn(zi, cz[k]);
+        }
+      }
+    }
+  }
+  if (ok) {
+    acc_w[i] = (float)aw;
+    acc_z[i] = (float)az;
+  }
+}
+
+// loss and gradients of chamfer_distance_3d_og (losses_jax.py:181-211)
+__global__ void k_chamfer_reduce(const float *__restrict__ wa, int64_t n, const float *__restrict__ wb, int64_t m,
+                                 const float *__restrict__ ma, const int32_t *__restrict__ ia,
+                                 const float *__restrict__ mb, const int32_t *__restrict__ ib, float *out) {
+  __shared__ double red[32];
+  double t = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+    if (ma[i] < 1e4f) t += (double)ma[i] * wa[i] * wb[ia[i]];
+  for (int64_t j = threadIdx.x; j < m; j += blockDim.x)
+    if (mb[j] < 1e4f) t += (double)mb[j] * wb[j] * wa[ib[j]];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) a += red[k];
+    out[0] = (float)a;
+  }
+}
+
+__global__ void k_chamfer_grad(HitSet4 pred, HitSet4 ref, const float *__restrict__ ma,
+                               const int32_t *__restrict__ ia, const float *__restrict__ acc_w,
+                               const float *__restrict__ acc_z, float *__restrict__ g_w, float *__restrict__ g_z) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= pred.n) return;
+  double gw = acc_w[i], gz = (double)pred.w[i] * acc_z[i];
+  if (ma[i] < 1e4f) {
+    const int j = ia[i];
+    gw += (double)ma[i] * ref.w[j];
+    gz += (double)pred.w[i] * ref.w[j] * 2.0 * (double)__fsub_rn(pred.z[i], ref.z[j]);
+  }
+  if (g_w) g_w[i] = (float)gw;
+  if (g_z) g_z[i] = (float)gz;
+}
+
 struct MseAdcWs {
   float *a, *az, *b, *bz, *c;
   int2 *rng_pred, *rng_ref;
@@ -254,6 +525,81 @@ int run_mse_adc(const float *x, const float *y, const float *z, const int32_t *e
     k_mse_adc_grad<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pred, s.a, s.b, s.az, s.bz, s.tot, lambda_q,
                                                                 (float)(1.0 / ((double)sigma * (double)sigma)),
                                                                 grad_w, grad_z);
+  return LSIM_OK;
+}
+
+
+// nll_loss: out[0..2] = loss, sum of hit_prob, sum of log(lambda + 1e-10)
+size_t nll_workspace_bytes(int64_t n, int64_t m) {
+  auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  return 3 * al(4 * (size_t)n) + 2 * al(4 * (size_t)m) +
+         al(sizeof(int2) * (size_t)((n + kRbfChunk - 1) / kRbfChunk + 1)) +
+         al(sizeof(int2) * (size_t)((m + kRbfChunk - 1) / kRbfChunk + 1));
+}
+
+int run_nll(const float *x, const float *y, const float *z, const float *q, const int32_t *event, const float *hp,
+            int64_t n, const float *rx, const float *ry, const float *rz, const float *rq, const int32_t *revent,
+            const float *rhp, int64_t m, float sigma, float *out, float *g_q, float *g_z, float *g_hp, void *ws,
+            cudaStream_t st) {
+  auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  char *b = static_cast<char *>(ws);
+  float *s = reinterpret_cast<float *>(b); b += al(4 * (size_t)n);
+  float *sz = reinterpret_cast<float *>(b); b += al(4 * (size_t)n);
+  float *sq = reinterpret_cast<float *>(b); b += al(4 * (size_t)n);
+  float *lam = reinterpret_cast<float *>(b); b += al(4 * (size_t)m);
+  float *cw = reinterpret_cast<float *>(b); b += al(4 * (size_t)m);
+  int2 *rng_pred = reinterpret_cast<int2 *>(b); b += al(sizeof(int2) * (size_t)((n + kRbfChunk - 1) / kRbfChunk + 1));
+  int2 *rng_ref = reinterpret_cast<int2 *>(b);
+  const float two_s2 = (float)(2.0 * (double)sigma * (double)sigma);
+  const HitSet4 pred{x, y, z, q, hp, event, n};
+  if (n > 0) k_chunk_events<<<(unsigned)((n + kRbfChunk - 1) / kRbfChunk), kRbfChunk, 0, st>>>(event, n, rng_pred);
+  if (m > 0) k_chunk_events<<<(unsigned)((m + kRbfChunk - 1) / kRbfChunk), kRbfChunk, 0, st>>>(revent, m, rng_ref);
+  if (m > 0)   // lambda_j = sum_i hp_i K_ij
+    k_gauss4_rows<<<(unsigned)((m + kRbfRows - 1) / kRbfRows), kRbfRows, 0, st>>>(
+        HitSet4{rx, ry, rz, rq, rhp, revent, m}, pred, rng_pred, two_s2, lam, nullptr, nullptr);
+  if (m > 0) k_nll_colw<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(rhp, lam, m, cw);
+  if (n > 0)
+    k_gauss4_rows<<<(unsigned)((n + kRbfRows - 1) / kRbfRows), kRbfRows, 0, st>>>(
+        pred, HitSet4{rx, ry, rz, rq, cw, revent, m}, rng_ref, two_s2, s, sz, sq);
+  k_nll_reduce<<<1, 1024, 0, st>>>(hp, n, rhp, lam, m, out);
+  if (n > 0 && (g_q || g_z || g_hp))
+    k_nll_grad<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(hp, n, s, sz, sq,
+                                                            (float)(1.0 / ((double)sigma * (double)sigma)), g_hp,
+                                                            g_z, g_q);
+  return LSIM_OK;
+}
+
+size_t chamfer_workspace_bytes(int64_t n, int64_t m) {
+  auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  return 4 * al(4 * (size_t)n) + 2 * al(4 * (size_t)m) +
+         al(sizeof(int2) * (size_t)((n + kRbfChunk - 1) / kRbfChunk + 1)) +
+         al(sizeof(int2) * (size_t)((m + kRbfChunk - 1) / kRbfChunk + 1));
+}
+
+int run_chamfer(const float *x, const float *y, const float *z, const int32_t *event, const float *w, int64_t n,
+                const float *rx, const float *ry, const float *rz, const int32_t *revent, const float *rw, int64_t m,
+                float *out, float *g_w, float *g_z, void *ws, cudaStream_t st) {
+  auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  char *b = static_cast<char *>(ws);
+  float *ma = reinterpret_cast<float *>(b); b += al(4 * (size_t)n);
+  int32_t *ia = reinterpret_cast<int32_t *>(b); b += al(4 * (size_t)n);
+  float *aw = reinterpret_cast<float *>(b); b += al(4 * (size_t)n);
+  float *az = reinterpret_cast<float *>(b); b += al(4 * (size_t)n);
+  float *mb = reinterpret_cast<float *>(b); b += al(4 * (size_t)m);
+  int32_t *ib = reinterpret_cast<int32_t *>(b); b += al(4 * (size_t)m);
+  int2 *rng_pred = reinterpret_cast<int2 *>(b); b += al(sizeof(int2) * (size_t)((n + kRbfChunk - 1) / kRbfChunk + 1));
+  int2 *rng_ref = reinterpret_cast<int2 *>(b);
+  const HitSet4 pred{x, y, z, nullptr, w, event, n}, ref{rx, ry, rz, nullptr, rw, revent, m};
+  if (n > 0) k_chunk_events<<<(unsigned)((n + kRbfChunk - 1) / kRbfChunk), kRbfChunk, 0, st>>>(event, n, rng_pred);
+  if (m > 0) k_chunk_events<<<(unsigned)((m + kRbfChunk - 1) / kRbfChunk), kRbfChunk, 0, st>>>(revent, m, rng_ref);
+  if (n > 0) k_nn_rows<<<(unsigned)((n + kRbfRows - 1) / kRbfRows), kRbfRows, 0, st>>>(pred, ref, rng_ref, ma, ia);
+  if (m > 0) k_nn_rows<<<(unsigned)((m + kRbfRows - 1) / kRbfRows), kRbfRows, 0, st>>>(ref, pred, rng_pred, mb, ib);
+  k_chamfer_reduce<<<1, 1024, 0, st>>>(w, n, rw, m, ma, ia, mb, ib, out);
+  if (n > 0 && (g_w || g_z)) {
+    k_chamfer_back<<<(unsigned)((n + kRbfRows - 1) / kRbfRows), kRbfRows, 0, st>>>(pred, ref, rng_ref, mb, ib, aw,
+                                                                                   az);
+    k_chamfer_grad<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pred, ref, ma, ia, aw, az, g_w, g_z);
+  }
   return LSIM_OK;
 }
 

@@ -8,14 +8,17 @@ hand-written CUDA kernels in ``liblsim.so`` (C ABI: include/lsim.h).
 
 from .consts import (Params, RecombinationMode, build_params_class, default_params, get_vdrift,  # noqa: F401
                      load_detector_properties)
-from .sim import (get_adc_values, load_lut, pad_size, prepare_lut, simulate_parametrized,  # noqa: F401
-                  simulate_stochastic, simulate_wfs)
+from .sim import (average_hit_values, get_adc_values, get_adc_values_average_noise_vmap,  # noqa: F401
+                  get_average_hit_values, load_lut, pad_size, prepare_lut, simulate_parametrized,
+                  simulate_probabilistic, simulate_stochastic, simulate_wfs)
 from .fee import digitize  # noqa: F401
-from .losses import adc2charge  # noqa: F401
+from .losses import adc2charge, chamfer_3d, mse_adc, nll_loss  # noqa: F401
 from .dataio import chop_tracks  # noqa: F401
 
 __all__ = [
     "Params", "RecombinationMode", "build_params_class", "default_params", "get_vdrift",
     "load_detector_properties", "get_adc_values", "load_lut", "pad_size", "prepare_lut",
     "simulate_parametrized", "simulate_stochastic", "simulate_wfs", "digitize", "adc2charge", "chop_tracks",
+    "simulate_probabilistic", "get_adc_values_average_noise_vmap", "get_average_hit_values", "average_hit_values",
+    "mse_adc", "nll_loss", "chamfer_3d",
 ]

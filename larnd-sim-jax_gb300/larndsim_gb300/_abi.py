@@ -99,6 +99,12 @@ _SIGNATURES = {
     "lsim_mse_adc_workspace_bytes": (_sz, [_i64, _i64]),
     "lsim_mse_adc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, C.c_float, C.c_float,
                                _vp, _vp, _vp, _vp, _sz, _vp]),
+    "lsim_nll_workspace_bytes": (_sz, [_i64, _i64]),
+    "lsim_nll_loss": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _i64, C.c_float,
+                                _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "lsim_chamfer_workspace_bytes": (_sz, [_i64, _i64]),
+    "lsim_chamfer_3d": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
+                                  _sz, _vp]),
     "lsim_chop_workspace_bytes": (_sz, [_i64]),
     "lsim_chop_tracks": (C.c_int, [_PF, _vp, _i64, C.c_double, _vp, _i64, _vp, _vp, _sz, _vp]),
     "lsim_param_stage1": (C.c_int, [_PP, _PF, _vp, _i64, _i32, _vp, _vp, _sz, _vp, _vp]),

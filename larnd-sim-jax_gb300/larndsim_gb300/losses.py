@@ -73,3 +73,102 @@ def mse_adc(params, Q, x, y, z, ticks, hit_prob, event, ref_Q, ref_x, ref_y, ref
     aux = {"charge_loss": parts[2], "mmd_loss_term": parts[1], "Q": Q, "ref_Q": rQ, "ref_hit_prob": rhp,
            "hit_prob": hp}
     return loss, aux
+
+
+class _NllFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, q, z, hp, x, y, event, rq, rx, ry, rz, revent, rhp, sigma):
+        from . import _abi, sim
+        lib = _abi.load()
+        dev = q.device
+        n, m = q.shape[0], rq.shape[0]
+        ws = torch.empty(max(lib.lsim_nll_workspace_bytes(n, m), 1), dtype=torch.uint8, device=dev)
+        out = torch.empty(4, dtype=torch.float32, device=dev)
+        grads = [torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3)]
+        p = sim._ptr
+        _abi.check(lib, lib.lsim_nll_loss(p(x), p(y), p(z), p(q), p(event), p(hp), n, p(rx), p(ry), p(rz), p(rq),
+                                          p(revent), p(rhp), m, float(sigma), p(out), *(p(g) for g in grads), p(ws),
+                                          ws.numel(), sim._stream()))
+        ctx.save_for_backward(*grads)
+        ctx.mark_non_differentiable(out)
+        return out[0].clone(), out
+
+    @staticmethod
+    def backward(ctx, g, _g_out):
+        gq, gz, ghp = ctx.saved_tensors
+        return g * gq, g * gz, g * ghp, *(None,) * 10
+
+
+def nll_loss(params, Q, x, y, z, ticks, hit_prob, event, ref_Q, ref_x, ref_y, ref_z, ref_ticks, ref_hit_prob,
+             ref_event, adc_norm=10., sigma=1., match_z=False):
+    """losses_jax.py:329-359: negative log-likelihood of the reference hits
+    under the Gaussian intensity of the predicted hits on
+    (x + event * 1e9, y, z, Q / adc_norm).  Returns (loss, {}); the loss is
+    differentiable with respect to Q, z and hit_prob."""
+    from .sim import pad_size
+    Q = torch.as_tensor(Q, dtype=torch.float32)
+    dev = Q.device if Q.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    Q = Q.to(dev)
+    pad_size((len(ref_Q), Q.shape[0]), "nll_loss")   # the reference's size history (padding adds nothing)
+    q = (Q / np.float32(adc_norm)).contiguous()
+    rq = (_f32(ref_Q, dev) / np.float32(adc_norm)).contiguous()
+    hp = torch.as_tensor(hit_prob, dtype=torch.float32).to(dev).contiguous()
+    zt = torch.as_tensor(z, dtype=torch.float32).to(dev).contiguous()
+    loss, _ = _NllFn.apply(q, zt, hp, _f32(x, dev), _f32(y, dev), _i32(event, dev), rq, _f32(ref_x, dev),
+                           _f32(ref_y, dev), _f32(ref_z, dev), _i32(ref_event, dev), _f32(ref_hit_prob, dev),
+                           float(sigma))
+    return loss, dict()
+
+
+class _ChamferFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, w, z, x, y, event, rw, rx, ry, rz, revent):
+        from . import _abi, sim
+        lib = _abi.load()
+        dev = w.device
+        n, m = w.shape[0], rw.shape[0]
+        ws = torch.empty(max(lib.lsim_chamfer_workspace_bytes(n, m), 1), dtype=torch.uint8, device=dev)
+        out = torch.empty(4, dtype=torch.float32, device=dev)
+        gw = torch.empty(n, dtype=torch.float32, device=dev)
+        gz = torch.empty(n, dtype=torch.float32, device=dev)
+        p = sim._ptr
+        _abi.check(lib, lib.lsim_chamfer_3d(p(x), p(y), p(z), p(event), p(w), n, p(rx), p(ry), p(rz), p(revent),
+                                            p(rw), m, p(out), p(gw), p(gz), p(ws), ws.numel(), sim._stream()))
+        ctx.save_for_backward(gw, gz)
+        ctx.mark_non_differentiable(out)
+        return out[0].clone(), out
+
+    @staticmethod
+    def backward(ctx, g, _g_out):
+        gw, gz = ctx.saved_tensors
+        return g * gw, g * gz, *(None,) * 8
+
+
+def _pad(t, n, value=0):
+    if t.shape[0] >= n:
+        return t
+    return torch.cat([t, torch.full((n - t.shape[0],), value, dtype=t.dtype, device=t.device)])
+
+
+def chamfer_3d(params, Q, x, y, z, ticks, hit_prob, event, ref_Q, ref_x, ref_y, ref_z, ref_ticks, ref_hit_prob,
+               ref_event, adc_norm=10., match_z=False):
+    """losses_jax.py:213-229: nearest-neighbour (Chamfer) distance between
+    predicted and reference hits on (x + event * 1e9, y, z), weighted by
+    Q / adc_norm, with both sets zero-padded to pad_size's buckets as the
+    reference pads them.  Returns (loss, {}); differentiable with respect
+    to Q and z."""
+    from .sim import pad_size
+    Q = torch.as_tensor(Q, dtype=torch.float32)
+    dev = Q.device if Q.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    Q = Q.to(dev)
+    n, m = Q.shape[0], len(ref_Q)
+    new_ref, new_cur = pad_size((m, n), "chamfer_3d")
+    w = _pad(Q / np.float32(adc_norm), new_cur).contiguous()
+    rw = _pad(_f32(ref_Q, dev) / np.float32(adc_norm), new_ref).contiguous()
+    zt = _pad(torch.as_tensor(z, dtype=torch.float32).to(dev), new_cur).contiguous()
+    loss, _ = _ChamferFn.apply(w, zt, _pad(_f32(x, dev), new_cur).contiguous(), _pad(_f32(y, dev), new_cur).contiguous(),
+                               _pad(_i32(event, dev), new_cur).contiguous(), rw,
+                               _pad(_f32(ref_x, dev), new_ref).contiguous(), _pad(_f32(ref_y, dev), new_ref).contiguous(),
+                               _pad(_f32(ref_z, dev), new_ref).contiguous(),
+                               _pad(_i32(ref_event, dev), new_ref).contiguous())
+    return loss, dict()

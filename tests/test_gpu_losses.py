@@ -100,7 +100,7 @@ def test_params_loss_gradient(cuda):
     zd = z.detach().requires_grad_(True)
     l2, _ = losses.mse_adc(pp, Qd, x, y, zd, t, hp, ev, *ref)
     l2.backward()
-    assert abs(float(l2) - float(loss)) <= 1e-6 * abs(float(loss))
+    assert abs(float(l2.detach()) - float(loss.detach())) <= 1e-6 * abs(float(loss.detach()))
     g_explicit = torch.autograd.grad((Q * Qd.grad).sum() + (z * zd.grad).sum(), th)[0].cpu().numpy()
     g_vec = np.array([g[k] for k in grad.GRAD_PARAMS])
     np.testing.assert_allclose(g_vec, g_explicit, rtol=1e-5, atol=1e-6 * np.abs(g_vec).max())
@@ -144,3 +144,48 @@ def test_params_loss_gradient(cuda):
     for k in G.GRAD_PARAMS:
         err = abs(g[k] - fd[k])
         assert err <= 2e-3 * abs(fd[k]) or err * abs(th0[k]) <= 1e-4 * sens, (k, g[k], fd[k])
+
+
+def test_nll_loss_matches_oracle(cuda):
+    from larndsim_gb300 import consts, losses
+    from oracle import losses_np as L
+    rng = np.random.default_rng(12)
+    x, y, z, ev = _hits(rng, 500, 4, spread=1.5)
+    rx, ry, rz, rev = _hits(rng, 450, 4, spread=1.5)
+    Q = rng.uniform(5, 40, 500).astype(np.float32)
+    rQ = rng.uniform(5, 40, 450).astype(np.float32)
+    hp = rng.uniform(0.1, 1.0, 500).astype(np.float32)
+    rhp = (rng.uniform(0, 1, 450) > 0.2).astype(np.float32)
+    tQ = torch.from_numpy(Q).cuda().requires_grad_(True)
+    tz = torch.from_numpy(z).cuda().requires_grad_(True)
+    thp = torch.from_numpy(hp).cuda().requires_grad_(True)
+    loss, _ = losses.nll_loss(consts.Params(), tQ, x, y, tz, None, thp, ev, rQ, rx, ry, rz, None, rhp, rev,
+                              adc_norm=10.0, sigma=1.0)
+    loss.backward()
+    ref, gq, gz, ghp = L.nll_loss(Q, x, y, z, hp, ev, rQ, rx, ry, rz, rhp, rev, adc_norm=10.0, sigma=1.0)
+    assert abs(float(loss.detach()) - ref) <= 1e-5 * abs(ref)
+    for got, exp in ((tQ.grad, gq), (tz.grad, gz), (thp.grad, ghp)):
+        np.testing.assert_allclose(got.cpu().numpy(), exp, atol=1e-4 * np.abs(exp).max(), rtol=0)
+
+
+@pytest.mark.parametrize("n_events", [1, 4])
+def test_chamfer_3d_matches_oracle(cuda, n_events):
+    """Including the reference's zero padding (pad_size buckets) and the
+    float32 rounding of x + event * 1e9."""
+    from larndsim_gb300 import consts, losses, sim
+    from oracle import losses_np as L
+    rng = np.random.default_rng(20 + n_events)
+    x, y, z, ev = _hits(rng, 600, n_events)
+    rx, ry, rz, rev = _hits(rng, 520, n_events)
+    Q = rng.uniform(5, 40, 600).astype(np.float32)
+    rQ = rng.uniform(5, 40, 520).astype(np.float32)
+    sim.reset_size_history()
+    tQ = torch.from_numpy(Q).cuda().requires_grad_(True)
+    tz = torch.from_numpy(z).cuda().requires_grad_(True)
+    loss, _ = losses.chamfer_3d(consts.Params(), tQ, x, y, tz, None, None, ev, rQ, rx, ry, rz, None, None, rev)
+    loss.backward()
+    sizes = sim.get_size_history()["chamfer_3d"][0]
+    ref, gq, gz = L.chamfer_3d(Q, x, y, z, ev, rQ, rx, ry, rz, rev, adc_norm=10.0, pad_to=(sizes[1], sizes[0]))
+    assert abs(float(loss.detach()) - ref) <= 1e-5 * abs(ref)
+    np.testing.assert_allclose(tQ.grad.cpu().numpy(), gq, atol=1e-4 * np.abs(gq).max(), rtol=0)
+    np.testing.assert_allclose(tz.grad.cpu().numpy(), gz, atol=1e-4 * np.abs(gz).max(), rtol=0)
