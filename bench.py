@@ -64,9 +64,10 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--events", type=int, default=N_EVENTS, help="events per batch (profiling runs use fewer)")
-    ap.add_argument("--path", choices=["grad", "chop", "prob"], default="grad",
+    ap.add_argument("--path", choices=["grad", "chop", "prob", "loss"], default="grad",
                     help="grad: the fwd+bwd step (default); chop: on-device chop_tracks of one 500k-segment event; "
-                         "prob: the probabilistic front end on the waveforms of 8 events")
+                         "prob: the probabilistic front end on the waveforms of 8 events; loss: mse_adc forward + "
+                         "gradient on the hits of the 64-event batch")
     return ap.parse_args()
 
 
@@ -580,6 +581,94 @@ def run_prob(args):
     print(json.dumps(rec), flush=True)
 
 
+# ---------------------------------------------------------------- hit-level fit loss
+
+def run_loss(args):
+    """mse_adc (losses_jax.py:60-79) forward + gradient with respect to the
+    hit charges and z, on the hits of the 64-event batch simulated at the
+    perturbed parameters against those at the nominal ones."""
+    import torch
+    from larndsim_gb300 import grad, losses, sim, workloads
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    params = nominal_params()
+    tmpl, params = sim.load_lut(workloads.synthetic_response(seed=0), params)
+    tracks, fields = workload(0, args.seed)
+    chain = grad.LUTChain(params, tmpl, tracks, fields)
+    with torch.no_grad():
+        ref = [t.detach() for t in grad.predicted_hits(grad.theta_of(params, device="cuda"), chain, params)]
+        pred = [t.detach() for t in grad.predicted_hits(grad.theta_of(perturbed(params), device="cuda"), chain,
+                                                        perturbed(params))]
+    Q, x, y, z, t, hp, ev = pred
+    n, m = Q.shape[0], ref[0].shape[0]
+
+    def step():
+        q = Q.clone().requires_grad_(True)
+        zz = z.clone().requires_grad_(True)
+        loss, _ = losses.mse_adc(params, q, x, y, zz, t, hp, ev, *ref)
+        loss.backward()
+        return loss
+
+    for _ in range(args.warmup):
+        step()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(torch.cuda.current_device())
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        starts[i].record()
+        step()
+        ends[i].record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in zip(starts, ends)]))
+    counts = torch.bincount(ev.long()).cpu().numpy().astype(np.float64)
+    rcounts = torch.bincount(ref[6].long()).cpu().numpy().astype(np.float64)
+    k = min(len(counts), len(rcounts))
+    pairs = float((counts ** 2).sum() + (rcounts ** 2).sum() + (counts[:k] * rcounts[:k]).sum())
+    host = [a.cpu().pin_memory() for a in pred + ref]
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        hq = host[0].cuda(non_blocking=True).requires_grad_(True)
+        hz = host[3].cuda(non_blocking=True).requires_grad_(True)
+        rest = [a.cuda(non_blocking=True) for a in host]
+        loss, _ = losses.mse_adc(params, hq, rest[1], rest[2], hz, rest[4], rest[5], rest[6], *rest[7:])
+        loss.backward()
+        out = (float(loss.detach()), hq.grad.cpu(), hz.grad.cpu())
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    rec = {"metric": "mse_adc fwd+bwd hits/s", "value": n / (ms * 1e-3), "unit": "hits/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tracks and LUT)",
+           "config": {"workload": f"mse_adc (sigma=1, lambda_Q=1) of the {n} predicted vs {m} reference hits of the "
+                                  "64-event batch, loss + dL/dQ + dL/dz", "hits": n, "ref_hits": m,
+                      "same_event_pair_terms": pairs, "l2": "working set < L2 (hits only)"},
+           "e2e": {"value": n / e2e_s, "unit": "hits/s", "ms_per_step": e2e_s * 1e3,
+                   "h2d_bytes_per_step": int(sum(a.numel() * 4 for a in host)), "d2h_bytes_per_step": 4 + 8 * n},
+           "roofline": {"bound": "issue", "kernel": "k_rbf_rows",
+                        "note": "pairwise exp per same-event pair; inputs are a few MB"},
+           "gpu_launches": 7 * args.steps, "clocks": clk}
+    if not args.no_cpu_baseline:
+        from oracle import losses_np as L
+        e0 = (ev == 0).cpu().numpy()
+        r0 = (ref[6] == 0).cpu().numpy()
+        a = [v.cpu().numpy() for v in pred]
+        b = [v.cpu().numpy() for v in ref]
+        t0 = time.perf_counter()
+        L.mse_adc(a[0][e0], a[1][e0], a[2][e0], a[3][e0], a[5][e0], a[6][e0], b[0][r0], b[1][r0], b[2][r0],
+                  b[3][r0], b[5][r0], b[6][r0])
+        L.mse_adc_grad(a[0][e0], a[1][e0], a[2][e0], a[3][e0], a[6][e0], b[0][r0], b[1][r0], b[2][r0], b[3][r0],
+                       b[6][r0])
+        dt = time.perf_counter() - t0
+        rec["cpu_baseline"] = {"value": float(e0.sum()) / dt, "unit": "hits/s", "cores": 1, "kind": "port",
+                               "sample": f"event 0 ({int(e0.sum())} hits vs {int(r0.sum())}), float64 numpy "
+                                         f"restatement, loss + gradients, {dt:.2f} s"}
+    print(json.dumps(rec), flush=True)
+
+
 def run_chop_reference(args):
     """CPU arm of --path chop: the numpy restatement of chop_tracks, one
     bounded sample (the first 20k tracks of the same event) per step."""
@@ -611,6 +700,13 @@ def run_chop_reference(args):
 
 def main():
     args = parse()
+    if args.path == "loss":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "loss path: its CPU arm is the cpu_baseline of "
+                                                                  "--path loss (the numpy restatement)"}))
+        else:
+            run_loss(args)
+        return
     if args.path == "prob":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "prob path: its CPU arm is the cpu_baseline of "
