@@ -231,6 +231,18 @@ int lsim_lut_grad_stored(const LsimParams *p, const void *tables, const void *ws
                          const int32_t *tgt_pids, const float *tgt_adc, int64_t n_tgt, float *loss_out,
                          float *grad_out, float *adc_out, void *stream);
 
+/* Vector-Jacobian product of simulate_wfs: for a cotangent g_wfs on the
+ * waveforms lsim_lut_stage2 writes ([p_pad][n_ticks - 1], the n_valid valid
+ * rows last), dL/dtheta = sum g_wfs * d wfs / d theta for the LSIM_NPARAM
+ * parameters into grad_out.  ws holds the stage-1 state at the parameters
+ * (lsim_lut_stage1 / lsim_lut_stage1_theta).  Rows with a negative pixel id
+ * are zero in this library and carry no gradient.  Replaces jax.vjp /
+ * jax.grad through simulate_wfs, src/larndsim/sim_jax.py:689-736, as the
+ * reference's Taylor scans (tests/taylor/scan_utils.py:120-137) and
+ * waveform-level losses use it. */
+int lsim_lut_wfs_vjp(const LsimParams *p, const void *tables, const void *ws, int64_t n_rows, int32_t n_events,
+                     const float *g_wfs, int64_t p_pad, int32_t n_valid, float *grad_out, void *stream);
+
 /* ---------------------------------------------------------------- FEE + hits */
 
 /* Self-trigger FEE + digitize on waveforms wfs[n_pix][n_t]: ADC values and

@@ -567,7 +567,9 @@ __device__ __forceinline__ int32_t slot_pid(const LsimParams &p, const Grid &g, 
 
 template <int MODE>
 __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a) {
-  constexpr bool GRAD = (MODE == kModeGrad || MODE == kModeGradStored);
+  // kModeVjpWfs: the cotangent row comes from memory (no forward, no front end)
+  constexpr bool VJP = MODE == kModeVjpWfs;
+  constexpr bool GRAD = (MODE == kModeGrad || MODE == kModeGradStored || VJP);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x % kWarp, wid = threadIdx.x / kWarp;
   unsigned char *wbase = smem_raw + (size_t)wid * a.warp_smem;
@@ -601,7 +603,7 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a
     // adjoint mode: this lane's hit cotangent, or the target ADC of the
     // pixel (digitize(0) where the target has no such pixel), loaded early
     float cot = 0.f;
-    if constexpr (GRAD) {
+    if constexpr (GRAD && !VJP) {
       if (lane < H) {
         if (a.g_adc) {
           cot = a.g_adc[(int64_t)r * H + lane];
@@ -614,8 +616,9 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a
     float4 *b4 = reinterpret_cast<float4 *>(sm.buf);
     for (int i = lane; i < kRowFloats / 4; i += kWarp) b4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     build_list(a.g, a.w.cnt, a.w.off, slot, sm.list, lane);
-    if (MODE == kModeGradStored) {
-      // the waveform stored by a preceding simulate_wfs pass (columns 1..T)
+    if (MODE == kModeGradStored || VJP) {
+      // the waveform stored by a preceding simulate_wfs pass, or (VJP) the
+      // cotangent of the waveform row (columns 1..T; tick 0 stays zero)
       const float4 *src = reinterpret_cast<const float4 *>(a.wfs + (a.row_offset + r) * (int64_t)T);
       float4 *dst = reinterpret_cast<float4 *>(row + 1);
       for (int i = lane; i < T / 4; i += kWarp) dst[i] = __ldg(src + i);
@@ -633,19 +636,24 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a
       for (int i = lane; i < T / 4; i += kWarp) dst[i] = src[i];
       continue;
     }
-    // ---- front end on the output ticks (row + 1)
-    const float *nrm = a.normals ? a.normals + (int64_t)r * (1 + 3 * H) : nullptr;
-    float *adc_dst = a.adc_out ? a.adc_out + (int64_t)r * H : nullptr;
-    float *tick_dst = a.tick_out ? a.tick_out + (int64_t)r * H : nullptr;
-    warp_cumsum_charge(row + 1, T, p.t_sampling, lane);
-    if (MODE == kModeAdc) {
-      fee_forward(p, row + 1, T, nrm, adc_dst, tick_dst, nullptr, nullptr, early_exit, lane);
-      continue;
+    float loss = 0.f;
+    if constexpr (!VJP) {
+      // ---- front end on the output ticks (row + 1)
+      const float *nrm = a.normals ? a.normals + (int64_t)r * (1 + 3 * H) : nullptr;
+      float *adc_dst = a.adc_out ? a.adc_out + (int64_t)r * H : nullptr;
+      float *tick_dst = a.tick_out ? a.tick_out + (int64_t)r * H : nullptr;
+      warp_cumsum_charge(row + 1, T, p.t_sampling, lane);
+      if (MODE == kModeAdc) {
+        fee_forward(p, row + 1, T, nrm, adc_dst, tick_dst, nullptr, nullptr, early_exit, lane);
+        continue;
+      }
     }
-    if constexpr (GRAD) {
+    if constexpr (GRAD && !VJP) {
+      const float *nrm = a.normals ? a.normals + (int64_t)r * (1 + 3 * H) : nullptr;
+      float *adc_dst = a.adc_out ? a.adc_out + (int64_t)r * H : nullptr;
+      float *tick_dst = a.tick_out ? a.tick_out + (int64_t)r * H : nullptr;
       fee_forward(p, row + 1, T, nrm, adc_dst, tick_dst, &sm.fee, nullptr, early_exit, lane);
       // loss terms and digitisation adjoint, lane h for hit h
-      float loss = 0.f;
       if (lane < H) {
         const float raw = sm.fee.raw[lane];
         const float adc = digitize(p, raw);
@@ -664,6 +672,8 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a
       fee_backward(p, row + 1, T, &sm.fee, sm.gint, lane);
       if (lane == 0) row[0] = 0.f;
       __syncwarp();
+    }
+    if constexpr (GRAD) {
       Theta th;
 #pragma unroll
       for (int i = 0; i < LSIM_NPARAM; ++i) th.v[i] = 0.f;
@@ -819,7 +829,8 @@ static int run_heavy_pixels(const AccumArgs &a, cudaStream_t st) {
 // workspace, one kFeeMaskWords block per warp).
 template <int MODE>
 static size_t warp_smem_bytes(const LsimParams &) {
-  return (sizeof(WarpSmem<MODE == kModeGrad || MODE == kModeGradStored>) + 15) & ~size_t(15);
+  return (sizeof(WarpSmem<MODE == kModeGrad || MODE == kModeGradStored || MODE == kModeVjpWfs>) + 15) &
+         ~size_t(15);
 }
 
 // Persistent grid: every SM filled to its occupancy limit.
@@ -886,6 +897,9 @@ int run_accum(AccumMode mode, const AccumArgs &a, cudaStream_t st) {
         if (cudaGetLastError() != cudaSuccess) return LSIM_ERR_CUDA;
       }
       rc = launch_mode<kModeGrad>(a, st);
+      return rc != LSIM_OK ? rc : run_main_adjoint(a, st);
+    case kModeVjpWfs:
+      rc = launch_mode<kModeVjpWfs>(a, st);
       return rc != LSIM_OK ? rc : run_main_adjoint(a, st);
     case kModeGradStored:
       if (!a.g_adc && a.n_tgt > 0 && a.n_rows > 0) {

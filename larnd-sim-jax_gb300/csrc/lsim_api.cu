@@ -302,6 +302,23 @@ int lsim_lut_grad_stored(const LsimParams *p, const void *tables, const void *ws
   return wrap(run_grad_finalize(a, loss_out, grad_out, st), "lsim_lut_grad_stored");
 }
 
+int lsim_lut_wfs_vjp(const LsimParams *p, const void *tables, const void *ws, int64_t n_rows, int32_t n_events,
+                     const float *g_wfs, int64_t p_pad, int32_t n_valid, float *grad_out, void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (!tables || !ws || !grad_out || (n_valid > 0 && !g_wfs)) return fail(LSIM_ERR_INVALID, "lsim_lut_wfs_vjp: null pointer");
+  if (n_valid < 0 || p_pad < n_valid) return fail(LSIM_ERR_CAPACITY, "lsim_lut_wfs_vjp: p_pad < n_valid");
+  cudaStream_t st = (cudaStream_t)stream;
+  AccumArgs a = make_args(p, tables, ws, n_rows, n_events);
+  a.n_valid = n_valid;
+  a.row_offset = p_pad - n_valid;
+  a.wfs = const_cast<float *>(g_wfs);
+  rc = run_accum(kModeVjpWfs, a, st);
+  if (rc) return wrap(rc, "lsim_lut_wfs_vjp");
+  return wrap(run_grad_finalize(a, nullptr, grad_out, st), "lsim_lut_wfs_vjp");
+}
+
 int lsim_fee(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, const float *normals, float *adc_out,
              float *tick_out, float *integral_out, void *stream) {
   g_err.clear();

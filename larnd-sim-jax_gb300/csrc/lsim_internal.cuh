@@ -15,7 +15,7 @@ int run_fill_unique(const LsimParams &p, const Workspace &w, const Grid &g, int6
                     int32_t n_valid, int32_t *unique_pixels, float *wfs, int32_t nt_out, cudaStream_t st);
 
 // lsim_accum.cu
-enum AccumMode { kModeWfs = 0, kModeAdc = 1, kModeGrad = 2, kModeGradStored = 3 };
+enum AccumMode { kModeWfs = 0, kModeAdc = 1, kModeGrad = 2, kModeGradStored = 3, kModeVjpWfs = 4 };
 struct AccumArgs {
   LsimParams p;
   int64_t n_rows;           // segments (rows of the track table)

@@ -155,6 +155,34 @@ class LUTChain:
             raise ValueError("set_tracks needs the shape of the original batch")
         self.tracks.copy_(src, non_blocking=True)
 
+    def wfs(self, params):
+        """simulate_wfs at params on this chain's tracks: (wfs (P_pad, T),
+        unique_pixels (P_pad,)), rows as the reference orders them."""
+        st = self.stage1(params)
+        st.raise_status()
+        p_unique = st.n_em1 + st.n_valid + st.any_m1 + 1
+        p_pad = sim.pad_size(p_unique, "unique_pixels", 0.2)
+        T = int(st.lp.n_ticks) - 1
+        dev = self.tracks.device
+        wfs = torch.empty((p_pad, T), dtype=torch.float32, device=dev)
+        unique = torch.empty((p_pad,), dtype=torch.int32, device=dev)
+        _abi.check(self.lib, self.lib.lsim_lut_stage2(st.lp, sim._ptr(self.lut.tables), sim._ptr(st.ws), st.n_rows,
+                                                      st.n_events, p_pad, st.n_em1, st.n_valid, sim._ptr(wfs),
+                                                      sim._ptr(unique), sim._stream()))
+        return wfs, unique
+
+    def wfs_vjp(self, params, g_wfs: torch.Tensor):
+        """dL/dtheta for a cotangent on the waveforms ``wfs`` returns (same
+        shape; rows with a negative pixel id carry no gradient)."""
+        st = self.stage1(params)
+        n_valid = self._check(st)
+        g = g_wfs.to(device=self.tracks.device, dtype=torch.float32).contiguous()
+        out = torch.empty(_abi.NPARAM, dtype=torch.float32, device=self.tracks.device)
+        _abi.check(self.lib, self.lib.lsim_lut_wfs_vjp(st.lp, sim._ptr(self.lut.tables), sim._ptr(st.ws), st.n_rows,
+                                                       st.n_events, sim._ptr(g), g.shape[0], n_valid, sim._ptr(out),
+                                                       sim._stream()))
+        return out
+
     def vjp(self, params, g_adc: torch.Tensor, normals=None):
         """dL/dtheta for a given cotangent on the (n_valid, H) ADC grid."""
         g = g_adc.to(torch.float32).contiguous()
@@ -179,6 +207,32 @@ class _AdcFn(torch.autograd.Function):
             return None, None, None, None
         grad = ctx.chain.vjp(ctx.params, g_adc, ctx.normals)
         return grad.to(device=ctx.theta_device, dtype=ctx.theta_dtype), None, None, None
+
+
+class _WfsFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, theta, chain, params):
+        vals = theta.detach().cpu().numpy().astype(np.float64)
+        p = params.replace(**{k: float(v) for k, v in zip(GRAD_PARAMS, vals)})
+        wfs, unique = chain.wfs(p)
+        ctx.chain, ctx.params = chain, p
+        ctx.theta_device, ctx.theta_dtype = theta.device, theta.dtype
+        ctx.mark_non_differentiable(unique)
+        return wfs, unique
+
+    @staticmethod
+    def backward(ctx, g_wfs, g_unique):
+        if g_wfs is None:
+            return None, None, None
+        grad = ctx.chain.wfs_vjp(ctx.params, g_wfs)
+        return grad.to(device=ctx.theta_device, dtype=ctx.theta_dtype), None, None
+
+
+def wfs_fn(theta: torch.Tensor, chain: LUTChain, params):
+    """Differentiable simulate_wfs (sim_jax.py:689-736) as a function of
+    ``theta`` = the 8 parameter values (order ``GRAD_PARAMS``): returns
+    (wfs, unique_pixels); backward runs lsim_lut_wfs_vjp."""
+    return _WfsFn.apply(theta, chain, params)
 
 
 def lut_value_and_grad(params, response_template, tracks, fields, target: Target, n_events=None):

@@ -156,3 +156,32 @@ def test_stored_waveform_variant_matches_recompute(cuda):
     loss, g, wfs = chain.loss_and_grad_stored(pp, target)
     assert wfs.shape[0] == chain._stage.n_valid
     assert (loss, g) == a
+
+
+@pytest.mark.parametrize("case", [dict(n_neighbors=1), dict(n_neighbors=2, seed=5, n_tracks=2, shower=300)])
+def test_wfs_vjp_matches_complex_step(cuda, case):
+    """lsim_lut_wfs_vjp through grad.wfs_fn (jax.vjp of simulate_wfs): an
+    arbitrary cotangent on the waveform rows pulled back to the 8
+    parameters, against the complex-step derivative of the float64
+    waveforms of the oracle (decisions frozen)."""
+    from larndsim_gb300 import grad
+    from oracle import grad64 as G
+    p, tmpl, tracks, fields, chain, target = _setup(**case)
+    pp = _perturbed(p)
+    theta = grad.theta_of(pp).requires_grad_(True)
+    wfs, unique = grad.wfs_fn(theta, chain, pp)
+    rng = np.random.default_rng(4)
+    c = torch.from_numpy(rng.standard_normal(tuple(wfs.shape)).astype(np.float32)).cuda()
+    (wfs * c).sum().backward()
+    g_gpu = dict(zip(grad.GRAD_PARAMS, theta.grad.cpu().numpy().tolist()))
+    fr = G.Frozen(pp, tmpl, tracks, fields, target.pids.cpu().numpy(), target.adc.cpu().numpy())
+    u = unique.cpu().numpy()
+    assert np.array_equal(fr.unique[fr.valid], u[u >= 0])
+    cv = c.cpu().numpy().astype(np.float64)[u >= 0]
+    th = G.theta_dict(pp)
+    g_cs = {}
+    for k in G.GRAD_PARAMS:
+        tc = {q: complex(v) for q, v in th.items()}
+        tc[k] += 1e-30j
+        g_cs[k] = float((G.waveforms64(fr, tc)[fr.valid] * cv).sum().imag / 1e-30)
+    _check(g_gpu, g_cs, th)
