@@ -173,3 +173,48 @@ def test_library_rejects_bad_arguments_without_gpu(lib):
     assert b"null" in lib.lsim_last_error()
     p.n_neighbors = 7
     assert lib.lsim_lut_prepare(p, ctypes.c_void_p(16), ctypes.c_void_p(16), 1 << 40, None) == _abi.LSIM_ERR_UNSUPPORTED
+
+
+def test_next_row_entry_points_reject_bad_arguments_without_gpu(lib):
+    """The probabilistic front end, the fit losses, the waveform VJP and the
+    pixel coordinates validate their arguments before any launch."""
+    V = ctypes.c_void_p
+    p = _abi.make_params(consts.Params(number_pix_neighbors=4), (100, 45, 45, 1950))
+    ws = V(256)
+    big = 1 << 30
+    # probabilistic front end
+    assert lib.lsim_fee_prob_workspace_bytes(p) >= 4 * int(p.max_adc_values)
+    assert lib.lsim_fee_prob(p, V(16), 4, 2000, 20, 1e-9, V(16), V(16), V(16), None, None, ws, big,
+                             None) == _abi.LSIM_ERR_INVALID            # reductions: all three or none
+    assert lib.lsim_fee_prob(p, V(16), 4, 2000, 20, 0.0, None, None, None, None, None, ws, big,
+                             None) == _abi.LSIM_ERR_INVALID            # stop threshold
+    assert lib.lsim_fee_prob(p, V(16), 4, 2000, 20, 1e-9, None, None, None, None, None, ws, 0,
+                             None) == _abi.LSIM_ERR_CAPACITY
+    assert lib.lsim_fee_prob(p, V(16), 4, 4096, 20, 1e-9, None, None, None, None, None, ws, big,
+                             None) == _abi.LSIM_ERR_UNSUPPORTED        # n_t > 2048
+    assert lib.lsim_fee_prob(p, V(16), 4, 2000, 40, 1e-9, None, None, None, None, None, ws, big,
+                             None) == _abi.LSIM_ERR_UNSUPPORTED        # more than 32 paths
+    p0 = _abi.make_params(consts.Params(RESET_NOISE_CHARGE=0))
+    assert lib.lsim_fee_prob(p0, V(16), 4, 2000, 20, 1e-9, None, None, None, None, None, ws, big,
+                             None) == _abi.LSIM_ERR_INVALID            # noise width 0
+    # losses
+    out = V(64)
+    assert lib.lsim_mse_adc_workspace_bytes(1000, 900) > 4 * 1900
+    assert lib.lsim_mse_adc(V(16), V(16), V(16), V(16), V(16), 10, V(16), V(16), V(16), V(16), V(16), 10, 0.0, 1.0,
+                            out, None, None, ws, big, None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_mse_adc(V(16), V(16), V(16), V(16), V(16), 10, V(16), V(16), V(16), V(16), V(16), 10, 1.0, 1.0,
+                            out, None, None, ws, 8, None) == _abi.LSIM_ERR_CAPACITY
+    assert lib.lsim_mse_adc(None, V(16), V(16), V(16), V(16), 10, V(16), V(16), V(16), V(16), V(16), 10, 1.0, 1.0,
+                            out, None, None, ws, big, None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_nll_loss(V(16), V(16), V(16), V(16), V(16), V(16), 10, V(16), V(16), V(16), V(16), V(16), V(16),
+                             10, -1.0, out, None, None, None, ws, big, None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_nll_loss(V(16), V(16), V(16), V(16), V(16), V(16), 10, V(16), V(16), V(16), V(16), V(16), V(16),
+                             10, 1.0, out, None, None, None, ws, 8, None) == _abi.LSIM_ERR_CAPACITY
+    assert lib.lsim_chamfer_3d(V(16), V(16), V(16), V(16), V(16), 10, None, V(16), V(16), V(16), V(16), 10, out,
+                               None, None, ws, big, None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_chamfer_3d(V(16), V(16), V(16), V(16), V(16), 1 << 32, V(16), V(16), V(16), V(16), V(16), 10,
+                               out, None, None, ws, big, None) == _abi.LSIM_ERR_INVALID   # int32 neighbour indices
+    # waveform VJP and pixel coordinates
+    assert lib.lsim_lut_wfs_vjp(p, None, ws, 10, 1, V(16), 8, 4, V(16), None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_lut_wfs_vjp(p, V(16), ws, 10, 1, V(16), 2, 4, V(16), None) == _abi.LSIM_ERR_CAPACITY
+    assert lib.lsim_pixel_coords(p, None, 5, None, None, None, None, None) == _abi.LSIM_ERR_INVALID
