@@ -252,6 +252,20 @@ int lsim_lut_wfs_vjp(const LsimParams *p, const void *tables, const void *ws, in
 int lsim_fee(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, const float *normals,
              float *adc_out, float *tick_out, float *integral_out, void *stream);
 
+/* Workspace bytes of lsim_fee_vjp for n_pix pixel rows. */
+size_t lsim_fee_vjp_workspace_bytes(int64_t n_pix);
+
+/* Vector-Jacobian product of lsim_fee's ADCs with respect to the waveforms:
+ * for g_adc[n_pix][max_adc_values] = dL/dADC, writes g_wfs[n_pix][n_t] =
+ * dL/dwfs (n_t a multiple of 4, at most 2048).  The gradient treatment is
+ * the reference's under jax.vjp: crossing ticks, rejections and reset
+ * positions carry none, the reset clamp max(C - C[e2], 0) and the digitize
+ * clamps pass the cotangent where active (1/2 at exact ties).  normals
+ * (optional) are the noise draws of the forward.  Replaces the backward of
+ * get_adc_values + digitize, src/larndsim/fee_jax.py:55-71, :168-279. */
+int lsim_fee_vjp(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, const float *normals,
+                 const float *g_adc, float *g_wfs, void *ws, size_t ws_bytes, void *stream);
+
 /* Workspace bytes of lsim_hits for n_pix pixel rows. */
 size_t lsim_hits_workspace_bytes(int64_t n_pix, int32_t max_adc_values);
 

@@ -328,6 +328,22 @@ int lsim_fee(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, 
   return wrap(run_fee(*p, wfs, n_pix, n_t, normals, adc_out, tick_out, integral_out, (cudaStream_t)stream), "lsim_fee");
 }
 
+size_t lsim_fee_vjp_workspace_bytes(int64_t n_pix) { return n_pix < 0 ? 0 : fee_vjp_workspace_bytes(n_pix); }
+
+int lsim_fee_vjp(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, const float *normals,
+                 const float *g_adc, float *g_wfs, void *ws, size_t ws_bytes, void *stream) {
+  g_err.clear();
+  if (!p) return fail(LSIM_ERR_INVALID, "lsim_fee_vjp: null parameter block");
+  if (n_pix < 0 || (n_pix > 0 && (!wfs || !g_adc || !g_wfs))) return fail(LSIM_ERR_INVALID, "lsim_fee_vjp: null pointer");
+  if (p->max_adc_values < 1 || p->max_adc_values > LSIM_MAX_HITS)
+    return fail(LSIM_ERR_UNSUPPORTED, "lsim_fee_vjp: bad MAX_ADC_VALUES");
+  if (n_t < 4 || n_t > 2048 || n_t % 4 != 0)
+    return fail(LSIM_ERR_UNSUPPORTED, "lsim_fee_vjp: n_t %d must be a multiple of 4 up to 2048", n_t);
+  if (!ws || ws_bytes < fee_vjp_workspace_bytes(n_pix))
+    return fail(LSIM_ERR_CAPACITY, "lsim_fee_vjp: workspace %zu < %zu bytes", ws_bytes, fee_vjp_workspace_bytes(n_pix));
+  return wrap(run_fee_vjp(*p, wfs, n_pix, n_t, normals, g_adc, g_wfs, ws, (cudaStream_t)stream), "lsim_fee_vjp");
+}
+
 int lsim_pixel_coords(const LsimParams *p, const int32_t *unique_pixels, int64_t n_pix, float *x_out, float *y_out,
                       int32_t *plane_out, int32_t *event_out, void *stream) {
   g_err.clear();

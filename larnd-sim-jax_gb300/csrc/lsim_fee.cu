@@ -55,6 +55,61 @@ int run_fee(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, c
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------- FEE vector-Jacobian product
+
+// dL/dwfs of the front end + digitize for a cotangent on the ADCs: the
+// forward is recomputed per row (reset masks kept per warp in the
+// workspace), then the same adjoint the fused LUT gradient runs.
+__global__ void __launch_bounds__(kFeeWarps * kWarp)
+    k_fee_vjp(LsimParams p, const float *__restrict__ wfs, int64_t n_pix, int32_t T, const float *__restrict__ normals,
+              const float *__restrict__ g_adc, float *__restrict__ g_wfs, uint32_t *masks) {
+  __shared__ __align__(16) float rows[kFeeWarps][kFeeRow];
+  __shared__ FeeState fs[kFeeWarps];
+  __shared__ float gint[kFeeWarps][LSIM_MAX_HITS];
+  const int lane = threadIdx.x % kWarp, wid = threadIdx.x / kWarp;
+  float *C = rows[wid];
+  FeeState &st = fs[wid];
+  if (lane == 0) st.mask = masks + (size_t)(blockIdx.x * kFeeWarps + wid) * kFeeMaskWords;
+  __syncwarp();
+  const int H = p.max_adc_values;
+  const bool early_exit = normals == nullptr && p.threshold > 0.f;
+  for (int64_t r = (int64_t)blockIdx.x * kFeeWarps + wid; r < n_pix; r += (int64_t)gridDim.x * kFeeWarps) {
+    const float4 *s4 = reinterpret_cast<const float4 *>(wfs + r * (int64_t)T);
+    float4 *c4 = reinterpret_cast<float4 *>(C);
+    for (int i = lane; i < T / 4; i += kWarp) c4[i] = __ldg(s4 + i);
+    __syncwarp();
+    warp_cumsum_charge(C, T, p.t_sampling, lane);
+    const float *nrm = normals ? normals + r * (1 + 3 * H) : nullptr;
+    fee_forward(p, C, T, nrm, nullptr, nullptr, &st, nullptr, early_exit, lane);
+    __syncwarp();
+    if (lane < H) gint[wid][lane] = digitize_vjp(p, st.raw[lane], g_adc[r * H + lane]);
+    __syncwarp();
+    fee_backward(p, C, T, &st, gint[wid], lane);
+    float4 *d4 = reinterpret_cast<float4 *>(g_wfs + r * (int64_t)T);
+    for (int i = lane; i < T / 4; i += kWarp) d4[i] = c4[i];
+    __syncwarp();
+  }
+}
+
+constexpr int64_t kFeeVjpMaxWarps = 8192;
+
+size_t fee_vjp_workspace_bytes(int64_t n_pix) {
+  const int64_t warps = n_pix < kFeeVjpMaxWarps ? n_pix : kFeeVjpMaxWarps;
+  const int64_t blocks = (warps + kFeeWarps - 1) / kFeeWarps;
+  return (size_t)(blocks > 0 ? blocks : 1) * kFeeWarps * kFeeMaskWords * sizeof(uint32_t);
+}
+
+int run_fee_vjp(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, const float *normals,
+                const float *g_adc, float *g_wfs, void *ws, cudaStream_t st) {
+  if (n_t > kFeeRow || n_t < 4 || n_t % 4 != 0 || p.max_adc_values > LSIM_MAX_HITS) return LSIM_ERR_UNSUPPORTED;
+  if (n_pix <= 0) return LSIM_OK;
+  const int64_t warps = n_pix < kFeeVjpMaxWarps ? n_pix : kFeeVjpMaxWarps;
+  const int64_t blocks = (warps + kFeeWarps - 1) / kFeeWarps;
+  k_fee_vjp<<<(unsigned)blocks, kFeeWarps * kWarp, 0, st>>>(p, wfs, n_pix, n_t, normals, g_adc, g_wfs,
+                                                           static_cast<uint32_t *>(ws));
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
 // ---------------------------------------------------------------- hits
 
 struct PixelGeo {

@@ -89,6 +89,8 @@ _SIGNATURES = {
     "lsim_lut_grad_stored": (C.c_int, [_PP, _vp, _vp, _i64, _i32, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp]),
     "lsim_lut_wfs_vjp": (C.c_int, [_PP, _vp, _vp, _i64, _i32, _vp, _i64, _i32, _vp, _vp]),
     "lsim_fee": (C.c_int, [_PP, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp]),
+    "lsim_fee_vjp_workspace_bytes": (_sz, [_i64]),
+    "lsim_fee_vjp": (C.c_int, [_PP, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _sz, _vp]),
     "lsim_hits_workspace_bytes": (_sz, [_i64, _i32]),
     "lsim_hits": (C.c_int, [_PP, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz,
                             _vp]),

@@ -420,3 +420,49 @@ def simulate_probabilistic(params, wfs, unique_pixels):
     log_prob, charge = get_adc_values_average_noise_vmap(params, wfs)
     x, y, _, event = pixel_coordinates(params, unique_pixels)
     return digitize(params, charge), x, y, log_prob, event
+
+
+# ---------------------------------------------------------------- differentiable front end
+
+class _FeeFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, wfs, params, normals):
+        lib = _abi.load()
+        w = wfs.detach().to(dtype=torch.float32).contiguous()
+        P, T = w.shape
+        H = int(params.MAX_ADC_VALUES)
+        lp = _abi.make_params(params)
+        adc = torch.empty((P, H), dtype=torch.float32, device=w.device)
+        ticks = torch.empty((P, H), dtype=torch.float32, device=w.device)
+        _abi.check(lib, lib.lsim_fee(lp, _ptr(w), P, T, _ptr(normals), _ptr(adc), _ptr(ticks), None, _stream()))
+        ctx.save_for_backward(w)
+        ctx.lp, ctx.normals = lp, normals
+        ctx.mark_non_differentiable(ticks)
+        return adc, ticks
+
+    @staticmethod
+    def backward(ctx, g_adc, g_ticks):
+        (w,) = ctx.saved_tensors
+        lib = _abi.load()
+        P, T = w.shape
+        g = torch.zeros_like(w)
+        if g_adc is None:
+            return g, None, None
+        ga = g_adc.to(torch.float32).contiguous()
+        ws = torch.empty(lib.lsim_fee_vjp_workspace_bytes(P), dtype=torch.uint8, device=w.device)
+        _abi.check(lib, lib.lsim_fee_vjp(ctx.lp, _ptr(w), P, T, _ptr(ctx.normals), _ptr(ga), _ptr(g), _ptr(ws),
+                                         ws.numel(), _stream()))
+        return g, None, None
+
+
+def fee_adc(params, wfs, rngseed=0, normals=None):
+    """Self-trigger front end + digitize (fee_jax.py:55-71, :168-279) as a
+    differentiable function of the waveforms: (adc, ticks), each (P, H);
+    ``adc.backward(g)`` gives dL/dwfs with the reference's gradient
+    treatment (lsim_fee_vjp)."""
+    w = torch.as_tensor(wfs)
+    if not w.is_cuda:
+        w = w.to(device=_device())
+    w = w.to(torch.float32)
+    nrm = _noise_normals(params, w.shape[0], rngseed, normals)
+    return _FeeFn.apply(w, params, nrm)

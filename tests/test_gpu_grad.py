@@ -185,3 +185,49 @@ def test_wfs_vjp_matches_complex_step(cuda, case):
         tc[k] += 1e-30j
         g_cs[k] = float((G.waveforms64(fr, tc)[fr.valid] * cv).sum().imag / 1e-30)
     _check(g_gpu, g_cs, th)
+
+
+def test_fee_vjp_matches_fp64_front_end_adjoint(cuda):
+    """lsim_fee_vjp through sim.fee_adc: dL/dwfs for a random ADC cotangent,
+    against the float64 reverse-mode adjoint of the front end with its
+    decisions frozen (oracle fee_adjoint64)."""
+    from larndsim_gb300 import sim
+    from oracle import grad64 as G
+    p, tmpl, tracks, fields, chain, target = _setup(n_neighbors=2, seed=5, n_tracks=2, shower=300)
+    pp = _perturbed(p)
+    wfs, unique = chain.wfs(pp)
+    w = wfs[unique >= 0].contiguous().requires_grad_(True)
+    adc, ticks = sim.fee_adc(pp, w)
+    rng = np.random.default_rng(8)
+    g_adc = rng.standard_normal(tuple(adc.shape)).astype(np.float32)
+    (adc * torch.from_numpy(g_adc).cuda()).sum().backward()
+    fr = G.Frozen.__new__(G.Frozen)
+    fr.params = pp
+    fr._fee_decisions(w.detach().cpu().numpy())
+    # rows whose hit ticks agree on both sides (cumulative sums in another
+    # order can move a crossing that sits on the threshold by one tick)
+    T = w.shape[1]
+    same = np.all(ticks.cpu().numpy() == np.where(fr.cond, T - 2, fr.idx).astype(np.float32), axis=1)
+    assert same.mean() > 0.99 and same.sum() > 50
+    ref = G.fee_adjoint64(fr, g_adc.astype(np.float64))[same]
+    got = w.grad.cpu().numpy()[same]
+    assert np.abs(ref).max() > 0
+    np.testing.assert_allclose(got, ref, atol=1e-5 * np.abs(ref).max(), rtol=0)
+
+
+def test_modular_chain_equals_fused_gradient(cuda):
+    """wfs_fn -> fee_adc in torch autograd (waveforms materialised, two
+    vector-Jacobian products) gives the gradient the fused lsim_lut_grad
+    computes without storing waveforms, for the same ADC cotangent."""
+    from larndsim_gb300 import grad, sim
+    p, tmpl, tracks, fields, chain, target = _setup(n_neighbors=1, seed=9, n_tracks=3, shower=200)
+    pp = _perturbed(p)
+    theta = grad.theta_of(pp).requires_grad_(True)
+    wfs, unique = grad.wfs_fn(theta, chain, pp)
+    adc, _ = sim.fee_adc(pp, wfs[unique >= 0])
+    rng = np.random.default_rng(2)
+    c = torch.from_numpy(rng.standard_normal(tuple(adc.shape)).astype(np.float32)).cuda()
+    (adc * c).sum().backward()
+    g_mod = dict(zip(grad.GRAD_PARAMS, theta.grad.cpu().numpy().tolist()))
+    g_fused = dict(zip(grad.GRAD_PARAMS, chain.vjp(pp, c).cpu().numpy().tolist()))
+    _check(g_mod, g_fused, {k: float(getattr(pp, k)) for k in grad.GRAD_PARAMS})

@@ -218,3 +218,7 @@ def test_next_row_entry_points_reject_bad_arguments_without_gpu(lib):
     assert lib.lsim_lut_wfs_vjp(p, None, ws, 10, 1, V(16), 8, 4, V(16), None) == _abi.LSIM_ERR_INVALID
     assert lib.lsim_lut_wfs_vjp(p, V(16), ws, 10, 1, V(16), 2, 4, V(16), None) == _abi.LSIM_ERR_CAPACITY
     assert lib.lsim_pixel_coords(p, None, 5, None, None, None, None, None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_fee_vjp_workspace_bytes(100) >= 100 * 4 * 1024
+    assert lib.lsim_fee_vjp(p, V(16), 4, 2002, None, V(16), V(16), ws, big, None) == _abi.LSIM_ERR_UNSUPPORTED
+    assert lib.lsim_fee_vjp(p, V(16), 4, 2000, None, None, V(16), ws, big, None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_fee_vjp(p, V(16), 4, 2000, None, V(16), V(16), ws, 16, None) == _abi.LSIM_ERR_CAPACITY
