@@ -64,10 +64,11 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--events", type=int, default=N_EVENTS, help="events per batch (profiling runs use fewer)")
-    ap.add_argument("--path", choices=["grad", "chop", "prob", "loss"], default="grad",
+    ap.add_argument("--path", choices=["grad", "forward", "param", "chop", "prob", "loss"], default="grad",
                     help="grad: the fwd+bwd step (default); chop: on-device chop_tracks of one 500k-segment event; "
                          "prob: the probabilistic front end on the waveforms of 8 events; loss: mse_adc forward + "
-                         "gradient on the hits of the 64-event batch")
+                         "gradient on the hits of the 64-event batch; forward / param: the plain forward "
+                         "drop-in (LUT mode / parametrised mode) on the 64-event batch")
     return ap.parse_args()
 
 
@@ -581,6 +582,116 @@ def run_prob(args):
     print(json.dumps(rec), flush=True)
 
 
+# ---------------------------------------------------------------- plain forward
+
+def _timed(step, steps, warmup, flush):
+    import torch
+    for _ in range(warmup):
+        step()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    clocks = ClockSampler(torch.cuda.current_device())
+    torch.cuda.synchronize()
+    for i in range(steps):
+        flush.fill_(float(i))
+        starts[i].record()
+        step()
+        ends[i].record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    return float(np.mean([a.elapsed_time(b) for a, b in zip(starts, ends)])), clk
+
+
+def run_forward(args, param_mode=False):
+    """The plain forward drop-in on the 64-event batch: simulate_wfs +
+    simulate_stochastic (sim_jax.py:689-769), or simulate_parametrized
+    (sim_jax.py:339-372, n_neighbors = 0, Monte-Carlo diffusion offsets
+    supplied), through the public functions with the reference's host
+    synchronisation points.  LUT mode also reports the roofline of the
+    waveform kernel k_lut_pixels<wfs> (CUDA events around its launch)."""
+    import torch
+    from larndsim_gb300 import _abi, sim, workloads
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    tracks, fields = workload(0, args.seed)
+    n_seg = tracks.shape[0]
+    t_dev = torch.from_numpy(tracks).to(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    if param_mode:
+        params = nominal_params().replace(number_pix_neighbors=0, mc_diff=True)
+        offsets = sim.draw_offsets(n_seg, 7, dev)
+
+        def step(tr=t_dev, off=offsets):
+            return sim.simulate_parametrized(params, tr, fields, offsets=off)
+    else:
+        params = nominal_params()
+        tmpl, params = sim.load_lut(workloads.synthetic_response(seed=0), params)
+
+        def step(tr=t_dev):
+            wfs, unique = sim.simulate_wfs(params, tmpl, tr, fields)
+            return sim.simulate_stochastic(params, wfs, unique), wfs, unique
+    ms, clk = _timed(step, args.steps, args.warmup, flush)
+    rec = {"metric": "forward segments/s", "value": n_seg / (ms * 1e-3), "unit": "segments/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tracks and LUT)",
+           "config": {"workload": ("simulate_parametrized (n_neighbors=0, mc_diff offsets supplied)" if param_mode
+                                   else "simulate_wfs + simulate_stochastic (n_neighbors=4, L=150, "
+                                        "100x45x45x1950 templates)") +
+                                  f" on the 64-event batch ({n_seg} segments), noise off",
+                      "segments": n_seg, "l2": "flushed between timed steps (512 MiB write)",
+                      "step": "public functions, eager, with the reference's device-to-host syncs"},
+           "clocks": clk}
+    host = torch.from_numpy(tracks).pin_memory()
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(e2e_steps):
+        if param_mode:
+            out = step(host.to(dev, non_blocking=True), offsets)
+        else:
+            out = step(host.to(dev, non_blocking=True))[0]
+        cpu = [o.cpu() for o in out]
+        d2h = sum(c.numel() * 4 for c in cpu)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    rec["e2e"] = {"value": n_seg / e2e_s, "unit": "segments/s", "ms_per_step": e2e_s * 1e3,
+                  "h2d_bytes_per_step": int(tracks.nbytes), "d2h_bytes_per_step": int(d2h)}
+    if not param_mode:
+        kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+        for e in kev:
+            flush.fill_(1.0)
+            _abi.set_kernel_events(*e)
+            _, wfs, unique = step()
+        torch.cuda.synchronize()
+        _abi.set_kernel_events(None, None)
+        k_ms = float(np.mean([a.elapsed_time(b) for a, b in kev]))
+        n_valid = int((unique >= 0).sum())
+        T = wfs.shape[1]
+        # the waveform kernel's share of the fixed forward formula: the rows it
+        # writes (4 T P), their pixel ids (8 P) and the distinct LUT floats
+        from larndsim_gb300 import grad
+        chain = grad.LUTChain(params, tmpl, tracks, fields)
+        st = chain.stage1(params)
+        seg_rec = st.ws[256:256 + 96 * n_seg].view(torch.int32).view(n_seg, 24).cpu().numpy()
+        ne = seg_rec[:, 0].view(np.float32)
+        lut = chain.lut
+        w_lut = lut_bytes_touched(seg_rec[ne > 0, 6], lut.n_templates, lut.shape[1], lut.shape[2], SIG_LEN,
+                                  lut.shape[3])
+        algo = 4 * T * n_valid + 8 * n_valid + 4 * w_lut
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        peak = peaks.get("hbm_gbs", 6800.0)
+        achieved = algo / (k_ms * 1e-3) / 1e9
+        rec["roofline"] = {"bound": "hbm", "kernel": "k_lut_pixels<wfs> (pixel-major waveform accumulation)",
+                           "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                           "algorithmic_bytes": int(algo), "kernel_ms": k_ms, "pixels": n_valid,
+                           "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None}
+    rec["gpu_launches"] = None
+    print(json.dumps(rec), flush=True)
+
+
 # ---------------------------------------------------------------- hit-level fit loss
 
 def run_loss(args):
@@ -700,6 +811,13 @@ def run_chop_reference(args):
 
 def main():
     args = parse()
+    if args.path in ("forward", "param"):
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "forward paths: the reference arm of the "
+                                                                  "default path times the CPU restatement"}))
+        else:
+            run_forward(args, param_mode=args.path == "param")
+        return
     if args.path == "loss":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "loss path: its CPU arm is the cpu_baseline of "
