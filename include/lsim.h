@@ -404,7 +404,10 @@ int lsim_chamfer_3d(const float *x, const float *y, const float *z, const int32_
 /* Stage 1 of simulate_parametrized: shift, quench, drift, Monte-Carlo
  * diffusion offsets (normals [n_rows][3], supplied), pixel of each
  * electron, pixel map.  Replaces simulate_drift + generate_electrons +
- * get_pixels, src/larndsim/sim_jax.py:122-139, src/larndsim/detsim_jax.py:376-400, :477-491. */
+ * get_pixels, src/larndsim/sim_jax.py:122-139, src/larndsim/detsim_jax.py:376-400, :477-491.
+ * Implements the reference's default current model with longitudinal
+ * smearing (diffusion_in_current_sim = true, current_model_diff); false
+ * returns LSIM_ERR_UNSUPPORTED. */
 int lsim_param_stage1(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,
                       int32_t n_events, const float *normals, void *ws, size_t ws_bytes,
                       LsimCounts *counts_dev, void *stream);

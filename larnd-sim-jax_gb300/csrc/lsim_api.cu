@@ -197,6 +197,10 @@ int lsim_adam_step(float *theta_dev, const float *grad_dev, const float *scale_d
 int lsim_param_stage1(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,
                       int32_t n_events, const float *normals, void *ws, size_t ws_bytes, LsimCounts *counts_dev,
                       void *stream) {
+  g_err.clear();
+  if (p && !p->diffusion_in_current_sim)
+    return fail(LSIM_ERR_UNSUPPORTED, "lsim_param_stage1: diffusion_in_current_sim = false (current_model without "
+                                      "longitudinal smearing) is not implemented");
   return stage1(true, p, f, tracks, n_rows, n_events, normals, ws, ws_bytes, counts_dev, stream, "lsim_param_stage1");
 }
 

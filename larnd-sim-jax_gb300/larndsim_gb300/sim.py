@@ -319,6 +319,9 @@ def simulate_parametrized_wfs(params, tracks, fields, rngseed=0, offsets=None):
     if not params.mc_diff:
         raise ValueError("parametrised mode needs mc_diff=True: the reference's deterministic branch "
                          "(apply_tran_diff) requires tran_diff_bin_edges, which it never sets")
+    if not params.diffusion_in_current_sim:
+        raise NotImplementedError("diffusion_in_current_sim=False (current_model, detsim_jax.py:545-579) is not "
+                                  "implemented; the default True (current_model_diff) is")
     st = run_stage1(params, t, fields, lp, param_mode=True, normals=nrm)
     st.raise_status()
     p_unique = st.n_em1 + st.n_valid + st.any_m1
