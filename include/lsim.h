@@ -420,6 +420,18 @@ int lsim_param_stage2(const LsimParams *p, const void *ws, int64_t n_rows, int32
                       int64_t p_pad, int32_t n_em1, int32_t n_valid, float *wfs, int32_t *unique_pixels,
                       void *stream);
 
+/* Vector-Jacobian product of simulate_parametrized's waveforms: for a
+ * cotangent g_wfs on the rows lsim_param_stage2 writes ([p_pad][n_ticks - 1],
+ * the n_valid valid rows last), dL/dtheta into grad_out[LSIM_NPARAM].  ws
+ * holds the lsim_param_stage1 state at the parameters (including the
+ * per-segment partial derivatives it records); the Monte-Carlo offsets are
+ * held fixed and pixel and tick assignments carry no gradient, as under
+ * jax.grad of simulate_parametrized (src/larndsim/sim_jax.py:339-372,
+ * src/larndsim/detsim_jax.py:581-639; the gradient params_loss_parametrized
+ * takes in optimize/fit_params.py). */
+int lsim_param_wfs_vjp(const LsimParams *p, const void *ws, int64_t n_rows, int32_t n_events, const float *g_wfs,
+                       int64_t p_pad, int32_t n_valid, float *grad_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -501,4 +501,19 @@ int lsim_param_stage2(const LsimParams *p, const void *ws, int64_t n_rows, int32
   return wrap(run_param_accum(*p, a.w, a.g, n_valid, p_pad - n_valid, wfs, st), "lsim_param_stage2");
 }
 
+int lsim_param_wfs_vjp(const LsimParams *p, const void *ws, int64_t n_rows, int32_t n_events, const float *g_wfs,
+                       int64_t p_pad, int32_t n_valid, float *grad_out, void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (!ws || !grad_out || (n_valid > 0 && !g_wfs)) return fail(LSIM_ERR_INVALID, "lsim_param_wfs_vjp: null pointer");
+  if (n_valid < 0 || p_pad < n_valid) return fail(LSIM_ERR_CAPACITY, "lsim_param_wfs_vjp: p_pad < n_valid");
+  cudaStream_t st = (cudaStream_t)stream;
+  AccumArgs a = make_args(p, nullptr, ws, n_rows, n_events);
+  a.n_valid = n_valid;
+  rc = run_param_vjp(*p, a.w, a.g, n_valid, p_pad - n_valid, g_wfs, n_rows, st);
+  if (rc) return wrap(rc, "lsim_param_wfs_vjp");
+  return wrap(run_grad_finalize(a, nullptr, grad_out, st), "lsim_param_wfs_vjp");
+}
+
 }  // extern "C"

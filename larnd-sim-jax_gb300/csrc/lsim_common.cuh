@@ -62,6 +62,18 @@ struct __align__(16) SegPar {
   float pad[6];
 };
 
+// Per-segment adjoint record of parametrised mode, stored in the SegAdj
+// slot: the non-zero partial derivatives of the current model's inputs.
+struct __align__(16) SegParAdj {
+  float dne[5];      // d ne / d(Ab, kb, eField, lifetime, lArDensity)
+  float dxd[2];      // d x_dist / d(eField, tran_diff)
+  float dyd[2];      // d y_dist / d(eField, tran_diff)
+  float dt0f[2];     // d t0f / d(eField, long_diff)
+  float dsig[2];     // d sigma / d(eField, long_diff)
+  float pad[11];
+};
+static_assert(sizeof(SegParAdj) <= sizeof(SegAdj), "parametrised adjoint record fits the SegAdj slot");
+
 // --------------------------------------------------------------- layout
 
 struct Grid {

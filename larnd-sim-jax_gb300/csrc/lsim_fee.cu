@@ -368,6 +368,196 @@ __global__ void __launch_bounds__(kParWarps * kWarp)
   }
 }
 
+// ---------------------------------------------------------------- parametrised adjoint
+// Forward-mode derivatives of the current model with respect to its four
+// continuous inputs (x_dist, y_dist, t0f, sigma), carried as dual numbers
+// through the same expressions as the forward (so the window
+// normalisation, which couples all 51 ticks, is differentiated exactly).
+
+struct Dual {
+  float v, d[4];
+};
+
+__device__ __forceinline__ Dual dconst(float c) { return Dual{c, {0.f, 0.f, 0.f, 0.f}}; }
+__device__ __forceinline__ Dual dseed(float c, int i) {
+  Dual r = dconst(c);
+  r.d[i] = 1.f;
+  return r;
+}
+__device__ __forceinline__ Dual operator+(const Dual &a, const Dual &b) {
+  return Dual{a.v + b.v, {a.d[0] + b.d[0], a.d[1] + b.d[1], a.d[2] + b.d[2], a.d[3] + b.d[3]}};
+}
+__device__ __forceinline__ Dual operator-(const Dual &a, const Dual &b) {
+  return Dual{a.v - b.v, {a.d[0] - b.d[0], a.d[1] - b.d[1], a.d[2] - b.d[2], a.d[3] - b.d[3]}};
+}
+__device__ __forceinline__ Dual operator*(const Dual &a, const Dual &b) {
+  Dual r;
+  r.v = a.v * b.v;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+__device__ __forceinline__ Dual operator*(float c, const Dual &a) {
+  return Dual{c * a.v, {c * a.d[0], c * a.d[1], c * a.d[2], c * a.d[3]}};
+}
+__device__ __forceinline__ Dual operator/(const Dual &a, const Dual &b) {
+  Dual r;
+  r.v = a.v / b.v;
+  const float ib = 1.f / b.v;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  return r;
+}
+__device__ __forceinline__ Dual chain(float v, float dv, const Dual &a) {
+  return Dual{v, {dv * a.d[0], dv * a.d[1], dv * a.d[2], dv * a.d[3]}};
+}
+__device__ __forceinline__ Dual dexp(const Dual &a) {
+  const float e = expf(a.v);
+  return chain(e, e, a);
+}
+// erf' = 2/sqrt(pi) exp(-x^2), erfc' = -erf'
+__device__ __forceinline__ Dual derf(const Dual &a) {
+  return chain(erff(a.v), 1.12837916709551257f * expf(-a.v * a.v), a);
+}
+__device__ __forceinline__ Dual derfc(const Dual &a) {
+  return chain(erfcf(a.v), -1.12837916709551257f * expf(-a.v * a.v), a);
+}
+
+__device__ __forceinline__ Dual ied_edge_d(float x, const Dual &loc, const Dual &diff, const Dual &lambd) {
+  const float s2 = 1.41421356237309515f;
+  const Dual sd = s2 * diff;
+  const Dual e = 0.5f * derf((dconst(x) - loc) / sd);
+  const Dual coeff = 0.5f * lambd;
+  const Dual ls2 = lambd * (diff * diff);
+  const Dual expo = coeff * (((2.f * loc) + ls2) - dconst(2.f * x));
+  const Dual pdf = (coeff * dexp(expo)) * derfc(((loc + ls2) - dconst(x)) / sd);
+  return e - pdf / lambd;
+}
+
+__device__ __forceinline__ Dual quad_d(const float c[6], const Dual &x, const Dual &y) {
+  return ((((dconst(c[0]) + c[1] * x) + c[2] * y) + (c[3] * x) * y) + (c[4] * x) * x) + (c[5] * y) * y;
+}
+
+struct ParamShapeD {
+  Dual a, lam_b, lam_c, loc, diff, norm_b, norm_c;
+};
+
+__device__ __forceinline__ ParamShapeD param_shape_d(const LsimParams &p, const SegPar &s) {
+  const float B[6] = {1.060f, -0.909f, -0.909f, 5.856f, 0.207f, 0.207f};
+  const float C[6] = {0.679f, -1.083f, -1.083f, 8.772f, -5.521f, -5.521f};
+  const float D[6] = {2.644f, -9.174f, -9.174f, 13.483f, 45.887f, 45.887f};
+  const float T0[6] = {2.948f, -2.705f, -2.705f, 4.825f, 20.814f, 20.814f};
+  const Dual x = dseed(s.xd, 0), y = dseed(s.yd, 1), t0f = dseed(s.t0f, 2);
+  ParamShapeD sh;
+  Dual a = quad_d(B, x, y);
+  // jnp.minimum(a, 1): the derivative passes below 1, half of it at a tie
+  if (a.v > 1.f) a = dconst(1.f);
+  else if (a.v == 1.f) a = Dual{1.f, {0.5f * a.d[0], 0.5f * a.d[1], 0.5f * a.d[2], 0.5f * a.d[3]}};
+  sh.a = a;
+  const Dual b = quad_d(C, x, y), c = quad_d(D, x, y);
+  const Dual st0 = t0f + quad_d(T0, x, y);
+  sh.loc = dconst(0.f) - st0;
+  sh.diff = dseed(s.sigma, 3);
+  sh.lam_b = dconst(1.f) / b;
+  sh.lam_c = dconst(1.f) / c;
+  const int n = p.param_nticks;
+  const float hd = p.param_dt * 0.5f;
+  const float x0 = -p.param_ticks[0], xl = -p.param_ticks[n - 1];
+  sh.norm_b = ied_edge_d(x0 - hd, sh.loc, sh.diff, sh.lam_b) - ied_edge_d(xl + hd, sh.loc, sh.diff, sh.lam_b);
+  sh.norm_c = ied_edge_d(x0 - hd, sh.loc, sh.diff, sh.lam_c) - ied_edge_d(xl + hd, sh.loc, sh.diff, sh.lam_c);
+  return sh;
+}
+
+__device__ __forceinline__ Dual param_value_d(const LsimParams &p, const ParamShapeD &sh, int k) {
+  const float x = -p.param_ticks[k];
+  const float hd = p.param_dt * 0.5f;
+  const float idt = 1.f / p.param_dt;
+  const Dual ub = ied_edge_d(x + hd, sh.loc, sh.diff, sh.lam_b), lb = ied_edge_d(x - hd, sh.loc, sh.diff, sh.lam_b);
+  const Dual uc = ied_edge_d(x + hd, sh.loc, sh.diff, sh.lam_c), lc = ied_edge_d(x - hd, sh.loc, sh.diff, sh.lam_c);
+  const Dual vb = idt * ((ub - lb) / sh.norm_b);
+  const Dual vc = idt * ((uc - lc) / sh.norm_c);
+  return sh.a * vb + (dconst(1.f) - sh.a) * vc;
+}
+
+// dL/dtheta per pixel for a waveform cotangent g_wfs (rows as stage 2
+// writes them): per segment the cotangent of its 51 current samples,
+// folded into d/d(ne, x_dist, y_dist, t0f, sigma) and projected through the
+// segment's SegParAdj record.
+__global__ void __launch_bounds__(kParWarps * kWarp)
+    k_param_vjp(LsimParams p, Workspace w, Grid g, int64_t row_offset, const float *__restrict__ g_wfs) {
+  __shared__ __align__(16) float rows[kParWarps][2052];
+  const int lane = threadIdx.x % kWarp, wid = threadIdx.x / kWarp;
+  float *row = rows[wid] + 3;   // col 1 16-byte aligned
+  const int NT = p.n_ticks, T = NT - 1;
+  const int n = p.param_nticks;
+  const int n_valid = w.counts->n_valid;
+  for (;;) {
+    int r = 0;
+    if (lane == 0) r = atomicAdd(&w.counts->work, 1);
+    r = __shfl_sync(0xffffffffu, r, 0);
+    if (r >= n_valid) break;
+    const int64_t slot = w.pix_slot[r];
+    const float4 *src = reinterpret_cast<const float4 *>(g_wfs + (row_offset + r) * (int64_t)T);
+    float4 *dst = reinterpret_cast<float4 *>(row + 1);
+    for (int i = lane; i < T / 4; i += kWarp) dst[i] = __ldg(src + i);
+    if (lane == 0) row[0] = 0.f;   // the garbage column carries no gradient
+    __syncwarp();
+    float th[LSIM_NPARAM];
+#pragma unroll
+    for (int i = 0; i < LSIM_NPARAM; ++i) th[i] = 0.f;
+    const int c = w.cnt[slot], o = w.off[slot];
+    for (int j = 0; j < c; ++j) {
+      const int s = w.seg_list[o + j];
+      const SegPar sp = w.segp[s];
+      if (sp.ne == 0.f) continue;
+      const ParamShapeD sh = param_shape_d(p, sp);
+      const int start = sp.t0_tick - n;
+      float gne = 0.f, gq[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int k = lane; k < n; k += kWarp) {
+        const int tt = start + k;
+        const float gk = (tt >= 0 && tt < NT - 1) ? row[tt + 1] : 0.f;
+        if (gk != 0.f) {
+          const Dual v = param_value_d(p, sh, k);
+          gne += gk * v.v;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) gq[q] += gk * sp.ne * v.d[q];
+        }
+      }
+      gne = warp_sum(gne);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) gq[q] = warp_sum(gq[q]);
+      const SegParAdj ja = *reinterpret_cast<const SegParAdj *>(w.sega + s);
+      // order: Ab kb eField lifetime vdrift long_diff tran_diff lArDensity
+      th[0] += gne * ja.dne[0];
+      th[1] += gne * ja.dne[1];
+      th[2] += gne * ja.dne[2] + gq[0] * ja.dxd[0] + gq[1] * ja.dyd[0] + gq[2] * ja.dt0f[0] + gq[3] * ja.dsig[0];
+      th[3] += gne * ja.dne[3];
+      th[5] += gq[2] * ja.dt0f[1] + gq[3] * ja.dsig[1];
+      th[6] += gq[0] * ja.dxd[1] + gq[1] * ja.dyd[1];
+      th[7] += gne * ja.dne[4];
+    }
+    if (lane == 0) {
+      float *out = w.pix_out + (size_t)r * kPixRec;
+      out[0] = 0.f;
+#pragma unroll
+      for (int i = 0; i < LSIM_NPARAM; ++i) out[1 + i] = th[i];
+    }
+    __syncwarp();
+  }
+}
+
+int run_param_vjp(const LsimParams &p, const Workspace &w, const Grid &g, int32_t n_valid, int64_t row_offset,
+                  const float *g_wfs, int64_t n_rows, cudaStream_t st) {
+  if (p.n_ticks - 1 > 2048 || (p.n_ticks - 1) % 4 != 0 || p.param_nticks > 64) return LSIM_ERR_UNSUPPORTED;
+  if (cudaMemsetAsync(&w.counts->work, 0, sizeof(int32_t), st) != cudaSuccess) return LSIM_ERR_CUDA;
+  // no main-bin records in this mode: their adjoint partials are zero
+  if (n_rows > 0 && cudaMemsetAsync(w.main_out, 0, sizeof(float) * kPixRec * (size_t)n_rows, st) != cudaSuccess)
+    return LSIM_ERR_CUDA;
+  int blocks = device_sm_count() * 4;
+  k_param_vjp<<<blocks, kParWarps * kWarp, 0, st>>>(p, w, g, row_offset, g_wfs);
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
 int run_param_accum(const LsimParams &p, const Workspace &w, const Grid &g, int32_t n_valid, int64_t row_offset,
                     float *wfs, cudaStream_t st) {
   if (p.n_ticks - 1 > 2048 || (p.n_ticks - 1) % 4 != 0 || p.param_nticks > 64) return LSIM_ERR_UNSUPPORTED;

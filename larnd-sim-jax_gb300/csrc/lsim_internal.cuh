@@ -57,6 +57,8 @@ int run_build_templates(const float *response, int nx, int ny, int nt, const flo
                         int extent, float *out, cudaStream_t st);
 int run_prepare_tables(const LsimParams &p, const float *templates, void *tables, cudaStream_t st);
 
+int run_param_vjp(const LsimParams &p, const Workspace &w, const Grid &g, int32_t n_valid, int64_t row_offset,
+                  const float *g_wfs, int64_t n_rows, cudaStream_t st);
 size_t fee_vjp_workspace_bytes(int64_t n_pix);
 int run_fee_vjp(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, const float *normals,
                 const float *g_adc, float *g_wfs, void *ws, cudaStream_t st);

@@ -329,6 +329,37 @@ __global__ void k_segments_param(LsimParams p, LsimFieldMap f, const float *__re
   r.py = py;
   for (int i = 0; i < 6; ++i) r.pad[i] = 0.f;
   w.segp[s] = r;
+  // ---- adjoint partials (the current model's inputs; parameter order as in LUT mode)
+  {
+    const float dv = ph.dvdrift;
+    const float dtdE = -tdr * dv / v;
+    const float k = t.dE * p.mev_to_electrons * red * (mask ? 1.0f : 0.0f);
+    SegParAdj ja;
+    ja.dne[0] = dR[0] * k;
+    ja.dne[1] = dR[1] * k;
+    ja.dne[2] = dR[2] * k + ne * (-1.0f / ph.lifetime) * dtdE;
+    ja.dne[3] = ne * tdr / (ph.lifetime * ph.lifetime);
+    ja.dne[4] = dR[3] * k;
+    const float dsT_E = sigT > 0.f ? (ph.tran_diff / sigT) * dtdE : 0.f;
+    const float dsT_D = sigT > 0.f ? tdr / sigT : 0.f;
+    const float dsL_E = sigL > 0.f ? (ph.long_diff / sigL) * dtdE : 0.f;
+    const float dsL_D = sigL > 0.f ? tdr / sigL : 0.f;
+    // |u| passes sign(u) (0 at 0, as jnp.abs)
+    const float ux = xe - pcx, uy = ye - pcy;
+    const float sx = ux > 0.f ? 1.f : (ux < 0.f ? -1.f : 0.f);
+    const float sy = uy > 0.f ? 1.f : (uy < 0.f ? -1.f : 0.f);
+    ja.dxd[0] = sx * nx * dsT_E;
+    ja.dxd[1] = sx * nx * dsT_D;
+    ja.dyd[0] = sy * ny * dsT_E;
+    ja.dyd[1] = sy * ny * dsT_D;
+    // t0 = |z - z_anode| / v (z carries no offset with the smeared current model)
+    ja.dt0f[0] = -t0 * dv / v;
+    ja.dt0f[1] = 0.f;
+    ja.dsig[0] = dsL_E / v - sigL * dv / (v * v);
+    ja.dsig[1] = dsL_D / v;
+    for (int i = 0; i < 11; ++i) ja.pad[i] = 0.f;
+    *reinterpret_cast<SegParAdj *>(w.sega + s) = ja;
+  }
   w.pid[s] = pid;
   if (pid == -1) atomicExch(&w.counts->any_m1, 1);
   int32_t key = -1;

@@ -111,6 +111,7 @@ _SIGNATURES = {
     "lsim_chop_workspace_bytes": (_sz, [_i64]),
     "lsim_chop_tracks": (C.c_int, [_PF, _vp, _i64, C.c_double, _vp, _i64, _vp, _vp, _sz, _vp]),
     "lsim_param_stage1": (C.c_int, [_PP, _PF, _vp, _i64, _i32, _vp, _vp, _sz, _vp, _vp]),
+    "lsim_param_wfs_vjp": (C.c_int, [_PP, _vp, _i64, _i32, _vp, _i64, _i32, _vp, _vp]),
     "lsim_param_stage2": (C.c_int, [_PP, _vp, _i64, _i32, _i64, _i32, _i32, _vp, _vp, _vp]),
 }
 

@@ -469,3 +469,56 @@ def fee_adc(params, wfs, rngseed=0, normals=None):
     w = w.to(torch.float32)
     nrm = _noise_normals(params, w.shape[0], rngseed, normals)
     return _FeeFn.apply(w, params, nrm)
+
+
+# ---------------------------------------------------------------- differentiable parametrised mode
+
+class _ParamWfsFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, theta, params, tracks, fields, offsets):
+        from .grad import GRAD_PARAMS
+        vals = theta.detach().cpu().numpy().astype(np.float64)
+        p = params.replace(**{k: float(v) for k, v in zip(GRAD_PARAMS, vals)})
+        lp = _abi.make_params(p)
+        st = run_stage1(p, tracks, fields, lp, param_mode=True, normals=offsets)
+        st.raise_status()
+        p_unique = st.n_em1 + st.n_valid + st.any_m1
+        p_pad = pad_size(p_unique, "unique_pixels")
+        lib = _abi.load()
+        T = lp.n_ticks - 1
+        wfs = torch.empty((p_pad, T), dtype=torch.float32, device=st.tracks.device)
+        unique = torch.empty((p_pad,), dtype=torch.int32, device=st.tracks.device)
+        _abi.check(lib, lib.lsim_param_stage2(lp, _ptr(st.ws), st.n_rows, st.n_events, p_pad, st.n_em1, st.n_valid,
+                                              _ptr(wfs), _ptr(unique), _stream()))
+        ctx.st, ctx.lp = st, lp
+        ctx.theta_device, ctx.theta_dtype = theta.device, theta.dtype
+        ctx.mark_non_differentiable(unique)
+        return wfs, unique
+
+    @staticmethod
+    def backward(ctx, g_wfs, g_unique):
+        if g_wfs is None:
+            return (None,) * 5
+        lib = _abi.load()
+        st = ctx.st
+        g = g_wfs.to(dtype=torch.float32).contiguous()
+        out = torch.empty(_abi.NPARAM, dtype=torch.float32, device=g.device)
+        _abi.check(lib, lib.lsim_param_wfs_vjp(ctx.lp, _ptr(st.ws), st.n_rows, st.n_events, _ptr(g), g.shape[0],
+                                               st.n_valid, _ptr(out), _stream()))
+        return out.to(device=ctx.theta_device, dtype=ctx.theta_dtype), None, None, None, None
+
+
+def param_wfs_fn(theta, params, tracks, fields, offsets):
+    """Differentiable parametrised-mode waveforms (simulate_parametrized's
+    signal stage, sim_jax.py:339-368) as a function of ``theta`` = the 8
+    parameter values (order grad.GRAD_PARAMS), with the Monte-Carlo
+    diffusion offsets (N, 3) held fixed: returns (wfs, unique_pixels);
+    backward runs lsim_param_wfs_vjp.  Compose with fee_adc for the ADCs."""
+    if int(params.number_pix_neighbors) != 0:
+        raise ValueError("parametrised mode requires number_pix_neighbors == 0")
+    if not params.mc_diff or not params.diffusion_in_current_sim:
+        raise NotImplementedError("the differentiable parametrised mode covers mc_diff=True with "
+                                  "diffusion_in_current_sim=True")
+    t = as_tracks(tracks)
+    off = torch.as_tensor(offsets).to(device=t.device, dtype=torch.float32).contiguous()
+    return _ParamWfsFn.apply(theta, params, t, tuple(fields), off)

@@ -433,3 +433,102 @@ def adjoint64(fr: Frozen, th: dict, g_adc=None):
     A_t0 = A_fr / p.t_sampling
     J = _jacobian(fr, th)
     return {k: float((A_ne * J[k][0] + A_sig * J[k][1] + A_ld * J[k][2] + A_t0 * J[k][3]).sum()) for k in GRAD_PARAMS}
+
+
+# ---------------------------------------------------------------- parametrised mode
+
+def param_waveforms64(params, tracks, fields, normals, th: dict, frozen=None):
+    """Parametrised-mode waveforms (sim_jax.py:122-139, :289-335;
+    detsim_jax.py:376-400, :440-474, :581-639, :207-228) in float64 / complex
+    (complex-step ready), with the discrete decisions of the float32
+    forward frozen: TPC plane and mask, electron pixel, t0 tick, the
+    min(a, 1) branch.  Returns (W (P_valid, T), frozen, valid pixel ids)."""
+    p = params
+    f = tuple(fields)
+    cplx = any(isinstance(v, complex) for v in th.values())
+    dt = np.complex128 if cplx else np.float64
+    sh = R.shift_tracks(p, tracks, f)
+    x = sh[:, f.index("x")].astype(np.float64)
+    y = sh[:, f.index("y")].astype(np.float64)
+    z = sh[:, f.index("z")].astype(np.float64)
+    dE = sh[:, f.index("dE")].astype(np.float64)
+    dEdx = sh[:, f.index("dEdx")].astype(np.float64)
+    nrm = np.asarray(normals, np.float64)
+    if frozen is None:
+        mask, plane = R.tpc_membership(p, sh[:, f.index("x")], sh[:, f.index("y")], sh[:, f.index("z")])
+        # float32 forward for the decisions
+        t32 = R.drift(p, R.quench(p, sh, f), f)
+        e32 = R.generate_electrons(p, t32, f, normals)
+        pids = R.get_pixels(p, e32, f).ravel()
+        xp, yp, pl, _ = R.id2pixel(p, pids)
+        coords = R.get_pixel_coordinates(p, xp, yp, pl)
+        t0_tick, _ = R.current_mc(p, e32, coords, f)
+        ev = sh[:, f.index("eventID")].astype(int)
+        valid = np.unique(pids[(pids >= 0)])
+        frozen = dict(mask=mask.astype(np.float64), plane=plane, pids=pids, coords=coords.astype(np.float64),
+                      t0_tick=t0_tick, valid=valid, ev=ev)
+    fr = frozen
+    E, rho = th["eField"], th["lArDensity"]
+    Rb = th["Ab"] / (1 + th["kb"] * dEdx / (E * rho))                          # quenching_jax.py:23-25
+    ne0 = Rb * dE * p.MeVToElectrons
+    b = np.asarray(p.tpc_borders, np.float32)[fr["plane"]]
+    za = b[:, 2, 0].astype(np.float64)
+    dist = np.abs(z - za) + 1e-6
+    v = vdrift64(p, E)
+    tdr = dist / v
+    ne = ne0 * np.exp(-tdr / th["lifetime"]) * fr["mask"]
+    sT = np.sqrt(2 * tdr * th["tran_diff"])
+    sL = np.sqrt(2 * tdr * th["long_diff"])
+    xe = x + nrm[:, 0] * sT
+    ye = y + nrm[:, 1] * sT
+    ux = xe - fr["coords"][:, 0]
+    uy = ye - fr["coords"][:, 1]
+    xd = np.sign(np.real(ux)) * ux
+    yd = np.sign(np.real(uy)) * uy
+    uz = z - za
+    t0 = np.sign(uz) * uz / v
+    t0f = t0 - fr["t0_tick"] * p.t_sampling
+    sig = sL / v
+    nt = int(5 / p.t_sampling) + 1
+    tk = R.jax_linspace_f32(0, 5, nt).astype(np.float64)
+    dts = 5.0 / (nt - 1)
+    Bp = (1.060, -0.909, -0.909, 5.856, 0.207, 0.207)
+    Cp = (0.679, -1.083, -1.083, 8.772, -5.521, -5.521)
+    Dp = (2.644, -9.174, -9.174, 13.483, 45.887, 45.887)
+    Tp = (2.948, -2.705, -2.705, 4.825, 20.814, 20.814)
+
+    def quad(c):
+        return c[0] + c[1] * xd + c[2] * yd + c[3] * xd * yd + c[4] * xd * xd + c[5] * yd * yd
+
+    a = quad(Bp)
+    a = np.where(np.real(a) < 1, a, 1.0)
+    bq, cq = quad(Cp), quad(Dp)
+    st0 = t0f + quad(Tp)
+
+    def ied(xx, loc, scale, diff):
+        lam = 1 / scale
+        coeff = lam / 2
+        expo = coeff * (2 * loc + lam * diff ** 2 - 2 * xx)
+        pdf = coeff * np.exp(expo) * special.erfc((loc + lam * diff ** 2 - xx) / (np.sqrt(2) * diff))
+        return 0.5 * special.erf((xx - loc) / (np.sqrt(2) * diff)) - pdf / lam
+
+    X = -tk[None, :]
+    loc = (-st0)[:, None]
+    dd = sig[:, None]
+
+    def shape(scale):
+        up = ied(X + dts / 2, loc, scale[:, None], dd)
+        lo = ied(X - dts / 2, loc, scale[:, None], dd)
+        return (up - lo) / (lo[:, :1] - up[:, -1:]) / dts
+
+    cur = (a[:, None] * shape(bq) + (1 - a[:, None]) * shape(cq)) * ne[:, None]
+    Nt = R.n_ticks(p)
+    start = fr["t0_tick"] - nt
+    tt = start[:, None] + np.arange(nt)[None, :]
+    col = np.where((tt < 0) | (tt >= Nt - 1), 0, tt + 1)
+    rows = np.searchsorted(fr["valid"], fr["pids"])
+    ok = (fr["pids"] >= 0) & (rows < len(fr["valid"]))
+    W = np.zeros((len(fr["valid"]), Nt), dtype=dt)
+    for s in np.nonzero(ok)[0]:
+        np.add.at(W[rows[s]], col[s], cur[s])
+    return W[:, 1:], frozen, fr["valid"]
