@@ -64,11 +64,14 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--events", type=int, default=N_EVENTS, help="events per batch (profiling runs use fewer)")
-    ap.add_argument("--path", choices=["grad", "forward", "param", "chop", "prob", "loss"], default="grad",
+    ap.add_argument("--path", choices=["grad", "forward", "param", "param_grad", "chop", "prob", "loss"],
+                    default="grad",
                     help="grad: the fwd+bwd step (default); chop: on-device chop_tracks of one 500k-segment event; "
                          "prob: the probabilistic front end on the waveforms of 8 events; loss: mse_adc forward + "
                          "gradient on the hits of the 64-event batch; forward / param: the plain forward "
-                         "drop-in (LUT mode / parametrised mode) on the 64-event batch")
+                         "drop-in (LUT mode / parametrised mode) on the 64-event batch; param_grad: the "
+                         "parametrised-mode SSE-ADC loss and its gradient (autograd through the waveform, "
+                         "front-end and current-model adjoints)")
     return ap.parse_args()
 
 
@@ -692,6 +695,59 @@ def run_forward(args, param_mode=False):
     print(json.dumps(rec), flush=True)
 
 
+def run_param_grad(args):
+    """Parametrised mode fwd+bwd on the 64-event batch: waveforms at the
+    perturbed parameters (offsets fixed), front end, SSE against the ADCs
+    at the nominal parameters, and dL/dtheta through lsim_fee_vjp and
+    lsim_param_wfs_vjp (torch autograd composes them)."""
+    import torch
+    from larndsim_gb300 import grad, sim
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    tracks, fields = workload(0, args.seed)
+    n_seg = tracks.shape[0]
+    t_dev = torch.from_numpy(tracks).to(dev)
+    params = nominal_params().replace(number_pix_neighbors=0, mc_diff=True)
+    offsets = sim.draw_offsets(n_seg, 7, dev)
+    with torch.no_grad():
+        w0, u0 = sim.param_wfs_fn(grad.theta_of(params, device=dev), params, t_dev, fields, offsets)
+        a0, _ = sim.fee_adc(params, w0[u0 >= 0])
+    pp = params.replace(lifetime=float(params.lifetime) * 1.05, Ab=float(params.Ab) * 0.97)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def step(tr=t_dev):
+        theta = grad.theta_of(pp, device=dev).requires_grad_(True)
+        wfs, unique = sim.param_wfs_fn(theta, pp, tr, fields, offsets)
+        adc, _ = sim.fee_adc(pp, wfs[unique >= 0])
+        loss = ((adc - a0) ** 2).sum()
+        loss.backward()
+        return loss.detach(), theta.grad
+
+    ms, clk = _timed(step, args.steps, args.warmup, flush)
+    host = torch.from_numpy(tracks).pin_memory()
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        loss, g = step(host.to(dev, non_blocking=True))
+        vals = (float(loss), g.cpu())
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    rec = {"metric": "parametrised fwd+bwd segments/s", "value": n_seg / (ms * 1e-3), "unit": "segments/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tracks)",
+           "config": {"workload": f"parametrised mode (n_neighbors=0, mc_diff offsets fixed) on the 64-event batch "
+                                  f"({n_seg} segments): waveforms, front end, SSE-ADC loss against the nominal "
+                                  "parameters' ADCs, gradient in the 8 parameters (eager, waveforms stored)",
+                      "segments": n_seg, "l2": "flushed between timed steps (512 MiB write)"},
+           "e2e": {"value": n_seg / e2e_s, "unit": "segments/s", "ms_per_step": e2e_s * 1e3,
+                   "h2d_bytes_per_step": int(tracks.nbytes), "d2h_bytes_per_step": 4 * (1 + 8)},
+           "clocks": clk, "gpu_launches": None}
+    print(json.dumps(rec), flush=True)
+
+
 # ---------------------------------------------------------------- hit-level fit loss
 
 def run_loss(args):
@@ -811,6 +867,12 @@ def run_chop_reference(args):
 
 def main():
     args = parse()
+    if args.path == "param_grad":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "param_grad path: no CPU arm"}))
+        else:
+            run_param_grad(args)
+        return
     if args.path in ("forward", "param"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "forward paths: the reference arm of the "

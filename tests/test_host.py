@@ -223,6 +223,8 @@ def test_next_row_entry_points_reject_bad_arguments_without_gpu(lib):
     fm = _abi.field_map(("eventID", "x", "y", "z", "x_start", "y_start", "z_start", "x_end", "y_end", "z_end",
                          "dx", "dE", "dEdx"))
     assert lib.lsim_param_stage1(pn, fm, V(16), 10, 1, None, ws, big, V(64), None) == _abi.LSIM_ERR_UNSUPPORTED
+    assert lib.lsim_param_wfs_vjp(p, None, 10, 1, V(16), 8, 4, V(16), None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_param_wfs_vjp(p, ws, 10, 1, V(16), 2, 4, V(16), None) == _abi.LSIM_ERR_CAPACITY
     assert lib.lsim_fee_vjp_workspace_bytes(100) >= 100 * 4 * 1024
     assert lib.lsim_fee_vjp(p, V(16), 4, 2002, None, V(16), V(16), ws, big, None) == _abi.LSIM_ERR_UNSUPPORTED
     assert lib.lsim_fee_vjp(p, V(16), 4, 2000, None, None, V(16), ws, big, None) == _abi.LSIM_ERR_INVALID
