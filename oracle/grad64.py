@@ -41,8 +41,7 @@ class Frozen:
     """Discrete decisions of one float32 forward pass plus the inputs."""
 
     def __init__(self, params, templates, tracks, fields, target_pids, target_adc):
-        if getattr(params.recombination_mode, "value", params.recombination_mode) != 2:
-            raise NotImplementedError("the FP64 gradient oracle covers Birks recombination")
+        self.mode = int(getattr(params.recombination_mode, "value", params.recombination_mode))
         self.params = params
         self.T = np.asarray(templates, np.float32)   # widened to float64 per slice
         self.fields = tuple(fields)
@@ -53,6 +52,13 @@ class Frozen:
         self.z = sh[:, fields.index("z")].astype(np.float64)
         self.dE = sh[:, fields.index("dE")].astype(np.float64)
         self.dEdx = sh[:, fields.index("dEdx")].astype(np.float64)
+        # ellipsoid Box model: the angle factor beta / sqrt(sin^2 + cos^2 / R^2)
+        # (no parameter dependence); Box models: the max(0, f) branch taken
+        zs, ze = sh[:, fields.index("z_start")], sh[:, fields.index("z_end")]
+        cosphi = (np.abs(ze - zs) / (sh[:, fields.index("dx")] + np.float32(1e-10))).astype(np.float64)
+        self.b_phi = params.beta / np.sqrt((1 - cosphi ** 2) + cosphi ** 2 / params.R_param ** 2)
+        q32 = R.quench(params, sh, fields)[:, fields.index("n_electrons")]
+        self.recomb_on = q32 > 0
         mask, plane = R.tpc_membership(params, sh[:, fields.index("x")], sh[:, fields.index("y")], sh[:, fields.index("z")])
         self.mask = mask.astype(np.float64)
         self.plane = plane
@@ -129,8 +135,15 @@ def segment_quantities(fr: Frozen, th: dict):
     """n_e, sigma_T, long diffusion (ticks), t0 in float64 (quench + drift)."""
     p = fr.params
     v = vdrift64(p, th["eField"])
-    X = th["kb"] * fr.dEdx / (th["eField"] * th["lArDensity"])
-    R_ = th["Ab"] / (1 + X)
+    erho = th["eField"] * th["lArDensity"]
+    if fr.mode == 2:                                       # Birks, quenching_jax.py:23-25
+        R_ = th["Ab"] / (1 + th["kb"] * fr.dEdx / erho)
+    elif fr.mode == 1:                                     # Box, :18-21
+        csi = p.beta * fr.dEdx / erho
+        R_ = np.where(fr.recomb_on, np.log(p.alpha + csi) / csi, 0.0)
+    else:                                                  # ellipsoid Box, :30-35, :55-66
+        csi = fr.b_phi * fr.dEdx / erho
+        R_ = np.where(fr.recomb_on, np.log(p.alpha + csi) / (csi + 1e-10), 0.0)
     dist = np.abs(fr.z - fr.z_anode) + 1e-6
     t = dist / v
     ne = R_ * fr.dE * p.MeVToElectrons * np.exp(-t / th["lifetime"]) * fr.mask

@@ -158,16 +158,23 @@ def test_stored_waveform_variant_matches_recompute(cuda):
     assert (loss, g) == a
 
 
-@pytest.mark.parametrize("case", [dict(n_neighbors=1), dict(n_neighbors=2, seed=5, n_tracks=2, shower=300)])
+@pytest.mark.parametrize("case", [dict(n_neighbors=1), dict(n_neighbors=2, seed=5, n_tracks=2, shower=300),
+                                  dict(n_neighbors=1, seed=11, n_tracks=2, recomb="BOX"),
+                                  dict(n_neighbors=1, seed=12, n_tracks=2, recomb="ELLIPSOID")])
 def test_wfs_vjp_matches_complex_step(cuda, case):
     """lsim_lut_wfs_vjp through grad.wfs_fn (jax.vjp of simulate_wfs): an
     arbitrary cotangent on the waveform rows pulled back to the 8
     parameters, against the complex-step derivative of the float64
     waveforms of the oracle (decisions frozen)."""
-    from larndsim_gb300 import grad
+    from larndsim_gb300 import consts, grad
     from oracle import grad64 as G
+    case = dict(case)
+    recomb = case.pop("recomb", None)
     p, tmpl, tracks, fields, chain, target = _setup(**case)
     pp = _perturbed(p)
+    if recomb is not None:   # Box models: eField and lArDensity enter through csi
+        pp = pp.replace(recombination_mode=getattr(consts.RecombinationMode, recomb))
+        target = chain.target(pp)
     theta = grad.theta_of(pp).requires_grad_(True)
     wfs, unique = grad.wfs_fn(theta, chain, pp)
     rng = np.random.default_rng(4)
