@@ -15,8 +15,11 @@ finite differences are the pathwise gradient, free of the jumps a full
 re-simulation shows when an index flips.
 
 Parameters: Ab, kb, eField, lifetime, vdrift, long_diff, tran_diff,
-lArDensity (Birks recombination).  ``vdrift`` does not enter (the reference
-never reads params.vdrift), so its derivative is 0.
+lArDensity (Birks, Box and ellipsoid Box recombination; the Box models'
+max(0, f) branch is frozen too).  ``vdrift`` does not enter (the reference
+never reads params.vdrift), so its derivative is 0.  ``param_waveforms64``
+does the same for the parametrised mode's waveforms (sim_jax.py:122-139,
+:289-335).
 """
 
 from __future__ import annotations
