@@ -349,6 +349,24 @@ int lsim_fee_prob(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t 
                   float stop_threshold, float *log_prob_out, float *charge_out, float *exp_tick_out,
                   float *exp_adc_out, float *lambda_out, void *ws, size_t ws_bytes, void *stream);
 
+/* Workspace bytes of lsim_fee_prob_vjp (the forward's per-step path states). */
+size_t lsim_fee_prob_vjp_workspace_bytes(const LsimParams *p, int64_t n_pix, int32_t n_paths);
+
+/* Vector-Jacobian product of lsim_fee_prob with respect to the waveforms:
+ * given cotangents on any of its outputs (g_log_prob, g_charge
+ * [n_pix][H][n_t - 1]; g_e_tick, g_e_adc, g_lambda [n_pix][H], all three or
+ * none), writes g_wfs[n_pix][n_t].  The forward is re-run with each step's
+ * paths recorded; the reverse pass follows jax.grad of
+ * get_adc_values_average_noise_vmap (src/larndsim/fee_jax.py:334-461) and
+ * get_average_hit_values (:463-480): top-K choices held, the running
+ * maximum's cotangent routed to the tick where it was first attained (the
+ * reference splits exact ties), jax.scipy.special.log_ndtr's derivative
+ * exp(norm_logpdf(x) - log_ndtr(x)). */
+int lsim_fee_prob_vjp(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, int32_t n_paths,
+                      float stop_threshold, const float *g_log_prob, const float *g_charge, const float *g_e_tick,
+                      const float *g_e_adc, const float *g_lambda, float *g_wfs, void *ws, size_t ws_bytes,
+                      void *stream);
+
 /* ---------------------------------------------------------------- fit losses */
 
 /* Workspace bytes of lsim_mse_adc for n_hits predicted and n_ref reference hits. */

@@ -381,6 +381,30 @@ int lsim_fee_prob(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t 
               "lsim_fee_prob");
 }
 
+size_t lsim_fee_prob_vjp_workspace_bytes(const LsimParams *p, int64_t n_pix, int32_t n_paths) {
+  return p && n_pix >= 0 && n_paths > 0 ? fee_prob_vjp_workspace_bytes(n_pix, p->max_adc_values, n_paths) : 0;
+}
+
+int lsim_fee_prob_vjp(const LsimParams *p, const float *wfs, int64_t n_pix, int32_t n_t, int32_t n_paths,
+                      float stop_threshold, const float *g_log_prob, const float *g_charge, const float *g_e_tick,
+                      const float *g_e_adc, const float *g_lambda, float *g_wfs, void *ws, size_t ws_bytes,
+                      void *stream) {
+  g_err.clear();
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (n_pix < 0 || (n_pix > 0 && (!wfs || !g_wfs))) return fail(LSIM_ERR_INVALID, "lsim_fee_prob_vjp: bad arguments");
+  const bool any_red = g_e_tick || g_e_adc || g_lambda;
+  if (any_red && !(g_e_tick && g_e_adc && g_lambda))
+    return fail(LSIM_ERR_INVALID, "lsim_fee_prob_vjp: give all three reduction cotangents or none");
+  if (!(stop_threshold > 0.0f)) return fail(LSIM_ERR_INVALID, "lsim_fee_prob_vjp: stop_threshold %g", stop_threshold);
+  if (n_paths < 1 || n_paths > 32) return fail(LSIM_ERR_UNSUPPORTED, "lsim_fee_prob_vjp: n_paths %d", n_paths);
+  const size_t need = fee_prob_vjp_workspace_bytes(n_pix, p->max_adc_values, n_paths);
+  if (!ws || ws_bytes < need) return fail(LSIM_ERR_CAPACITY, "lsim_fee_prob_vjp: workspace %zu < %zu bytes", ws_bytes, need);
+  return wrap(run_fee_prob_vjp(*p, wfs, n_pix, n_t, n_paths, stop_threshold, g_log_prob, g_charge, g_e_tick, g_e_adc,
+                               g_lambda, g_wfs, ws, (cudaStream_t)stream),
+              "lsim_fee_prob_vjp");
+}
+
 size_t lsim_mse_adc_workspace_bytes(int64_t n_hits, int64_t n_ref) {
   return n_hits < 0 || n_ref < 0 ? 0 : mse_adc_workspace_bytes(n_hits, n_ref);
 }

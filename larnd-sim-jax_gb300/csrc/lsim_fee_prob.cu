@@ -143,21 +143,25 @@ __device__ __forceinline__ void warp_best(float &bv, int &bi) {
 // in-place inclusive scan of a[0..n) with op (sum, max) or a suffix max;
 // each thread scans a contiguous chunk of kProbTicks, warps and the block
 // combine the chunk totals.
-enum ScanOp { kScanSum = 0, kScanMax = 1, kScanSuffixMax = 2 };
+enum ScanOp { kScanSum = 0, kScanMax = 1, kScanSuffixMax = 2, kScanSuffixSum = 3 };
 
 template <int OP>
 __device__ void block_scan_row(float *a, int n, float *red) {
+  constexpr bool SUFFIX = OP == kScanSuffixMax || OP == kScanSuffixSum;
+  constexpr bool SUM = OP == kScanSum || OP == kScanSuffixSum;
+  const float ident = SUM ? 0.0f : -INFINITY;
+  auto comb = [](float x, float y) { return SUM ? x + y : fmaxf(x, y); };
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   float v[kProbTicks];
-  const int base = OP == kScanSuffixMax ? n - (tid + 1) * kProbTicks : tid * kProbTicks;
-  float run = OP == kScanSum ? 0.0f : -INFINITY;
+  // suffix scans walk each thread's chunk from the right, thread 0 holding the last chunk
+  const int base = SUFFIX ? n - (tid + 1) * kProbTicks : tid * kProbTicks;
+  float run = ident;
 #pragma unroll
   for (int i = 0; i < kProbTicks; ++i) {
-    // suffix max walks its chunk from the right
-    const int t = OP == kScanSuffixMax ? base + kProbTicks - 1 - i : base + i;
+    const int t = SUFFIX ? base + kProbTicks - 1 - i : base + i;
     const bool ok = t >= 0 && t < n;
-    const float x = ok ? a[t] : (OP == kScanSum ? 0.0f : -INFINITY);
-    run = OP == kScanSum ? run + x : fmaxf(run, x);
+    const float x = ok ? a[t] : ident;
+    run = comb(run, x);
     v[i] = run;
   }
   // exclusive prefix of the chunk totals across the block
@@ -165,20 +169,20 @@ __device__ void block_scan_row(float *a, int n, float *red) {
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const float y = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl = OP == kScanSum ? incl + y : fmaxf(incl, y);
+    if (lane >= o) incl = comb(incl, y);
   }
   if (lane == 31) red[wid] = incl;
   __syncthreads();
-  float carry = OP == kScanSum ? 0.0f : -INFINITY;
-  for (int w = 0; w < wid; ++w) carry = OP == kScanSum ? carry + red[w] : fmaxf(carry, red[w]);
+  float carry = ident;
+  for (int w = 0; w < wid; ++w) carry = comb(carry, red[w]);
   float ex = __shfl_up_sync(0xffffffffu, incl, 1);
-  if (lane == 0) ex = OP == kScanSum ? 0.0f : -INFINITY;
-  const float pre = OP == kScanSum ? carry + ex : fmaxf(carry, ex);
+  if (lane == 0) ex = ident;
+  const float pre = comb(carry, ex);
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < kProbTicks; ++i) {
-    const int t = OP == kScanSuffixMax ? base + kProbTicks - 1 - i : base + i;
-    if (t >= 0 && t < n) a[t] = OP == kScanSum ? pre + v[i] : fmaxf(pre, v[i]);
+    const int t = SUFFIX ? base + kProbTicks - 1 - i : base + i;
+    if (t >= 0 && t < n) a[t] = comb(pre, v[i]);
   }
   __syncthreads();
 }
@@ -204,6 +208,8 @@ struct ProbArgs {
   float z, thr, log_stop;
   float *log_prob, *charge, *e_tick, *e_adc, *lam;
   int32_t *step_active;   // [H]: some pixel kept a total path probability above the stop level after step h
+  float *state;           // optional [n_pix][H][2][K]: each step's input path charges and log-probabilities
+  int32_t *state_top;     // optional [n_pix][H][K]: each step's selected ticks (for the adjoint)
 };
 
 // The per-tick work of a step reads, for tick t, only the running maximum
@@ -287,6 +293,11 @@ __global__ void __launch_bounds__(kProbThreads, 2) k_fee_prob(ProbArgs a) {
         for (int j = 0; j < K; ++j)
           if (j != tid && pc[j] == pc[tid] && plp[j] > plp[tid] + 110.0f) sk = 1;
         pskip[tid] = sk;
+        if (a.state) {
+          float *st = a.state + ((pix * H + h) * 2) * (int64_t)K;
+          st[tid] = pc[tid];
+          st[K + tid] = plp[tid];
+        }
       }
       float hm[kProbTicks], hs[kProbTicks], dm[kProbTicks], ds[kProbTicks], sm_[kProbTicks], ss[kProbTicks];
 #pragma unroll
@@ -433,6 +444,7 @@ __global__ void __launch_bounds__(kProbThreads, 2) k_fee_prob(ProbArgs a) {
             const int tt = bi >= 0 && bi < T - 1 ? bi : T - 2;
             nlp[r] = vd[cls[tt]];
             nc[r] = qs[min(shifted(tt) + 1, T - 1)];
+            if (a.state_top) a.state_top[(pix * H + h) * (int64_t)K + r] = tt;
           }
         }
       }
@@ -486,19 +498,313 @@ __global__ void k_fee_prob_mask(ProbArgs a, int H) {
   }
 }
 
+// ---------------------------------------------------------------- adjoint
+// Reverse mode through the beam search as jax.grad takes it: the top-K tick
+// choices are held (lax.stop_gradient), jnp.where passes the cotangent to
+// the selected branch, jnp.minimum to the smaller argument (half each at a
+// tie), the running maximum to the tick where it was first attained, and
+// softplus / sigmoid / log-sum-exp by their derivatives.
+
+// d log_ndtr / dx as jax.scipy.special.log_ndtr defines it (a custom
+// derivative, the same on every branch): exp(norm_logpdf(x) - log_ndtr(x))
+__device__ __forceinline__ float dlog_ndtr_f(float x, float lx) {
+  return expf((-0.5f * x * x - 0.918938533204672742f) - lx);
+}
+
+// log_diff_ndtr value and partials d/da, d/db (la = log_ndtr(a), dla its derivative)
+__device__ __forceinline__ float ldn_grad(float a, float b, float la, float lb, float dla, float dlb, float term_m1,
+                                          float &ga, float &gb) {
+  float lts, dlts_du = 0.f;
+  const bool sel = a > b;
+  if (sel) {
+    const float u = lb - la;
+    const float neg = -expm1f(u);
+    const float y = (neg - 1e-30f) * 1e10f;
+    const float ns = 1e-30f + softplus_f(y) / 1e10f;
+    const float lt = logf(ns);
+    lts = -100.0f + ((lt + 100.0f) * 10.0f) / 10.0f;
+    // softplus' = sigmoid; d neg / du = -exp(u); the second clamp is the identity there
+    dlts_du = (1.0f / ns) * sigmoid_f(y) * (-expf(u));
+  } else {
+    lts = term_m1;
+  }
+  const float lp = la + lts;
+  const float w = sigmoid_f((a - b) * 1000.0f);
+  const float out = w * lp + (1.0f - w) * kProbFloor;
+  const float gw = (lp - kProbFloor) * w * (1.0f - w) * 1000.0f;   // through the gate
+  ga = w * (dla - dlts_du * dla) + gw;
+  gb = w * (dlts_du * dlb) - gw;
+  if (!sel) {
+    ga = w * dla + gw;
+    gb = -gw;
+  }
+  return out;
+}
+
+struct ProbVjpArgs {
+  ProbArgs f;                  // the forward's arguments (state, state_top, step_active read)
+  const float *g_log_prob;     // optional [n_pix][H][T-1]
+  const float *g_charge;       // optional [n_pix][H][T-1]
+  const float *g_e_tick, *g_e_adc, *g_lam;   // optional [n_pix][H] (all three or none)
+  float *g_wfs;                // [n_pix][T]
+};
+
+__global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va) {
+  extern __shared__ __align__(16) float sm[];
+  const ProbArgs &a = va.f;
+  float *qs = sm, *cm = qs + kProbMaxT, *esp = cm + kProbMaxT, *sw = esp + kProbMaxT;
+  float *Aq0 = sw + kProbMaxT, *Aqs = Aq0 + kProbMaxT, *Am0 = Aqs + kProbMaxT, *Am1 = Am0 + kProbMaxT;
+  float *Aesp = Am1 + kProbMaxT, *Gd = Aesp + kProbMaxT, *tmp = Gd + kProbMaxT;
+  float *part = tmp + kProbMaxT;   // [warps][2][kProbMaxPaths]
+  __shared__ float red[kProbThreads / 32];
+  __shared__ float pc[kProbMaxPaths], plp[kProbMaxPaths], glp_n[kProbMaxPaths], gc_n[kProbMaxPaths];
+  __shared__ int pskip[kProbMaxPaths], ptop[kProbMaxPaths];
+  __shared__ int n_exec;
+
+  const LsimParams &p = a.p;
+  const int T = a.T, K = a.K, H = p.max_adc_values, tid = threadIdx.x;
+  const int lane = tid & 31, wid = tid >> 5;
+  const float z = a.z, thr = a.thr;
+  const float term_m1 = ldn_log_term(-1.0f);
+  auto shifted = [&](int t) { return min(t + a.interval + 1, T - 1); };
+  if (tid == 0) {
+    int first = H;
+    for (int h = 1; h < H; ++h)
+      if (!a.step_active[h - 1]) {
+        first = h;
+        break;
+      }
+    n_exec = first;
+  }
+
+  for (int64_t pix = blockIdx.x; pix < a.n_pix; pix += gridDim.x) {
+    const float *w = a.wfs + pix * T;
+    for (int t = tid; t < T; t += kProbThreads) qs[t] = w[t] * p.t_sampling;
+    __syncthreads();
+    block_scan_row<kScanSum>(qs, T, red);
+    for (int t = tid; t < T; t += kProbThreads) {
+      cm[t] = qs[t];
+      Aq0[t] = Aqs[t] = Am0[t] = Am1[t] = Aesp[t] = 0.f;
+    }
+    __syncthreads();
+    block_scan_row<kScanMax>(cm, T, red);
+    for (int t = tid; t < T - 1; t += kProbThreads) {
+      const float e = (qs[shifted(t)] + thr) - 0.5f * (qs[t + 1] + qs[t]);
+      esp[t] = e;
+      sw[t] = sigmoid_f((e - thr) * 10.0f);
+    }
+    if (tid < K) {
+      glp_n[tid] = 0.f;
+      gc_n[tid] = 0.f;
+    }
+    __syncthreads();
+
+    for (int h = n_exec - 1; h >= 0; --h) {
+      // step h's input paths and selected ticks, recorded by the forward
+      if (tid < K) {
+        const float *st = a.state + ((pix * H + h) * 2) * (int64_t)K;
+        pc[tid] = st[tid];
+        plp[tid] = st[K + tid];
+        ptop[tid] = a.state_top[(pix * H + h) * (int64_t)K + tid];
+      }
+      for (int t = tid; t < T; t += kProbThreads) Gd[t] = 0.f;
+      __syncthreads();
+      if (tid < K) {
+        int sk = 0;
+        for (int j = 0; j < K; ++j)
+          if (j != tid && pc[j] == pc[tid] && plp[j] > plp[tid] + 110.0f) sk = 1;
+        pskip[tid] = sk;
+      }
+      if (tid == 0) {
+        // the next step's state cotangents: new lp_j = dist[top_j], new c_j = q[best_j]
+        for (int j = 0; j < K; ++j) {
+          const int tt = ptop[j];
+          Gd[tt] += glp_n[j];
+          Aq0[min(shifted(tt) + 1, T - 1)] += gc_n[j];
+        }
+      }
+      __syncthreads();
+      // ---- pass 1: hit and dist log-sum-exps per tick
+      float hitv[kProbTicks], distv[kProbTicks];
+#pragma unroll
+      for (int i = 0; i < kProbTicks; ++i) {
+        float hm = -INFINITY, hs = 0.f, dm = -INFINITY, ds = 0.f;
+        const int t = tid + i * kProbThreads;
+        if (t < T - 1) {
+          const int sidx = shifted(t);
+          for (int k = 0; k < K; ++k) {
+            if (pskip[k]) continue;
+            const float c = pc[k], lp = plp[k];
+            const float zm0 = ((cm[t] - c) - thr) * z, zm1 = ((cm[t + 1] - c) - thr) * z;
+            const float LM0 = log_ndtr_f(zm0);
+            const float LM1 = zm1 == zm0 ? LM0 : log_ndtr_f(zm1);
+            const float lg = log_diff_ndtr_f(zm1, zm0, LM1, LM0, term_m1);
+            const float zq0 = ((qs[t] - c) - thr) * z, zqs = ((qs[sidx] - c) - thr) * z;
+            const float LQ0 = log_ndtr_f(zq0);
+            const float LQs = zqs == zq0 ? LQ0 : log_ndtr_f(zqs);
+            float le = log_diff_ndtr_f(zqs, zq0, LQs, LQ0, term_m1);
+            le = fminf(le, lg);
+            le = kProbFloor + softplus_f(le - kProbFloor);
+            le = sw[t] * le + (1.0f - sw[t]) * kProbFloor;
+            lse_add(hm, hs, le + lp);
+            lse_add(dm, ds, lg + lp);
+          }
+          hitv[i] = lse_final(hm, hs);
+          distv[i] = lse_final(dm, ds);
+        } else {
+          hitv[i] = distv[i] = 0.f;
+        }
+      }
+      // ---- cotangents of the step's outputs on each tick
+      float ghit[kProbTicks], pr[kProbTicks];
+      float l_sum = 0.f, t_sum = 0.f, a_sum = 0.f;
+#pragma unroll
+      for (int i = 0; i < kProbTicks; ++i) {
+        const int t = tid + i * kProbThreads;
+        ghit[i] = 0.f;
+        pr[i] = 0.f;
+        if (t < T - 1) {
+          const int64_t o = (pix * H + h) * (int64_t)(T - 1) + t;
+          if (va.g_log_prob) ghit[i] = va.g_log_prob[o];
+          if (va.g_charge) Aesp[t] += va.g_charge[o];
+          pr[i] = expf(hitv[i]);
+          l_sum += pr[i];
+          t_sum += (float)t * pr[i];
+          a_sum += digitize(p, esp[t]) * pr[i];
+        }
+      }
+      if (va.g_lam) {
+        const float L = block_sum(l_sum, red);
+        const float Ts = block_sum(t_sum, red);
+        const float As = block_sum(a_sum, red);
+        const float den = fmaxf(L, 1e-10f);
+        const float on = L > 1e-10f ? 1.f : (L == 1e-10f ? 0.5f : 0.f);   // jnp.maximum's share
+        const float ET = Ts / den, EA = As / den;
+        const int64_t o = pix * H + h;
+        const float gl = va.g_lam[o], gt = va.g_e_tick[o], ga = va.g_e_adc[o];
+        // the lambda cotangent also reaches ET and EA through the denominator
+        const float gden = -(gt * ET + ga * EA) / den;
+#pragma unroll
+        for (int i = 0; i < kProbTicks; ++i) {
+          const int t = tid + i * kProbThreads;
+          if (t < T - 1) {
+            const float adc = digitize(p, esp[t]);
+            const float gp = gl + gt * (float)t / den + ga * adc / den + on * gden;
+            ghit[i] += gp * pr[i];
+            Aesp[t] += digitize_vjp(p, esp[t], ga * pr[i] / den);
+          }
+        }
+      }
+      float gdist[kProbTicks];
+#pragma unroll
+      for (int i = 0; i < kProbTicks; ++i) {
+        const int t = tid + i * kProbThreads;
+        gdist[i] = t < T - 1 ? Gd[t] : 0.f;
+      }
+      // ---- pass 2: derivatives per tick and path
+      for (int k = 0; k < K; ++k) {
+        float glp = 0.f, gc = 0.f;
+        if (!pskip[k]) {
+          const float c = pc[k], lp = plp[k];
+#pragma unroll
+          for (int i = 0; i < kProbTicks; ++i) {
+            const int t = tid + i * kProbThreads;
+            if (t >= T - 1 || (ghit[i] == 0.f && gdist[i] == 0.f)) continue;
+            const int sidx = shifted(t);
+            const float zm0 = ((cm[t] - c) - thr) * z, zm1 = ((cm[t + 1] - c) - thr) * z;
+            const float LM0 = log_ndtr_f(zm0), LM1 = log_ndtr_f(zm1);
+            float g_m1, g_m0;
+            const float lg = ldn_grad(zm1, zm0, LM1, LM0, dlog_ndtr_f(zm1, LM1), dlog_ndtr_f(zm0, LM0), term_m1,
+                                      g_m1, g_m0);
+            const float zq0 = ((qs[t] - c) - thr) * z, zqs = ((qs[sidx] - c) - thr) * z;
+            const float LQ0 = log_ndtr_f(zq0), LQs = log_ndtr_f(zqs);
+            float g_qs, g_q0;
+            const float lep = ldn_grad(zqs, zq0, LQs, LQ0, dlog_ndtr_f(zqs, LQs), dlog_ndtr_f(zq0, LQ0), term_m1,
+                                       g_qs, g_q0);
+            const float le1 = fminf(lep, lg);
+            const float le2 = kProbFloor + softplus_f(le1 - kProbFloor);
+            const float wt = sw[t];
+            const float le = wt * le2 + (1.0f - wt) * kProbFloor;
+            const float al = ghit[i] != 0.f ? expf((le + lp) - hitv[i]) : 0.f;
+            const float be = gdist[i] != 0.f ? expf((lg + lp) - distv[i]) : 0.f;
+            const float g_le = ghit[i] * al;
+            glp += g_le + gdist[i] * be;
+            // le = w le2 + (1 - w)(-1000); w = sigmoid((esp - thr) 10)
+            Aesp[t] += g_le * (le2 - kProbFloor) * wt * (1.0f - wt) * 10.0f;
+            const float g_le1 = g_le * wt * sigmoid_f(le1 - kProbFloor);
+            const float s_lep = lep < lg ? 1.f : (lep == lg ? 0.5f : 0.f);
+            const float g_lep = g_le1 * s_lep, g_lg = g_le1 * (1.f - s_lep) + gdist[i] * be;
+            const float gzqs = g_lep * g_qs, gzq0 = g_lep * g_q0;
+            const float gzm1 = g_lg * g_m1, gzm0 = g_lg * g_m0;
+            Aq0[t] += gzq0 * z;
+            Aqs[t] += gzqs * z;
+            Am0[t] += gzm0 * z;
+            Am1[t] += gzm1 * z;
+            gc -= (gzq0 + gzqs + gzm0 + gzm1) * z;
+          }
+        }
+        glp = warp_sum(glp);
+        gc = warp_sum(gc);
+        if (lane == 0) {
+          part[(wid * 2) * kProbMaxPaths + k] = glp;
+          part[(wid * 2 + 1) * kProbMaxPaths + k] = gc;
+        }
+      }
+      __syncthreads();
+      if (tid < K) {
+        float s1 = 0.f, s2 = 0.f;
+        for (int w2 = 0; w2 < kProbThreads / 32; ++w2) {
+          s1 += part[(w2 * 2) * kProbMaxPaths + tid];
+          s2 += part[(w2 * 2 + 1) * kProbMaxPaths + tid];
+        }
+        glp_n[tid] = s1;   // cotangent of this step's input state = the previous step's output state
+        gc_n[tid] = s2;
+      }
+      __syncthreads();
+    }
+    // ---- assemble dL/dq from the per-tick partials
+    // running maximum: cm[t] (tick t's zm0) and cm[t] as tick t-1's cm[t+1]
+    for (int t = tid; t < T; t += kProbThreads) tmp[t] = (t < T - 1 ? Am0[t] : 0.f) + (t > 0 ? Am1[t - 1] : 0.f);
+    __syncthreads();
+    block_scan_row<kScanSum>(tmp, T, red);   // prefix sums P of dL/dcm
+    // each run of a constant running maximum routes its sum to the run's first tick
+    for (int t = tid; t < T; t += kProbThreads) {
+      float g = Aq0[t];
+      const bool start = t == 0 || cm[t] != cm[t - 1];
+      if (start) {
+        int e = t;
+        while (e + 1 < T && cm[e + 1] == cm[t]) ++e;
+        g += tmp[e] - (t > 0 ? tmp[t - 1] : 0.f);
+      }
+      // shifted-tick role q[s_t] (s_t = min(t + interval + 1, T - 1)), with the esperance terms
+      const int t0 = t - a.interval - 1;
+      if (t < T - 1) {
+        if (t0 >= 0) g += Aqs[t0] + Aesp[t0];
+      } else {
+        for (int u = max(t0, 0); u < T - 1; ++u) g += Aqs[u] + Aesp[u];
+      }
+      // esperance: - 0.5 (q[t + 1] + q[t])
+      if (t < T - 1) g -= 0.5f * Aesp[t];
+      if (t > 0) g -= 0.5f * Aesp[t - 1];
+      Gd[t] = g;
+    }
+    __syncthreads();
+    // q = cumsum(w * ts): dL/dw[i] = ts * sum_{j >= i} dL/dq[j]
+    block_scan_row<kScanSuffixSum>(Gd, T, red);
+    for (int t = tid; t < T; t += kProbThreads) va.g_wfs[pix * T + t] = Gd[t] * p.t_sampling;
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 size_t fee_prob_workspace_bytes(int32_t max_adc_values) {
   return ((size_t)(max_adc_values > 0 ? max_adc_values : 1) * sizeof(int32_t) + 255) & ~size_t(255);
 }
 
-int run_fee_prob(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, int32_t n_paths,
-                 float stop_threshold, float *log_prob, float *charge, float *e_tick, float *e_adc, float *lam,
-                 void *ws, cudaStream_t st) {
-  if (n_t < 3 || n_t > kProbMaxT) return set_error(LSIM_ERR_UNSUPPORTED, "probabilistic FEE: n_t must be in [3, 2048]");
-  if (n_paths < 1 || n_paths > kProbMaxPaths || n_paths > n_t - 1)
-    return set_error(LSIM_ERR_UNSUPPORTED, "probabilistic FEE: fee_paths_scaling must be in [1, min(32, n_t - 1)]");
-  if (!(p.reset_noise > 0.0f)) return set_error(LSIM_ERR_INVALID, "probabilistic FEE: RESET_NOISE_CHARGE must be > 0");
+static ProbArgs prob_args(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, int32_t n_paths,
+                          float stop_threshold, float *log_prob, float *charge, float *e_tick, float *e_adc,
+                          float *lam, void *ws) {
   ProbArgs a;
   a.p = p;
   a.wfs = wfs;
@@ -515,6 +821,21 @@ int run_fee_prob(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n
   a.e_adc = e_adc;
   a.lam = lam;
   a.step_active = static_cast<int32_t *>(ws);
+  a.state = nullptr;
+  a.state_top = nullptr;
+  return a;
+}
+
+static int run_fee_prob_impl(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, int32_t n_paths,
+                             float stop_threshold, float *log_prob, float *charge, float *e_tick, float *e_adc,
+                             float *lam, void *ws, float *state, int32_t *state_top, cudaStream_t st) {
+  if (n_t < 3 || n_t > kProbMaxT) return set_error(LSIM_ERR_UNSUPPORTED, "probabilistic FEE: n_t must be in [3, 2048]");
+  if (n_paths < 1 || n_paths > kProbMaxPaths || n_paths > n_t - 1)
+    return set_error(LSIM_ERR_UNSUPPORTED, "probabilistic FEE: fee_paths_scaling must be in [1, min(32, n_t - 1)]");
+  if (!(p.reset_noise > 0.0f)) return set_error(LSIM_ERR_INVALID, "probabilistic FEE: RESET_NOISE_CHARGE must be > 0");
+  ProbArgs a = prob_args(p, wfs, n_pix, n_t, n_paths, stop_threshold, log_prob, charge, e_tick, e_adc, lam, ws);
+  a.state = state;
+  a.state_top = state_top;
   if (cudaMemsetAsync(a.step_active, 0, sizeof(int32_t) * p.max_adc_values, st) != cudaSuccess) return LSIM_ERR_CUDA;
   if (n_pix == 0) return LSIM_OK;
   const size_t smem = sizeof(float) * (kProbArrays * kProbMaxT + kProbExtraFloats);
@@ -525,8 +846,52 @@ int run_fee_prob(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n
   const int64_t cap = (int64_t)device_sm_count() * (per_sm > 0 ? per_sm : 1);
   const unsigned grid = (unsigned)(n_pix < cap ? n_pix : cap);
   k_fee_prob<<<grid, kProbThreads, smem, st>>>(a);
-  k_fee_prob_mask<<<(unsigned)device_sm_count() * 4, 256, 0, st>>>(a, p.max_adc_values);
+  if (log_prob || charge || lam)
+    k_fee_prob_mask<<<(unsigned)device_sm_count() * 4, 256, 0, st>>>(a, p.max_adc_values);
   return LSIM_OK;
+}
+
+size_t fee_prob_vjp_workspace_bytes(int64_t n_pix, int32_t max_adc_values, int32_t n_paths) {
+  auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  const size_t states = (size_t)(n_pix > 0 ? n_pix : 0) * (size_t)max_adc_values * (size_t)n_paths;
+  return fee_prob_workspace_bytes(max_adc_values) + al(sizeof(float) * 2 * states) + al(sizeof(int32_t) * states);
+}
+
+int run_fee_prob_vjp(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, int32_t n_paths,
+                     float stop_threshold, const float *g_log_prob, const float *g_charge, const float *g_e_tick,
+                     const float *g_e_adc, const float *g_lam, float *g_wfs, void *ws, cudaStream_t st) {
+  auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  const size_t states = (size_t)n_pix * (size_t)p.max_adc_values * (size_t)n_paths;
+  char *b = static_cast<char *>(ws);
+  float *state = reinterpret_cast<float *>(b + fee_prob_workspace_bytes(p.max_adc_values));
+  int32_t *state_top = reinterpret_cast<int32_t *>(reinterpret_cast<char *>(state) + al(sizeof(float) * 2 * states));
+  // forward with the step states recorded (no outputs), then the reverse pass
+  int rc = run_fee_prob_impl(p, wfs, n_pix, n_t, n_paths, stop_threshold, nullptr, nullptr, nullptr, nullptr,
+                             nullptr, ws, state, state_top, st);
+  if (rc != LSIM_OK || n_pix == 0) return rc;
+  ProbVjpArgs va;
+  va.f = prob_args(p, wfs, n_pix, n_t, n_paths, stop_threshold, nullptr, nullptr, nullptr, nullptr, nullptr, ws);
+  va.f.state = state;
+  va.f.state_top = state_top;
+  va.g_log_prob = g_log_prob;
+  va.g_charge = g_charge;
+  va.g_e_tick = g_e_tick;
+  va.g_e_adc = g_e_adc;
+  va.g_lam = g_lam;
+  va.g_wfs = g_wfs;
+  const size_t smem = sizeof(float) * (11 * kProbMaxT + 2 * (kProbThreads / 32) * kProbMaxPaths);
+  if (cudaFuncSetAttribute(k_fee_prob_vjp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return LSIM_ERR_CUDA;
+  const int64_t cap = device_sm_count();
+  k_fee_prob_vjp<<<(unsigned)(n_pix < cap ? n_pix : cap), kProbThreads, smem, st>>>(va);
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
+int run_fee_prob(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, int32_t n_paths,
+                 float stop_threshold, float *log_prob, float *charge, float *e_tick, float *e_adc, float *lam,
+                 void *ws, cudaStream_t st) {
+  return run_fee_prob_impl(p, wfs, n_pix, n_t, n_paths, stop_threshold, log_prob, charge, e_tick, e_adc, lam, ws,
+                           nullptr, nullptr, st);
 }
 
 }  // namespace lsim

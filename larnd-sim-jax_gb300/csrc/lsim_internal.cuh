@@ -87,6 +87,11 @@ int run_chamfer(const float *x, const float *y, const float *z, const int32_t *e
                 const float *rx, const float *ry, const float *rz, const int32_t *revent, const float *rw, int64_t m,
                 float *out, float *g_w, float *g_z, void *ws, cudaStream_t st);
 
+size_t fee_prob_vjp_workspace_bytes(int64_t n_pix, int32_t max_adc_values, int32_t n_paths);
+int run_fee_prob_vjp(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n_t, int32_t n_paths,
+                     float stop_threshold, const float *g_log_prob, const float *g_charge, const float *g_e_tick,
+                     const float *g_e_adc, const float *g_lam, float *g_wfs, void *ws, cudaStream_t st);
+
 // lsim_chop.cu
 size_t chop_workspace_bytes(int64_t n_rows);
 int run_chop(const LsimFieldMap &f, const float *tracks, int64_t n_rows, double precision, float *out,

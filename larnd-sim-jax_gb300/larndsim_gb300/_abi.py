@@ -99,6 +99,9 @@ _SIGNATURES = {
     "lsim_pixel_coords": (C.c_int, [_PP, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
     "lsim_fee_prob_workspace_bytes": (_sz, [_PP]),
     "lsim_fee_prob": (C.c_int, [_PP, _vp, _i64, _i32, _i32, C.c_float, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "lsim_fee_prob_vjp_workspace_bytes": (_sz, [_PP, _i64, _i32]),
+    "lsim_fee_prob_vjp": (C.c_int, [_PP, _vp, _i64, _i32, _i32, C.c_float, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz,
+                                    _vp]),
     "lsim_mse_adc_workspace_bytes": (_sz, [_i64, _i64]),
     "lsim_mse_adc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, C.c_float, C.c_float,
                                _vp, _vp, _vp, _vp, _sz, _vp]),

@@ -370,23 +370,74 @@ def _fee_prob(params, wfs, stop_threshold, distributions, reductions):
     return log_prob, charge, red
 
 
+def _fee_prob_vjp(params, wfs, stop_threshold, g_lp=None, g_ch=None, g_red=None):
+    lib = _abi.load()
+    w = wfs.detach().to(dtype=torch.float32).contiguous()
+    P, T = w.shape
+    lp = _abi.make_params(params)
+    K = int(params.fee_paths_scaling)
+    ws = torch.empty(lib.lsim_fee_prob_vjp_workspace_bytes(lp, P, K), dtype=torch.uint8, device=w.device)
+    g = torch.empty_like(w)
+    c = lambda t: None if t is None else t.to(torch.float32).contiguous()   # noqa: E731
+    red = [None] * 3 if g_red is None else [c(t) for t in g_red]
+    g_lp, g_ch = c(g_lp), c(g_ch)
+    _abi.check(lib, lib.lsim_fee_prob_vjp(lp, _ptr(w), P, T, K, float(stop_threshold), _ptr(g_lp), _ptr(g_ch),
+                                          *(_ptr(r) for r in red), _ptr(g), _ptr(ws), ws.numel(), _stream()))
+    return g
+
+
+class _FeeProbDistFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, wfs, params, stop_threshold):
+        log_prob, charge, _ = _fee_prob(params, wfs, stop_threshold, True, False)
+        ctx.save_for_backward(wfs)
+        ctx.params, ctx.stop = params, stop_threshold
+        return log_prob, charge
+
+    @staticmethod
+    def backward(ctx, g_lp, g_ch):
+        (wfs,) = ctx.saved_tensors
+        return _fee_prob_vjp(ctx.params, wfs, ctx.stop, g_lp=g_lp, g_ch=g_ch), None, None
+
+
+class _FeeProbRedFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, wfs, params, stop_threshold):
+        _, _, (e_tick, e_adc, lam) = _fee_prob(params, wfs, stop_threshold, False, True)
+        ctx.save_for_backward(wfs)
+        ctx.params, ctx.stop = params, stop_threshold
+        return e_tick, e_adc, lam
+
+    @staticmethod
+    def backward(ctx, g_t, g_a, g_l):
+        (wfs,) = ctx.saved_tensors
+        zero = lambda g: torch.zeros(wfs.shape[0], int(ctx.params.MAX_ADC_VALUES), device=wfs.device) \
+            if g is None else g   # noqa: E731
+        return _fee_prob_vjp(ctx.params, wfs, ctx.stop, g_red=(zero(g_t), zero(g_a), zero(g_l))), None, None
+
+
+def _as_wfs(wfs):
+    w = torch.as_tensor(wfs)
+    return (w if w.is_cuda else w.to(device=_device())).to(torch.float32)
+
+
 def get_adc_values_average_noise_vmap(params, wfs, stop_threshold=1e-9):
     """Probabilistic self-trigger front end (fee_jax.py:386-461): a beam
     search over ``fee_paths_scaling`` paths and MAX_ADC_VALUES hits with
     noise width RESET_NOISE_CHARGE.  Returns (log_prob, charge), each
     (P, MAX_ADC_VALUES, T - 1): the log-probability that hit h is read at
-    each tick and the expected charge if it is."""
-    log_prob, charge, _ = _fee_prob(params, wfs, stop_threshold, True, False)
-    return log_prob, charge
+    each tick and the expected charge if it is.  Differentiable with
+    respect to ``wfs`` (lsim_fee_prob_vjp)."""
+    return _FeeProbDistFn.apply(_as_wfs(wfs), params, stop_threshold)
 
 
 def average_hit_values(params, wfs, stop_threshold=1e-9):
     """get_average_hit_values (fee_jax.py:463-480) of the probabilistic
     front end's output, fused into the beam search so the (P, H, T - 1)
     distributions are never stored: (expected_ticks, expected_adcs,
-    lambda), each (P, MAX_ADC_VALUES)."""
-    _, _, (e_tick, e_adc, lam) = _fee_prob(params, wfs, stop_threshold, False, True)
-    return e_tick, e_adc, lam
+    lambda), each (P, MAX_ADC_VALUES).  Differentiable with respect to
+    ``wfs`` (lsim_fee_prob_vjp)."""
+    return _FeeProbRedFn.apply(_as_wfs(wfs), params, stop_threshold)
 
 
 def get_average_hit_values(ticks_prob, adcs_distrib):

@@ -880,3 +880,93 @@ def simulate_probabilistic(params, wfs, unique_pixels):
     px, py, plane, event = id2pixel(params, np.asarray(unique_pixels))
     pc = get_pixel_coordinates(params, px, py, plane)
     return adcs, pc[:, 0], pc[:, 1], log_prob, event
+
+
+# ---------------------------------------------------------------- probabilistic front end, float64, frozen
+
+def _ndtr64(x):
+    hs2 = 0.5 * np.sqrt(2.0)
+    w = x * hs2
+    z = np.abs(w)
+    return 0.5 * np.where(z < hs2, 1 + special.erf(w), np.where(w > 0, 2 - special.erfc(z), special.erfc(z)))
+
+
+def _log_ndtr64(x):
+    """The float32 piecewise form (segments at -10 and 5) in float64."""
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        upper = -_ndtr64(-x)
+        mid = np.log(_ndtr64(np.maximum(x, -10.0)))
+        xl = np.minimum(x, -10.0)
+        x2 = xl * xl
+        series = (1 + 3 / x2 ** 2) - (1 / x2 + 15 / x2 ** 3)
+        lower = -(x2 / 2) - np.log(-xl) - 0.5 * np.log(2 * np.pi) + np.log(series)
+    return np.where(x > 5, upper, np.where(x > -10, mid, lower))
+
+
+def _softplus64(y):
+    with np.errstate(over="ignore"):
+        return np.maximum(y, 0) + np.log1p(np.exp(-np.abs(y)))
+
+
+def _sigmoid64(x):
+    with np.errstate(over="ignore"):
+        return 1 / (1 + np.exp(-x))
+
+
+def _ldn64(a, b):
+    la, lb = _log_ndtr64(a), _log_ndtr64(b)
+    safe = np.where(a > b, lb - la, -1.0)
+    neg = -np.expm1(safe)
+    ns = 1e-30 + _softplus64((neg - 1e-30) * 1e10) / 1e10
+    with np.errstate(divide="ignore"):
+        lt = np.log(ns)
+    lts = -100 + _softplus64((lt + 100) * 10) / 10
+    w = _sigmoid64((a - b) * 1000)
+    return w * (la + lts) + (1 - w) * -1000.0
+
+
+def _lse64(x, axis):
+    m = np.max(x, axis=axis, keepdims=True)
+    return (np.log(np.sum(np.exp(x - m), axis=axis, keepdims=True)) + m).squeeze(axis)
+
+
+def beam_search64(params, wfs, top, n_exec):
+    """get_adc_values_average_noise_vmap (fee_jax.py:334-461) in float64 with
+    the top-K tick choices ``top`` (P, H, K) and the number of executed steps
+    held: (log_prob, charge), each (P, H, T-1).  Its derivatives are what
+    jax.grad takes through the beam search (test infrastructure for the
+    adjoint)."""
+    w = np.asarray(wfs, np.float64)
+    P, T = w.shape
+    K = int(params.fee_paths_scaling)
+    H = int(params.MAX_ADC_VALUES)
+    iv = fee_interval(params)
+    z = 1.0 / float(params.RESET_NOISE_CHARGE)
+    thr = float(params.DISCRIMINATION_THRESHOLD)
+    q = np.cumsum(w * float(params.t_sampling), axis=1)
+    cm = np.maximum.accumulate(q, axis=1)
+    t = np.arange(T - 1)
+    sh = np.minimum(t + iv + 1, T - 1)
+    esp = (q[:, sh] + thr) - 0.5 * (q[:, 1:] + q[:, :-1])
+    sw = _sigmoid64((esp - thr) * 10)
+    c = np.zeros((P, K))
+    lp = np.full((P, K), -1000.0)
+    lp[:, 0] = 0.0
+    out_lp = np.full((P, H, T - 1), -1000.0)
+    out_q = np.zeros((P, H, T - 1))
+    rows = np.arange(P)[:, None]
+    for h in range(n_exec):
+        zm = ((cm[:, None, :] - c[:, :, None]) - thr) * z
+        lg = _ldn64(zm[..., 1:], zm[..., :-1])
+        zq = ((q[:, None, :] - c[:, :, None]) - thr) * z
+        le = _ldn64(zq[..., sh], zq[..., :-1])
+        le = np.minimum(le, lg)
+        le = -1000.0 + _softplus64(le + 1000.0)
+        le = sw[:, None, :] * le + (1 - sw[:, None, :]) * -1000.0
+        out_lp[:, h] = _lse64(le + lp[:, :, None], axis=1)
+        out_q[:, h] = esp
+        dist = _lse64(lg + lp[:, :, None], axis=1)
+        tk = np.asarray(top[:, h], np.int64)
+        lp = dist[rows, tk]
+        c = q[rows, np.minimum(sh[tk] + 1, T - 1)]
+    return out_lp, out_q

@@ -197,6 +197,11 @@ def test_next_row_entry_points_reject_bad_arguments_without_gpu(lib):
     p0 = _abi.make_params(consts.Params(RESET_NOISE_CHARGE=0))
     assert lib.lsim_fee_prob(p0, V(16), 4, 2000, 20, 1e-9, None, None, None, None, None, ws, big,
                              None) == _abi.LSIM_ERR_INVALID            # noise width 0
+    assert lib.lsim_fee_prob_vjp(p, V(16), 4, 2000, 20, 1e-9, None, None, V(16), None, None, V(16), ws, big,
+                                 None) == _abi.LSIM_ERR_INVALID       # reduction cotangents: all three or none
+    assert lib.lsim_fee_prob_vjp(p, V(16), 4, 2000, 20, 1e-9, None, None, None, None, None, V(16), ws, 16,
+                                 None) == _abi.LSIM_ERR_CAPACITY
+    assert lib.lsim_fee_prob_vjp_workspace_bytes(p, 10, 20) >= 10 * int(p.max_adc_values) * 20 * 12
     # losses
     out = V(64)
     assert lib.lsim_mse_adc_workspace_bytes(1000, 900) > 4 * 1900
