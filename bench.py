@@ -559,6 +559,26 @@ def run_prob(args):
         out = [t.cpu() for t in sim.average_hit_values(params, host)]
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     H = int(params.MAX_ADC_VALUES)
+    # forward + adjoint with cotangents on the expected values (the collapsed-hit loss case)
+    wg = wfs.clone().requires_grad_(True)
+    cot = [torch.randn((P, H), device=wfs.device) for _ in range(3)]
+
+    def fwd_bwd():
+        wg.grad = None
+        et, ea, lam = sim.average_hit_values(params, wg)
+        torch.autograd.backward([et, ea, lam], cot)
+        return wg.grad
+
+    fwd_bwd()
+    torch.cuda.synchronize()
+    b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n_fb = 2
+    b0.record()
+    for _ in range(n_fb):
+        fwd_bwd()
+    b1.record()
+    torch.cuda.synchronize()
+    fb_ms = b0.elapsed_time(b1) / n_fb
     rec = {"metric": "probabilistic FEE pixels/s", "value": P / (ms * 1e-3), "unit": "pixels/s", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tracks and LUT)",
@@ -572,7 +592,10 @@ def run_prob(args):
            "roofline": {"bound": "issue", "kernel": "k_fee_prob",
                         "note": "transcendental-function bound (erf/erfc, log, exp, expm1 per path and tick); "
                                 "HBM traffic is the waveform read only"},
-           "gpu_launches": 2 * args.steps, "clocks": clk}
+           "gpu_launches": 2 * args.steps, "clocks": clk,
+           "fwd_bwd": {"ms": fb_ms, "pixels_per_s": P / (fb_ms * 1e-3),
+                       "note": "forward with the step paths recorded + lsim_fee_prob_vjp (per-tick reverse pass), "
+                               "cotangents on the expected tick, ADC and hit probability"}}
     if not args.no_cpu_baseline:
         from oracle import reference_np as R
         sample = wfs[:PROB_CPU_PIXELS].cpu().numpy()

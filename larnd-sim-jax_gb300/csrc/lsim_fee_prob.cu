@@ -882,7 +882,9 @@ int run_fee_prob_vjp(const LsimParams &p, const float *wfs, int64_t n_pix, int32
   const size_t smem = sizeof(float) * (11 * kProbMaxT + 2 * (kProbThreads / 32) * kProbMaxPaths);
   if (cudaFuncSetAttribute(k_fee_prob_vjp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return LSIM_ERR_CUDA;
-  const int64_t cap = device_sm_count();
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fee_prob_vjp, kProbThreads, smem);
+  const int64_t cap = (int64_t)device_sm_count() * (per_sm > 0 ? per_sm : 1);
   k_fee_prob_vjp<<<(unsigned)(n_pix < cap ? n_pix : cap), kProbThreads, smem, st>>>(va);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
