@@ -46,9 +46,9 @@ N_NEIGH, SIG_LEN = 4, 150
 PERTURB_SEED = 1234
 L2_FLUSH_BYTES = 512 << 20
 CPU_CHUNK = 150          # segments per CPU reference sample (one run per process)
-KERNELS_PER_STEP = 19   # stage 1: reset, segments, 3 scan, scatter, 2 sort; gradient: 3 template-order kernels,
-                        # main records, target index, pixels, main adjoint, 2 record reductions, target-only,
-                        # finalize
+KERNELS_PER_STEP = 20   # stage 1: reset, segments, 3 scan, scatter, 2 sort; gradient: 3 template-order kernels,
+                        # main records, heavy-pixel list, target index, pixels, main adjoint, 2 record reductions,
+                        # target-only, finalize (counted in the launch list of the step)
 # DRAM bytes per simulated pixel of one k_lut_pixels<grad> launch, from the
 # ncu capture summarised in profiles/k_lut_pixels_grad_8events.md (8 events,
 # 22,066 pixels; traffic scales with the pixel count)
