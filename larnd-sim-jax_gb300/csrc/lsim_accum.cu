@@ -565,6 +565,10 @@ __device__ __forceinline__ int32_t slot_pid(const LsimParams &p, const Grid &g, 
   return pixel2id(p, px, py, plane, (int)ev - 1);
 }
 
+// The persistent kernel hands out heavy pixels first (k_heavy_pixels) only
+// while at most 1 in kHeavyFractionInv pixels is heavy.
+constexpr int kHeavyFractionInv = 8;
+
 template <int MODE>
 __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a) {
   // kModeVjpWfs: the cotangent row comes from memory (no forward, no front end)
@@ -584,7 +588,11 @@ __global__ void __launch_bounds__(kAccWarps * kWarp, 5) k_lut_pixels(AccumArgs a
   const int T = NT - 1;
   const int H = p.max_adc_values;
   const int n_valid = a.w.counts->n_valid;
-  const int n_heavy = a.w.counts->n_heavy;
+  // heavy pixels first only while they are few: when most pixels are heavy
+  // (one dense event), grid order keeps neighbouring pixels, and their
+  // shared segments and LUT rows, together in time
+  const int n_heavy0 = a.w.counts->n_heavy;
+  const int n_heavy = n_heavy0 * kHeavyFractionInv > n_valid ? 0 : n_heavy0;
   const bool early_exit = (a.normals == nullptr) && p.threshold > 0.f;
   for (;;) {
     int r = 0;
