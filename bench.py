@@ -52,7 +52,7 @@ KERNELS_PER_STEP = 20   # stage 1: reset, segments, 3 scan, scatter, 2 sort; gra
 # DRAM bytes per simulated pixel of one k_lut_pixels<grad> launch, from the
 # ncu capture summarised in profiles/k_lut_pixels_grad_8events.md (8 events,
 # 22,066 pixels; traffic scales with the pixel count)
-PIXEL_KERNEL_DRAM_BYTES_PER_PIXEL = 13909   # 306.9 MB over 22,066 pixels
+PIXEL_KERNEL_DRAM_BYTES_PER_PIXEL = 13968   # 308.2 MB over 22,066 pixels
 
 
 def parse():
