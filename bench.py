@@ -64,14 +64,16 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--events", type=int, default=N_EVENTS, help="events per batch (profiling runs use fewer)")
-    ap.add_argument("--path", choices=["grad", "forward", "param", "param_grad", "chop", "prob", "loss"],
+    ap.add_argument("--hits", type=int, default=None, help="hits of --path records (profiling runs use fewer)")
+    ap.add_argument("--path", choices=["grad", "forward", "param", "param_grad", "chop", "prob", "loss", "records"],
                     default="grad",
                     help="grad: the fwd+bwd step (default); chop: on-device chop_tracks of one 500k-segment event; "
                          "prob: the probabilistic front end on the waveforms of 8 events; loss: mse_adc forward + "
                          "gradient on the hits of the 64-event batch; forward / param: the plain forward "
                          "drop-in (LUT mode / parametrised mode) on the 64-event batch; param_grad: the "
                          "parametrised-mode SSE-ADC loss and its gradient (autograd through the waveform, "
-                         "front-end and current-model adjoints)")
+                         "front-end and current-model adjoints); records: the driver's hit records (clean "
+                         "mask, compaction, charge, per-event runs) of 32M hits")
     return ap.parse_args()
 
 
@@ -888,8 +890,160 @@ def run_chop_reference(args):
           flush=True)
 
 
+# ---------------------------------------------------------------- output side
+
+RECORDS_HITS, RECORDS_EVENTS, RECORDS_CPU_HITS = 32_000_000, 1000, 4_000_000
+
+
+def _records_workload(n, seed=0):
+    """Hit columns of the shape simulate_stochastic returns: events sorted
+    (hits come out pixel-major, pixel ids packing the event), ADCs on the
+    digitisation range with 1% at the lowest ADC (dropped), 0.5% event -1."""
+    from larndsim_gb300 import consts, output
+    rng = np.random.default_rng(seed)
+    params = consts.Params()
+    ev = np.sort(rng.integers(0, RECORDS_EVENTS, n)).astype(np.int32)
+    ev[rng.random(n) < 0.005] = -1
+    adc = rng.uniform(75.8, 256, n).astype(np.float32)
+    adc[rng.random(n) < 0.01] = np.float32(output.adc_lowest(params))
+    cols = [adc, rng.uniform(-30, 30, n).astype(np.float32), rng.uniform(-60, 60, n).astype(np.float32),
+            rng.uniform(-30, 30, n).astype(np.float32), rng.integers(0, 1997, n).astype(np.float32),
+            np.ones(n, np.float32), ev, rng.integers(0, 1 << 30, n).astype(np.int32)]
+    return params, cols
+
+
+def run_records(args):
+    """Hit records of the simulate driver (optimize/simulate.py:129-176) on
+    32M synthetic hits of 1000 events.  value: input hits/s of
+    lsim_hit_records with the columns in HBM (6 launches: count, scan,
+    write, run count, run scan, run write); e2e: output.hit_records on pinned
+    host columns plus the copy of the records back to host memory."""
+    import torch
+    from larndsim_gb300 import _abi, output, sim
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _abi.load()
+    n = args.hits or RECORDS_HITS
+    params, cols = _records_workload(n)
+    din = [torch.from_numpy(c).to(dev) for c in cols]
+    names = ("adc", "pix_x", "pix_y", "pix_z", "ticks", "hit_prob", "event", "pixels")
+    dout = [torch.empty_like(c) for c in din]
+    clean, q = torch.empty(n, dtype=torch.float32, device=dev), torch.empty(n, dtype=torch.float32, device=dev)
+    run_event = torch.empty(n, dtype=torch.int32, device=dev)
+    run_start = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    counts = torch.zeros(2, dtype=torch.int64, device=dev)
+    ws = torch.empty(lib.lsim_hit_records_workspace_bytes(n), dtype=torch.uint8, device=dev)
+    lp = _abi.make_params(params)
+    lo = output.adc_lowest(params)
+    cin = _abi.LsimHitColumns(*[c.data_ptr() for c in din])
+    cout = _abi.LsimHitColumns(*[c.data_ptr() for c in dout])
+    s = sim._stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        _abi.check(lib, lib.lsim_hit_records(lp, lo, cin, n, cout, clean.data_ptr(), q.data_ptr(),
+                                             run_event.data_ptr(), run_start.data_ptr(), counts.data_ptr(),
+                                             ws.data_ptr(), ws.numel(), s))
+
+    for _ in range(args.warmup):
+        step()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(torch.cuda.current_device())
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        starts[i].record()
+        step()
+        ends[i].record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    kept, runs = (int(v) for v in counts.cpu().tolist())
+    ms = float(np.mean([a.elapsed_time(b) for a, b in zip(starts, ends)]))
+    host = [torch.from_numpy(c).pin_memory() for c in cols]
+    del din, dout, clean, q, run_event, run_start, ws
+
+    def e2e_step():
+        rec = output.hit_records(params, host)
+        return {k: v.cpu() for k, v in rec.items()}
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        back = e2e_step()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    d2h = int(sum(v.numel() * v.element_size() for v in back.values()))
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    algo = 32 * n + 40 * kept + 12 * runs + 8    # read 8 columns, write 10 kept columns and the runs
+    achieved = algo / (ms * 1e-3) / 1e9
+    rec = {"metric": "hit records hits/s", "value": n / (ms * 1e-3), "unit": "hits/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32/int32", "data": "synthetic (seeded hit columns)",
+           "config": {"workload": f"hit records (clean mask, compaction, charge, event runs) of {n} hits of "
+                                  f"{RECORDS_EVENTS} events", "hits": n, "kept": kept, "runs": runs,
+                      "l2": f"flushed between timed steps (512 MiB write); columns {32 * n / 1e9:.2f} GB in, "
+                            f"{40 * kept / 1e9:.2f} GB out"},
+           "e2e": {"value": n / e2e_s, "unit": "hits/s", "ms_per_step": e2e_s * 1e3,
+                   "h2d_bytes_per_step": int(sum(c.nbytes for c in cols)), "d2h_bytes_per_step": d2h},
+           "roofline": {"bound": "hbm", "kernel": "lsim_hit_records (6 launches timed together)",
+                        "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "algorithmic_bytes": algo,
+                        "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None},
+           "gpu_launches": 6 * args.steps, "clocks": clk}
+    if not args.no_cpu_baseline:
+        from oracle import reference_np as R
+        m = min(RECORDS_CPU_HITS, n)
+        t0 = time.perf_counter()
+        r = R.hit_records(params, *[c[:m] for c in cols])
+        R.hit_records_by_event(r)
+        dt = time.perf_counter() - t0
+        rec["cpu_baseline"] = {"value": m / dt, "unit": "hits/s", "cores": 1, "kind": "port",
+                               "sample": f"first {m} hits: numpy restatement (mask, compaction, charge, "
+                                         f"per-event split), {dt:.2f} s"}
+    print(json.dumps(rec), flush=True)
+
+
+def run_records_reference(args):
+    """CPU arm of --path records: the numpy restatement (mask, compaction,
+    charge and the per-event split of simulate.py:129-156) on the first 4M
+    hits of the same columns per step."""
+    if dist_env()[0] != 0:
+        return
+    from oracle import reference_np as R
+    params, cols = _records_workload(RECORDS_HITS)
+    m = RECORDS_CPU_HITS
+    sample = [c[:m] for c in cols]
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        R.hit_records_by_event(R.hit_records(params, *sample))
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    ms = float(np.mean(times)) * 1e3
+    value = m / (ms * 1e-3)
+    print(json.dumps({"metric": "hit records hits/s", "value": value, "unit": "hits/s", "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f32/int32", "impl": "reference",
+                      "data": "synthetic (seeded hit columns)",
+                      "config": {"workload": f"hit records of the first {m} of {RECORDS_HITS} hits"},
+                      "cpu_baseline": {"value": value, "unit": "hits/s", "cores": 1, "kind": "port",
+                                       "sample": f"{m} hits per step"},
+                      "e2e": {"value": value, "unit": "hits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
 def main():
     args = parse()
+    if args.path == "records":
+        (run_records_reference if args.impl == "reference" else run_records)(args)
+        return
     if args.path == "param_grad":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "param_grad path: no CPU arm"}))

@@ -301,6 +301,43 @@ int lsim_hits_noalloc(const LsimParams *p, const float *adc, const float *ticks,
                       float *out_z, float *out_ticks, float *out_hit_prob, int32_t *out_event,
                       int32_t *out_pixels, int32_t *nb_valid_dev, void *stream);
 
+/* ---------------------------------------------------------------- output side */
+
+/* One set of hit columns, each of one entry per hit (the 8 outputs of
+ * simulate_stochastic / simulate_parametrized, src/larndsim/sim_jax.py:738-769
+ * and :339-372, in that order).  Read-only where it is an input. */
+typedef struct LsimHitColumns {
+  float *adc;
+  float *pixel_x, *pixel_y, *pixel_z;
+  float *ticks, *hit_prob;
+  int32_t *event, *pixels;
+} LsimHitColumns;
+
+/* Workspace bytes of lsim_hit_records for n hits. */
+size_t lsim_hit_records_workspace_bytes(int64_t n);
+
+/* The hit records the simulate driver writes, optimize/simulate.py:129-176:
+ * keep hit i when adc[i] - adc_lowest != 0 and event[i] != -1 (adc_lowest =
+ * digitize(params, DISCRIMINATION_THRESHOLD), computed by the caller as the
+ * reference does once per run), in input order.  For the kept rows write
+ * out->event (required) and every other non-NULL column of *out (its input
+ * column must then be non-NULL), the cleaned ADC adc - adc_lowest to
+ * out_adc_clean and the charge adc2charge(adc) in ke-
+ * (src/larndsim/losses_jax.py:380-383) to out_q (either may be NULL).
+ * With run_start non-NULL, also list the runs of equal event in the kept
+ * rows: run_event[r] (may be NULL) and run_start[r] for each run r, and
+ * run_start[n_runs] = n_kept, which splits the records per event like the
+ * reference's per-event groups (simulate.py:139-166) when, as in the
+ * simulation's own output, the hits of each event are contiguous.
+ * counts_dev (int64[2], device memory) receives n_kept and n_runs.  Output
+ * columns hold n entries, run_event n and run_start n + 1.  The cleaned ADC
+ * is one float32 subtraction; the charge is computed in the form XLA gave
+ * adc2charge for the reference's committed outputs (folded constants, one
+ * fused multiply-add), which reproduces their charges bit for bit. */
+int lsim_hit_records(const LsimParams *p, float adc_lowest, const LsimHitColumns *in, int64_t n,
+                     const LsimHitColumns *out, float *out_adc_clean, float *out_q, int32_t *run_event,
+                     int64_t *run_start, int64_t *counts_dev, void *ws, size_t ws_bytes, void *stream);
+
 /* ---------------------------------------------------------------- input side */
 
 /* Workspace bytes of lsim_chop_tracks for n_rows input tracks. */

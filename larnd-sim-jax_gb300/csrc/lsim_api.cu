@@ -490,6 +490,29 @@ int lsim_chop_tracks(const LsimFieldMap *f, const float *tracks, int64_t n_rows,
               "lsim_chop_tracks");
 }
 
+size_t lsim_hit_records_workspace_bytes(int64_t n) { return n < 0 ? 0 : records_workspace_bytes(n); }
+
+int lsim_hit_records(const LsimParams *p, float adc_lowest, const LsimHitColumns *in, int64_t n,
+                     const LsimHitColumns *out, float *out_adc_clean, float *out_q, int32_t *run_event,
+                     int64_t *run_start, int64_t *counts_dev, void *ws, size_t ws_bytes, void *stream) {
+  g_err.clear();
+  if (!p) return fail(LSIM_ERR_INVALID, "lsim_hit_records: null parameter block");
+  if (!in || !out || !counts_dev || n < 0) return fail(LSIM_ERR_INVALID, "lsim_hit_records: bad arguments");
+  if (n > 0) {
+    if (!in->adc || !in->event || !out->event) return fail(LSIM_ERR_INVALID, "lsim_hit_records: adc and event columns are required");
+    const bool missing = (out->pixel_x && !in->pixel_x) || (out->pixel_y && !in->pixel_y) ||
+                         (out->pixel_z && !in->pixel_z) || (out->ticks && !in->ticks) ||
+                         (out->hit_prob && !in->hit_prob) || (out->pixels && !in->pixels);
+    if (missing) return fail(LSIM_ERR_INVALID, "lsim_hit_records: an output column has no input column");
+  }
+  if (run_event && !run_start) return fail(LSIM_ERR_INVALID, "lsim_hit_records: run_event needs run_start");
+  if (n > 0 && (!ws || ws_bytes < records_workspace_bytes(n)))
+    return fail(LSIM_ERR_CAPACITY, "lsim_hit_records: workspace %zu < %zu bytes", ws_bytes, records_workspace_bytes(n));
+  return wrap(run_records(*p, adc_lowest, *in, n, *out, out_adc_clean, out_q, run_event, run_start, counts_dev, ws,
+                          (cudaStream_t)stream),
+              "lsim_hit_records");
+}
+
 size_t lsim_hits_workspace_bytes(int64_t n_pix, int32_t max_adc_values) {
   return hits_ws_bytes(n_pix * (int64_t)max_adc_values);
 }

@@ -64,32 +64,6 @@ __device__ __forceinline__ int64_t block_sum_i64(int64_t v, int64_t *red) {
   return t;
 }
 
-// Inclusive block scan of one int64 per thread; returns the inclusive
-// prefix, *total gets the block total.
-__device__ __forceinline__ int64_t block_scan_i64(int64_t v, int64_t *warp_tot, int64_t *total) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  int64_t x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int64_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) warp_tot[wid] = x;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int64_t run = 0;
-    for (int i = 0; i < nw; ++i) {
-      int64_t t = warp_tot[i];
-      warp_tot[i] = run;
-      run += t;
-    }
-    *total = run;
-  }
-  __syncthreads();
-  x += warp_tot[wid];
-  return x;
-}
-
 __global__ void __launch_bounds__(kChopThreads) k_chop_count(const float *__restrict__ tracks, int64_t n_rows,
                                                              LsimFieldMap f, float prec32,
                                                              int64_t *__restrict__ row_n,

@@ -289,6 +289,33 @@ __device__ __forceinline__ int searchsorted_left(const float *grid, int n, float
   return lo;
 }
 
+// Inclusive block scan of one int64 per thread (blockDim.x a multiple of 32,
+// at most 1024); returns the inclusive prefix, *total gets the block total.
+// warp_tot holds blockDim.x / 32 entries.
+__device__ __forceinline__ int64_t block_scan_i64(int64_t v, int64_t *warp_tot, int64_t *total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[wid] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t run = 0;
+    for (int i = 0; i < nw; ++i) {
+      int64_t t = warp_tot[i];
+      warp_tot[i] = run;
+      run += t;
+    }
+    *total = run;
+  }
+  __syncthreads();
+  x += warp_tot[wid];
+  return x;
+}
+
 __device__ __forceinline__ void set_status(LsimCounts *c, int code, int row) {
   atomicCAS(&c->status, 0, code);
   atomicMin(&c->bad_row, row);

@@ -92,6 +92,12 @@ int run_fee_prob_vjp(const LsimParams &p, const float *wfs, int64_t n_pix, int32
                      float stop_threshold, const float *g_log_prob, const float *g_charge, const float *g_e_tick,
                      const float *g_e_adc, const float *g_lam, float *g_wfs, void *ws, cudaStream_t st);
 
+// lsim_records.cu
+size_t records_workspace_bytes(int64_t n);
+int run_records(const LsimParams &p, float adc_lowest, const LsimHitColumns &in, int64_t n, const LsimHitColumns &out,
+                float *out_clean, float *out_q, int32_t *run_event, int64_t *run_start, int64_t *counts, void *ws,
+                cudaStream_t st);
+
 // lsim_chop.cu
 size_t chop_workspace_bytes(int64_t n_rows);
 int run_chop(const LsimFieldMap &f, const float *tracks, int64_t n_rows, double precision, float *out,

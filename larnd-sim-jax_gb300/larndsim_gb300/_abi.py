@@ -31,6 +31,12 @@ class LsimFieldMap(C.Structure):
         "dx", "dE", "dEdx")]
 
 
+class LsimHitColumns(C.Structure):
+    """Device pointers of the 8 hit columns (NULL = column not used)."""
+    _fields_ = [(n, C.c_void_p) for n in ("adc", "pixel_x", "pixel_y", "pixel_z", "ticks", "hit_prob", "event",
+                                         "pixels")]
+
+
 class LsimParams(C.Structure):
     _fields_ = [
         ("recombination_mode", C.c_int32),
@@ -111,6 +117,9 @@ _SIGNATURES = {
     "lsim_chamfer_workspace_bytes": (_sz, [_i64, _i64]),
     "lsim_chamfer_3d": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
                                   _sz, _vp]),
+    "lsim_hit_records_workspace_bytes": (_sz, [_i64]),
+    "lsim_hit_records": (C.c_int, [_PP, C.c_float, C.POINTER(LsimHitColumns), _i64, C.POINTER(LsimHitColumns), _vp,
+                                   _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "lsim_chop_workspace_bytes": (_sz, [_i64]),
     "lsim_chop_tracks": (C.c_int, [_PF, _vp, _i64, C.c_double, _vp, _i64, _vp, _vp, _sz, _vp]),
     "lsim_param_stage1": (C.c_int, [_PP, _PF, _vp, _i64, _i32, _vp, _vp, _sz, _vp, _vp]),

@@ -499,6 +499,66 @@ def simulate_stochastic(params, wfs, unique_pixels, normals=None):
     return out
 
 
+# ---------------------------------------------------------------- output side
+
+HIT_RECORD_FIELDS = ("adc_clean", "adc", "Q", "pixels", "ticks", "eventID", "pix_x", "pix_y", "pix_z")
+
+
+def adc2charge_xla(dw, params):
+    """adc2charge (losses_jax.py:380-383) in the form XLA compiled it to for
+    the reference's committed outputs (output/jax_ref/output_*_1.npz): folded
+    constants and one fused multiply-add, fma(dw / ADC_COUNTS, V_REF - V_CM,
+    V_CM - V_PEDESTAL) * (1e-3 / GAIN); reproduces their charges bit for bit
+    (tests/test_oracle_golden.py).  The fma is evaluated exactly in float64
+    (a float32 product fits in 48 bits) and rounded once to float32."""
+    a = np.asarray(dw, F32) * (F32(1) / F32(params.ADC_COUNTS))
+    c = F32(params.V_REF - params.V_CM)
+    d = F32(params.V_CM) - F32(params.V_PEDESTAL)
+    f = (a.astype(np.float64) * np.float64(c) + np.float64(d)).astype(F32)
+    return (f * (F32(1e-3) / F32(params.GAIN))).astype(F32)
+
+
+def hit_records(params, adcs, pixel_x, pixel_y, pixel_z, ticks, hit_prob, event, hit_pixels, adc_lowest=None):
+    """optimize/simulate.py:129-133: the kept hit rows of one batch.
+
+    adc_lowest = digitize(DISCRIMINATION_THRESHOLD); a hit is kept when
+    adc - adc_lowest != 0 and its event is not -1.  Returns a dict of the
+    kept columns (input order) with the cleaned ADC and the charge in ke-
+    (adc2charge_xla, the form the committed outputs pin).
+    """
+    adcs = np.asarray(adcs, F32).reshape(-1)
+    event = np.asarray(event).reshape(-1)
+    lowest = F32(digitize(params, F32(params.DISCRIMINATION_THRESHOLD))) if adc_lowest is None else F32(adc_lowest)
+    clean = (adcs - lowest).astype(F32)
+    mask = (clean != 0) & (event != -1)
+    return {
+        "adc_clean": clean[mask], "adc": adcs[mask], "Q": adc2charge_xla(adcs[mask], params),
+        "pix_x": np.asarray(pixel_x, F32).reshape(-1)[mask], "pix_y": np.asarray(pixel_y, F32).reshape(-1)[mask],
+        "pix_z": np.asarray(pixel_z, F32).reshape(-1)[mask], "ticks": np.asarray(ticks, F32).reshape(-1)[mask],
+        "hit_prob": np.asarray(hit_prob, F32).reshape(-1)[mask], "event": event[mask],
+        "pixels": np.asarray(hit_pixels).reshape(-1)[mask],
+    }
+
+
+def hit_records_by_event(records, local_to_global=None):
+    """optimize/simulate.py:139-156: one group per local event id >= 0 of the
+    kept rows (np.unique order), keyed by the global event id, with the
+    reference's dataset names; eventID is int64 filled with the global id."""
+    groups = {}
+    ev = records["event"]
+    for local in np.unique(ev).astype(int):
+        if local < 0:
+            continue
+        g = (local_to_global or {}).get(local, local)
+        m = ev == local
+        grp = {name: records[key][m] for name, key in (("adc_clean", "adc_clean"), ("adc", "adc"), ("Q", "Q"),
+                                                       ("pixels", "pixels"), ("ticks", "ticks"),
+                                                       ("pix_x", "pix_x"), ("pix_y", "pix_y"), ("pix_z", "pix_z"))}
+        grp["eventID"] = np.full(int(m.sum()), g, dtype=np.int64)
+        groups[int(g)] = grp
+    return groups
+
+
 # ---------------------------------------------------------------- parametrised mode
 
 def generate_electrons(params, tracks, fields, normals):

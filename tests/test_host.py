@@ -234,3 +234,23 @@ def test_next_row_entry_points_reject_bad_arguments_without_gpu(lib):
     assert lib.lsim_fee_vjp(p, V(16), 4, 2002, None, V(16), V(16), ws, big, None) == _abi.LSIM_ERR_UNSUPPORTED
     assert lib.lsim_fee_vjp(p, V(16), 4, 2000, None, None, V(16), ws, big, None) == _abi.LSIM_ERR_INVALID
     assert lib.lsim_fee_vjp(p, V(16), 4, 2000, None, V(16), V(16), ws, 16, None) == _abi.LSIM_ERR_CAPACITY
+
+
+def test_hit_records_rejects_bad_arguments_without_gpu(lib):
+    V = ctypes.c_void_p
+    p = _abi.make_params(consts.Params())
+    cols = _abi.LsimHitColumns(16, 16, 16, 16, 16, 16, 16, 16)
+    no_pix = _abi.LsimHitColumns(16, 16, 16, 16, 16, 16, 16, None)
+    counts = V(64)
+    assert lib.lsim_hit_records_workspace_bytes(3_000_000) >= 2 * 8 * (3_000_000 // 1024)
+    assert lib.lsim_hit_records(None, 80.0, cols, 10, cols, None, None, None, None, counts, V(256), 1 << 20,
+                                None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_hit_records(p, 80.0, cols, 10, cols, None, None, None, None, None, V(256), 1 << 20,
+                                None) == _abi.LSIM_ERR_INVALID                  # counts required
+    assert lib.lsim_hit_records(p, 80.0, no_pix, 10, cols, None, None, None, None, counts, V(256), 1 << 20,
+                                None) == _abi.LSIM_ERR_INVALID                  # output column without input
+    assert lib.lsim_hit_records(p, 80.0, cols, 10, cols, None, None, V(16), None, counts, V(256), 1 << 20,
+                                None) == _abi.LSIM_ERR_INVALID                  # run_event without run_start
+    assert lib.lsim_hit_records(p, 80.0, cols, 10, cols, None, None, None, None, counts, V(256), 8,
+                                None) == _abi.LSIM_ERR_CAPACITY
+    assert b"workspace" in lib.lsim_last_error()
