@@ -915,9 +915,9 @@ def _records_workload(n, seed=0):
 def run_records(args):
     """Hit records of the simulate driver (optimize/simulate.py:129-176) on
     32M synthetic hits of 1000 events.  value: input hits/s of
-    lsim_hit_records with the columns in HBM (6 launches: count, scan,
-    write, run count, run scan, run write); e2e: output.hit_records on pinned
-    host columns plus the copy of the records back to host memory."""
+    lsim_hit_records with the columns in HBM (3 launches: tile summaries,
+    scan, write); e2e: output.hit_records on pinned host columns plus the
+    copy of the records back to host memory."""
     import torch
     from larndsim_gb300 import _abi, output, sim
     rank, world, local = dist_env()
@@ -992,11 +992,11 @@ def run_records(args):
                             f"{40 * kept / 1e9:.2f} GB out"},
            "e2e": {"value": n / e2e_s, "unit": "hits/s", "ms_per_step": e2e_s * 1e3,
                    "h2d_bytes_per_step": int(sum(c.nbytes for c in cols)), "d2h_bytes_per_step": d2h},
-           "roofline": {"bound": "hbm", "kernel": "lsim_hit_records (6 launches timed together)",
+           "roofline": {"bound": "hbm", "kernel": "lsim_hit_records (3 launches timed together)",
                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "algorithmic_bytes": algo,
                         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None},
-           "gpu_launches": 6 * args.steps, "clocks": clk}
+           "gpu_launches": 3 * args.steps, "clocks": clk}
     if not args.no_cpu_baseline:
         from oracle import reference_np as R
         m = min(RECORDS_CPU_HITS, n)

@@ -329,7 +329,8 @@ size_t lsim_hit_records_workspace_bytes(int64_t n);
  * run_start[n_runs] = n_kept, which splits the records per event like the
  * reference's per-event groups (simulate.py:139-166) when, as in the
  * simulation's own output, the hits of each event are contiguous.
- * counts_dev (int64[2], device memory) receives n_kept and n_runs.  Output
+ * counts_dev (int64[2], device memory) receives n_kept and n_runs (the
+ * runs are counted whether or not run_start is given).  Output
  * columns hold n entries, run_event n and run_start n + 1.  The cleaned ADC
  * is one float32 subtraction; the charge is computed in the form XLA gave
  * adc2charge for the reference's committed outputs (folded constants, one

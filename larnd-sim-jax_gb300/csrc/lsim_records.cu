@@ -3,24 +3,55 @@
 // rows whose ADC differs from the lowest ADC, digitize(threshold), and whose
 // event is not -1; write the kept rows' columns, the cleaned ADC
 // (adc - adc_lowest) and the charge in ke- (adc2charge, losses_jax.py:380-383),
-// then list the runs of equal event id in the kept rows (start offset and
+// and list the runs of equal event id in the kept rows (start offset and
 // event of each run), which is what splitting the output per event needs.
 //
-// Six launches, all over tiles of 1024 rows: count the kept rows per tile,
-// one CTA scanning the tile counts (kept total to counts[0]), a write pass
-// that recomputes the keep flag and stores every requested column at its
-// compacted position; then the same three steps over the compacted event
-// column for the run starts (run total to counts[1], run_start[n_runs] =
-// counts[0]).  The run kernels read the kept count from device memory, so
-// the whole sequence runs without a host synchronisation.  All arithmetic
-// uses _rn intrinsics, so the compiler contracts nothing beyond the one FMA
-// written out in adc_to_charge.
+// Three launches over tiles of 1024 hits (256 threads x 4 sub-tiles):
+//   k_rec_tiles  reads adc and event and summarises each tile: kept rows,
+//                run heads whose previous kept row is in the tile, first
+//                and last kept event;
+//   k_rec_scan   one CTA: exclusive row and run offsets per tile and the
+//                last kept event before it (kept and run totals to counts,
+//                run_start[n_runs] = n_kept);
+//   k_rec_write  loads all requested columns of its tile up front, ranks the
+//                kept rows and the run heads (ballots, one warp combining the
+//                32 warp-parts of the tile) and stores both.
+// A run head is a kept row whose previous kept row has another event (or
+// the first kept row).  Traffic: 8 B per hit in the summary pass, the input
+// columns once and the kept rows' outputs once in the write pass.  The
+// rounding: every operation is a _rn intrinsic, so the compiler contracts
+// nothing beyond the one FMA written out in adc_to_charge.
 #include "lsim_internal.cuh"
 
 namespace lsim {
 namespace {
 
-constexpr int kRecTile = 1024;  // rows per block
+constexpr int kRecThreads = 256;                   // threads per block
+constexpr int kRecSub = 4;                         // sub-tiles of kRecThreads rows per tile
+constexpr int kRecTile = kRecThreads * kRecSub;    // 1024 rows per tile
+constexpr int kRecWarps = kRecThreads / kWarp;     // 8
+constexpr int kRecParts = kRecSub * kRecWarps;     // 32 warp-parts of 32 rows, one lane of a warp each
+constexpr int kRecScanThreads = 1024;
+constexpr unsigned kFull = 0xffffffffu;
+static_assert(kRecParts == kWarp, "one combining lane per warp-part");
+
+struct TileSum {
+  int32_t kept;      // kept rows
+  int32_t heads;     // run heads whose previous kept row lies in the tile
+  int32_t first_ev;  // event of the first / last kept row (kept > 0)
+  int32_t last_ev;
+};
+
+struct TileOff {
+  int64_t row;       // kept rows before the tile
+  int64_t run;       // runs starting before the tile
+  int32_t prev_ev;   // event of the last kept row before the tile (has_prev)
+  int32_t has_prev;
+};
+
+struct Part {
+  int kept, heads, first_ev, last_ev;
+};
 
 __device__ __forceinline__ bool rec_keep(float adc, int32_t event, float adc_lowest) {
   return __fsub_rn(adc, adc_lowest) != 0.f && event != -1;
@@ -39,123 +70,230 @@ __device__ __forceinline__ float adc_to_charge(const LsimParams &p, float dw) {
   return __fmul_rn(__fmaf_rn(__fmul_rn(dw, inv_counts), p.vref_minus_cm, offset), scale);
 }
 
-// Number of flagged rows of this block's tile, summed over its warps.
-__device__ __forceinline__ int64_t tile_count(bool flag) {
-  __shared__ int warp_n[kRecTile / kWarp];
-  const unsigned bal = __ballot_sync(0xffffffffu, flag);
-  if ((threadIdx.x & 31) == 0) warp_n[threadIdx.x >> 5] = __popc(bal);
-  __syncthreads();
-  int64_t s = 0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < kRecTile / kWarp; ++w) s += warp_n[w];
-  return s;
+__device__ __forceinline__ unsigned lanes_below() { return (1u << (threadIdx.x & 31)) - 1u; }
+
+// One warp's 32 rows: the ballot of kept rows, for each lane whether a kept
+// row precedes it in the warp and that row's event, and the part summary.
+__device__ __forceinline__ Part warp_part(bool keep, int ev, unsigned &bal, bool &has_prev, int &prev_ev) {
+  bal = __ballot_sync(kFull, keep);
+  const unsigned before = bal & lanes_below();
+  prev_ev = __shfl_sync(kFull, ev, before ? 31 - __clz(before) : 0);
+  has_prev = before != 0;
+  const unsigned heads = __ballot_sync(kFull, keep && has_prev && ev != prev_ev);
+  Part q;
+  q.kept = __popc(bal);
+  q.heads = __popc(heads);
+  q.first_ev = __shfl_sync(kFull, ev, bal ? __ffs(bal) - 1 : 0);
+  q.last_ev = __shfl_sync(kFull, ev, bal ? 31 - __clz(bal) : 0);
+  return q;
 }
 
-// Position of a flagged row among the flagged rows of its tile.
-__device__ __forceinline__ int64_t tile_rank(bool flag) {
-  __shared__ int warp_n[kRecTile / kWarp];
-  const unsigned bal = __ballot_sync(0xffffffffu, flag);
+__device__ __forceinline__ int warp_incl_sum(int v) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, v, o);
+    if ((int)(threadIdx.x & 31) >= o) v += y;
+  }
+  return v;
+}
+
+// Lane p of one warp holds part p of the tile (parts in row order).  Gives
+// the last kept event of the parts before p within the tile.
+__device__ __forceinline__ bool prior_part(const Part &q, int &prior_last) {
+  const unsigned kb = __ballot_sync(kFull, q.kept > 0);
+  const unsigned before = kb & lanes_below();
+  prior_last = __shfl_sync(kFull, q.last_ev, before ? 31 - __clz(before) : 0);
+  return before != 0;
+}
+
+__global__ void __launch_bounds__(kRecThreads) k_rec_tiles(const float *__restrict__ adc,
+                                                           const int32_t *__restrict__ event, int64_t n,
+                                                           float adc_lowest, TileSum *__restrict__ sums) {
+  __shared__ Part parts[kRecParts];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) warp_n[wid] = __popc(bal);
+  const int64_t base = (int64_t)blockIdx.x * kRecTile + threadIdx.x;
+  float a[kRecSub];
+  int e[kRecSub];
+#pragma unroll
+  for (int s = 0; s < kRecSub; ++s) {
+    const int64_t i = base + s * kRecThreads;
+    a[s] = i < n ? adc[i] : adc_lowest;
+    e[s] = i < n ? event[i] : -1;
+  }
+#pragma unroll
+  for (int s = 0; s < kRecSub; ++s) {
+    unsigned bal;
+    bool hp;
+    int pe;
+    const Part q = warp_part(rec_keep(a[s], e[s], adc_lowest), e[s], bal, hp, pe);
+    if (lane == 0) parts[s * kRecWarps + wid] = q;
+  }
   __syncthreads();
-  int ofs = 0;
-  for (int w = 0; w < wid; ++w) ofs += warp_n[w];
-  return ofs + __popc(bal & ((1u << lane) - 1u));
+  if (wid != 0) return;
+  const Part q = parts[lane];
+  int prior_last;
+  const bool has_prior = prior_part(q, prior_last);
+  const int boundary = q.kept > 0 && has_prior && q.first_ev != prior_last;
+  const int kept = __reduce_add_sync(kFull, (unsigned)q.kept);
+  const int heads = __reduce_add_sync(kFull, (unsigned)(q.heads + boundary));
+  const unsigned kb = __ballot_sync(kFull, q.kept > 0);
+  const int first = __shfl_sync(kFull, q.first_ev, kb ? __ffs(kb) - 1 : 0);
+  const int last = __shfl_sync(kFull, q.last_ev, kb ? 31 - __clz(kb) : 0);
+  if (lane == 0) sums[blockIdx.x] = TileSum{kept, heads, first, last};
 }
 
-__global__ void __launch_bounds__(kRecTile) k_rec_count(const float *__restrict__ adc,
-                                                        const int32_t *__restrict__ event, int64_t n,
-                                                        float adc_lowest, int64_t *__restrict__ tile_n) {
-  const int64_t i = (int64_t)blockIdx.x * kRecTile + threadIdx.x;
-  const bool keep = i < n && rec_keep(adc[i], event[i], adc_lowest);
-  const int64_t s = tile_count(keep);
-  if (threadIdx.x == 0) tile_n[blockIdx.x] = s;
+// Inclusive block scan (sum, or max with identity `ident`) of one int64 per
+// thread; *total gets the block's sum / max.  The caller synchronises before
+// warp_tot or *total are written again.
+template <bool kMax>
+__device__ __forceinline__ int64_t block_incl_scan(int64_t v, int64_t ident, int64_t *warp_tot, int64_t *total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x = kMax ? (y > x ? y : x) : x + y;
+  }
+  if (lane == 31) warp_tot[wid] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t run = ident;
+    for (int i = 0; i < nw; ++i) {
+      const int64_t t = warp_tot[i];
+      warp_tot[i] = run;
+      run = kMax ? (t > run ? t : run) : run + t;
+    }
+    *total = run;
+  }
+  __syncthreads();
+  const int64_t c = warp_tot[wid];
+  return kMax ? (c > x ? c : x) : x + c;
 }
 
-// Exclusive scan of the tile counts in place; *total gets the sum.  When
-// run_start is given, run_start[sum] = *sentinel (the kept-row count).
-__global__ void __launch_bounds__(kRecTile) k_rec_scan(int64_t *__restrict__ tile_n, int64_t n_tiles,
-                                                       int64_t *__restrict__ total, int64_t *__restrict__ run_start,
-                                                       const int64_t *__restrict__ sentinel) {
-  __shared__ int64_t warp_tot[kRecTile / kWarp];
-  __shared__ int64_t chunk_total;
-  int64_t carry = 0;
-  for (int64_t base = 0; base < n_tiles; base += blockDim.x) {
-    const int64_t i = base + threadIdx.x;
-    const int64_t v = i < n_tiles ? tile_n[i] : 0;
-    const int64_t inc = block_scan_i64(v, warp_tot, &chunk_total);
-    if (i < n_tiles) tile_n[i] = carry + inc - v;
+// The last kept event before each tile is found by a max-scan of
+// (tile index << 32 | event) over the tiles with kept rows.
+__device__ __forceinline__ int64_t pack_last(int64_t tile, int32_t ev) {
+  return (int64_t)((uint64_t)tile << 32 | (uint32_t)ev);
+}
+
+__global__ void __launch_bounds__(kRecScanThreads) k_rec_scan(const TileSum *__restrict__ sums, int64_t n_tiles,
+                                                           TileOff *__restrict__ offs, int64_t *__restrict__ counts,
+                                                           int64_t *__restrict__ run_start) {
+  __shared__ int64_t wt_last[32], wt_rows[32], wt_runs[32];
+  __shared__ int64_t tot_last, tot_rows, tot_runs;
+  __shared__ int64_t incl_last[kRecScanThreads];
+  const int64_t kNone = INT64_MIN;
+  int64_t carry_rows = 0, carry_runs = 0, carry_last = kNone;
+  TileSum next = threadIdx.x < n_tiles ? sums[threadIdx.x] : TileSum{0, 0, 0, 0};
+  for (int64_t base = 0; base < n_tiles; base += kRecScanThreads) {
+    const int64_t t = base + threadIdx.x;
+    const TileSum ts = next;
+    const int64_t tn = t + kRecScanThreads;
+    next = tn < n_tiles ? sums[tn] : TileSum{0, 0, 0, 0};
+    const int64_t key = ts.kept > 0 ? pack_last(t, ts.last_ev) : kNone;
+    int64_t il = block_incl_scan<true>(key, kNone, wt_last, &tot_last);
+    il = il > carry_last ? il : carry_last;
+    incl_last[threadIdx.x] = il;
     __syncthreads();
-    carry += chunk_total;
+    const int64_t prev = threadIdx.x > 0 ? incl_last[threadIdx.x - 1] : carry_last;
+    const bool has_prev = prev != kNone;
+    const int32_t prev_ev = has_prev ? (int32_t)(uint32_t)(uint64_t)prev : 0;
+    const int64_t runs = ts.kept > 0 ? ts.heads + ((!has_prev || ts.first_ev != prev_ev) ? 1 : 0) : 0;
+    const int64_t ir = block_incl_scan<false>(ts.kept, 0, wt_rows, &tot_rows);
+    const int64_t iu = block_incl_scan<false>(runs, 0, wt_runs, &tot_runs);
+    if (t < n_tiles) offs[t] = TileOff{carry_rows + ir - ts.kept, carry_runs + iu - runs, prev_ev, has_prev ? 1 : 0};
+    carry_rows += tot_rows;
+    carry_runs += tot_runs;
+    carry_last = tot_last > carry_last ? tot_last : carry_last;
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    *total = carry;
-    if (run_start) run_start[carry] = *sentinel;
+    counts[0] = carry_rows;
+    counts[1] = carry_runs;
+    if (run_start) run_start[carry_runs] = carry_rows;
   }
 }
 
-__global__ void __launch_bounds__(kRecTile) k_rec_write(LsimParams p, LsimHitColumns in, int64_t n, float adc_lowest,
-                                                        const int64_t *__restrict__ tile_off, LsimHitColumns out,
-                                                        float *__restrict__ out_clean, float *__restrict__ out_q) {
-  const int64_t i = (int64_t)blockIdx.x * kRecTile + threadIdx.x;
-  float a = 0.f;
-  int32_t ev = -1;
-  if (i < n) {
-    a = in.adc[i];
-    ev = in.event[i];
+__global__ void __launch_bounds__(kRecThreads) k_rec_write(LsimParams p, LsimHitColumns in, int64_t n,
+                                                           float adc_lowest, const TileOff *__restrict__ offs,
+                                                           LsimHitColumns out, float *__restrict__ out_clean,
+                                                           float *__restrict__ out_q, int32_t *__restrict__ run_event,
+                                                           int64_t *__restrict__ run_start) {
+  __shared__ Part parts[kRecParts];
+  __shared__ int part_row[kRecParts], part_run[kRecParts], part_prev_ev[kRecParts];
+  __shared__ bool part_prev_has[kRecParts];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t base = (int64_t)blockIdx.x * kRecTile + threadIdx.x;
+  float a[kRecSub], x[kRecSub], y[kRecSub], z[kRecSub], tk[kRecSub], hp[kRecSub];
+  int ev[kRecSub], px[kRecSub];
+#pragma unroll
+  for (int s = 0; s < kRecSub; ++s) {
+    const int64_t i = base + s * kRecThreads;
+    const bool in_range = i < n;
+    a[s] = in_range ? in.adc[i] : adc_lowest;
+    ev[s] = in_range ? in.event[i] : -1;
+    x[s] = in_range && out.pixel_x ? in.pixel_x[i] : 0.f;
+    y[s] = in_range && out.pixel_y ? in.pixel_y[i] : 0.f;
+    z[s] = in_range && out.pixel_z ? in.pixel_z[i] : 0.f;
+    tk[s] = in_range && out.ticks ? in.ticks[i] : 0.f;
+    hp[s] = in_range && out.hit_prob ? in.hit_prob[i] : 0.f;
+    px[s] = in_range && out.pixels ? in.pixels[i] : 0;
   }
-  const bool keep = i < n && rec_keep(a, ev, adc_lowest);
-  const int64_t r = tile_rank(keep);
-  if (!keep) return;
-  const int64_t o = tile_off[blockIdx.x] + r;
-  out.event[o] = ev;
-  if (out.adc) out.adc[o] = a;
-  if (out_clean) out_clean[o] = __fsub_rn(a, adc_lowest);
-  if (out_q) out_q[o] = adc_to_charge(p, a);
-  if (out.pixel_x) out.pixel_x[o] = in.pixel_x[i];
-  if (out.pixel_y) out.pixel_y[o] = in.pixel_y[i];
-  if (out.pixel_z) out.pixel_z[o] = in.pixel_z[i];
-  if (out.ticks) out.ticks[o] = in.ticks[i];
-  if (out.hit_prob) out.hit_prob[o] = in.hit_prob[i];
-  if (out.pixels) out.pixels[o] = in.pixels[i];
-}
-
-// Run starts of the compacted event column: row o starts a run when it is
-// the first kept row or its event differs from the row before it.
-__device__ __forceinline__ bool run_head(const int32_t *__restrict__ ev, int64_t o, int64_t n_kept) {
-  return o < n_kept && (o == 0 || ev[o] != ev[o - 1]);
-}
-
-__global__ void __launch_bounds__(kRecTile) k_run_count(const int32_t *__restrict__ ev,
-                                                        const int64_t *__restrict__ counts,
-                                                        int64_t *__restrict__ tile_n) {
-  const int64_t n_kept = counts[0];
-  const int64_t o = (int64_t)blockIdx.x * kRecTile + threadIdx.x;
-  const int64_t s = tile_count(run_head(ev, o, n_kept));
-  if (threadIdx.x == 0) tile_n[blockIdx.x] = s;
-}
-
-__global__ void __launch_bounds__(kRecTile) k_run_write(const int32_t *__restrict__ ev,
-                                                        const int64_t *__restrict__ counts,
-                                                        const int64_t *__restrict__ tile_off,
-                                                        int32_t *__restrict__ run_event,
-                                                        int64_t *__restrict__ run_start) {
-  const int64_t n_kept = counts[0];
-  const int64_t o = (int64_t)blockIdx.x * kRecTile + threadIdx.x;
-  const bool head = run_head(ev, o, n_kept);
-  const int64_t r = tile_rank(head);
-  if (!head) return;
-  const int64_t k = tile_off[blockIdx.x] + r;
-  if (run_event) run_event[k] = ev[o];
-  run_start[k] = o;
+  unsigned bal[kRecSub];
+  bool has_prev[kRecSub];
+  int prev_ev[kRecSub];
+#pragma unroll
+  for (int s = 0; s < kRecSub; ++s) {
+    const Part q = warp_part(rec_keep(a[s], ev[s], adc_lowest), ev[s], bal[s], has_prev[s], prev_ev[s]);
+    if (lane == 0) parts[s * kRecWarps + wid] = q;
+  }
+  const TileOff to = offs[blockIdx.x];
+  __syncthreads();
+  if (wid == 0) {
+    const Part q = parts[lane];
+    int prior_last;
+    const bool has_prior = prior_part(q, prior_last);
+    const bool pp_has = has_prior || to.has_prev;
+    const int pp_ev = has_prior ? prior_last : to.prev_ev;
+    const int heads = q.heads + (q.kept > 0 && (!pp_has || q.first_ev != pp_ev) ? 1 : 0);
+    part_row[lane] = warp_incl_sum(q.kept) - q.kept;
+    part_run[lane] = warp_incl_sum(heads) - heads;
+    part_prev_has[lane] = pp_has;
+    part_prev_ev[lane] = pp_ev;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < kRecSub; ++s) {
+    const int pi = s * kRecWarps + wid;
+    const bool keep = (bal[s] >> lane) & 1u;
+    const bool head = keep && (has_prev[s] ? ev[s] != prev_ev[s]
+                                           : (part_prev_has[pi] ? ev[s] != part_prev_ev[pi] : true));
+    const unsigned hb = __ballot_sync(kFull, head);
+    if (!keep) continue;
+    const int64_t o = to.row + part_row[pi] + __popc(bal[s] & lanes_below());
+    out.event[o] = ev[s];
+    if (out.adc) out.adc[o] = a[s];
+    if (out_clean) out_clean[o] = __fsub_rn(a[s], adc_lowest);
+    if (out_q) out_q[o] = adc_to_charge(p, a[s]);
+    if (out.pixel_x) out.pixel_x[o] = x[s];
+    if (out.pixel_y) out.pixel_y[o] = y[s];
+    if (out.pixel_z) out.pixel_z[o] = z[s];
+    if (out.ticks) out.ticks[o] = tk[s];
+    if (out.hit_prob) out.hit_prob[o] = hp[s];
+    if (out.pixels) out.pixels[o] = px[s];
+    if (head && run_start) {
+      const int64_t k = to.run + part_run[pi] + __popc(hb & lanes_below());
+      run_start[k] = o;
+      if (run_event) run_event[k] = ev[s];
+    }
+  }
 }
 
 }  // namespace
 
 size_t records_workspace_bytes(int64_t n) {
   const int64_t tiles = (n + kRecTile - 1) / kRecTile;
-  return 2 * align256((size_t)(tiles + 1) * sizeof(int64_t));
+  return align256((size_t)tiles * sizeof(TileSum)) + align256((size_t)tiles * sizeof(TileOff));
 }
 
 int run_records(const LsimParams &p, float adc_lowest, const LsimHitColumns &in, int64_t n, const LsimHitColumns &out,
@@ -167,18 +305,12 @@ int run_records(const LsimParams &p, float adc_lowest, const LsimHitColumns &in,
     return LSIM_OK;
   }
   const int64_t tiles = (n + kRecTile - 1) / kRecTile;
-  int64_t *tile_rows = (int64_t *)ws;
-  int64_t *tile_runs = (int64_t *)((char *)ws + align256((size_t)(tiles + 1) * sizeof(int64_t)));
-  k_rec_count<<<(unsigned)tiles, kRecTile, 0, st>>>(in.adc, in.event, n, adc_lowest, tile_rows);
-  k_rec_scan<<<1, kRecTile, 0, st>>>(tile_rows, tiles, counts, nullptr, nullptr);
-  k_rec_write<<<(unsigned)tiles, kRecTile, 0, st>>>(p, in, n, adc_lowest, tile_rows, out, out_clean, out_q);
-  if (run_start) {
-    k_run_count<<<(unsigned)tiles, kRecTile, 0, st>>>(out.event, counts, tile_runs);
-    k_rec_scan<<<1, kRecTile, 0, st>>>(tile_runs, tiles, counts + 1, run_start, counts);
-    k_run_write<<<(unsigned)tiles, kRecTile, 0, st>>>(out.event, counts, tile_runs, run_event, run_start);
-  } else if (cudaMemsetAsync(counts + 1, 0, sizeof(int64_t), st) != cudaSuccess) {
-    return LSIM_ERR_CUDA;
-  }
+  TileSum *sums = (TileSum *)ws;
+  TileOff *offs = (TileOff *)((char *)ws + align256((size_t)tiles * sizeof(TileSum)));
+  k_rec_tiles<<<(unsigned)tiles, kRecThreads, 0, st>>>(in.adc, in.event, n, adc_lowest, sums);
+  k_rec_scan<<<1, kRecScanThreads, 0, st>>>(sums, tiles, offs, counts, run_start);
+  k_rec_write<<<(unsigned)tiles, kRecThreads, 0, st>>>(p, in, n, adc_lowest, offs, out, out_clean, out_q, run_event,
+                                                       run_start);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 
