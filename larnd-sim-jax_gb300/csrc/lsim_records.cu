@@ -142,32 +142,23 @@ __global__ void __launch_bounds__(kRecThreads) k_rec_tiles(const float *__restri
   if (lane == 0) sums[blockIdx.x] = TileSum{kept, heads, first, last};
 }
 
-// Inclusive block scan (sum, or max with identity `ident`) of one int64 per
-// thread; *total gets the block's sum / max.  The caller synchronises before
-// warp_tot or *total are written again.
-template <bool kMax>
-__device__ __forceinline__ int64_t block_incl_scan(int64_t v, int64_t ident, int64_t *warp_tot, int64_t *total) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  int64_t x = v;
+// Inclusive warp scans (max, sum) of one int64 per lane.
+__device__ __forceinline__ int64_t warp_incl_max(int64_t v) {
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const int64_t y = __shfl_up_sync(kFull, x, o);
-    if (lane >= o) x = kMax ? (y > x ? y : x) : x + y;
+    const int64_t y = __shfl_up_sync(kFull, v, o);
+    if ((int)(threadIdx.x & 31) >= o && y > v) v = y;
   }
-  if (lane == 31) warp_tot[wid] = x;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int64_t run = ident;
-    for (int i = 0; i < nw; ++i) {
-      const int64_t t = warp_tot[i];
-      warp_tot[i] = run;
-      run = kMax ? (t > run ? t : run) : run + t;
-    }
-    *total = run;
+  return v;
+}
+
+__device__ __forceinline__ int64_t warp_incl_sum64(int64_t v) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(kFull, v, o);
+    if ((int)(threadIdx.x & 31) >= o) v += y;
   }
-  __syncthreads();
-  const int64_t c = warp_tot[wid];
-  return kMax ? (c > x ? c : x) : x + c;
+  return v;
 }
 
 // The last kept event before each tile is found by a max-scan of
@@ -176,41 +167,83 @@ __device__ __forceinline__ int64_t pack_last(int64_t tile, int32_t ev) {
   return (int64_t)((uint64_t)tile << 32 | (uint32_t)ev);
 }
 
+// One CTA over all tiles, 1024 tiles per round: a max-scan for the last
+// kept event before each tile, then sum-scans of its kept rows and runs.
+// Every scan is warp shuffles plus one warp scanning the 32 warp totals;
+// four barriers per round, the next round's summaries loaded ahead.
 __global__ void __launch_bounds__(kRecScanThreads) k_rec_scan(const TileSum *__restrict__ sums, int64_t n_tiles,
-                                                           TileOff *__restrict__ offs, int64_t *__restrict__ counts,
-                                                           int64_t *__restrict__ run_start) {
-  __shared__ int64_t wt_last[32], wt_rows[32], wt_runs[32];
-  __shared__ int64_t tot_last, tot_rows, tot_runs;
-  __shared__ int64_t incl_last[kRecScanThreads];
+                                                              TileOff *__restrict__ offs,
+                                                              int64_t *__restrict__ counts,
+                                                              int64_t *__restrict__ run_start) {
+  constexpr int kW = kRecScanThreads / 32;
+  static_assert(kW == 32, "one lane of warp 0 per warp");
+  __shared__ int64_t w_last[kW], w_rows[kW], w_runs[kW];
+  __shared__ int64_t carry_sh[3];  // rows, runs and last key before the round
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t kNone = INT64_MIN;
-  int64_t carry_rows = 0, carry_runs = 0, carry_last = kNone;
+  if (threadIdx.x == 0) {
+    carry_sh[0] = 0;
+    carry_sh[1] = 0;
+    carry_sh[2] = kNone;
+  }
   TileSum next = threadIdx.x < n_tiles ? sums[threadIdx.x] : TileSum{0, 0, 0, 0};
+  __syncthreads();
   for (int64_t base = 0; base < n_tiles; base += kRecScanThreads) {
     const int64_t t = base + threadIdx.x;
     const TileSum ts = next;
     const int64_t tn = t + kRecScanThreads;
     next = tn < n_tiles ? sums[tn] : TileSum{0, 0, 0, 0};
+    const int64_t c_rows = carry_sh[0], c_runs = carry_sh[1], c_last = carry_sh[2];
+    // last kept event before the tile
     const int64_t key = ts.kept > 0 ? pack_last(t, ts.last_ev) : kNone;
-    int64_t il = block_incl_scan<true>(key, kNone, wt_last, &tot_last);
-    il = il > carry_last ? il : carry_last;
-    incl_last[threadIdx.x] = il;
+    const int64_t wl = warp_incl_max(key);
+    if (lane == 31) w_last[wid] = wl;
     __syncthreads();
-    const int64_t prev = threadIdx.x > 0 ? incl_last[threadIdx.x - 1] : carry_last;
+    if (wid == 0) {
+      const int64_t v = warp_incl_max(w_last[lane]);
+      const int64_t before = __shfl_up_sync(kFull, v, 1);
+      const int64_t ex = lane == 0 ? c_last : (before > c_last ? before : c_last);
+      w_last[lane] = ex;  // max over the warps before this one and the earlier rounds
+    }
+    __syncthreads();
+    const int64_t wprev = w_last[wid];
+    const int64_t lprev = __shfl_up_sync(kFull, wl, 1);
+    const int64_t prev = lane == 0 ? wprev : (lprev > wprev ? lprev : wprev);
     const bool has_prev = prev != kNone;
     const int32_t prev_ev = has_prev ? (int32_t)(uint32_t)(uint64_t)prev : 0;
     const int64_t runs = ts.kept > 0 ? ts.heads + ((!has_prev || ts.first_ev != prev_ev) ? 1 : 0) : 0;
-    const int64_t ir = block_incl_scan<false>(ts.kept, 0, wt_rows, &tot_rows);
-    const int64_t iu = block_incl_scan<false>(runs, 0, wt_runs, &tot_runs);
-    if (t < n_tiles) offs[t] = TileOff{carry_rows + ir - ts.kept, carry_runs + iu - runs, prev_ev, has_prev ? 1 : 0};
-    carry_rows += tot_rows;
-    carry_runs += tot_runs;
-    carry_last = tot_last > carry_last ? tot_last : carry_last;
+    // row and run offsets
+    const int64_t ir = warp_incl_sum64(ts.kept);
+    const int64_t iu = warp_incl_sum64(runs);
+    if (lane == 31) {
+      w_rows[wid] = ir;
+      w_runs[wid] = iu;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      const int64_t vr = warp_incl_sum64(w_rows[lane]);
+      const int64_t vu = warp_incl_sum64(w_runs[lane]);
+      const int64_t tr = __shfl_sync(kFull, vr, 31), tu = __shfl_sync(kFull, vu, 31);
+      w_rows[lane] = c_rows + vr - w_rows[lane];
+      w_runs[lane] = c_runs + vu - w_runs[lane];
+      if (lane == 0) {
+        carry_sh[0] = c_rows + tr;
+        carry_sh[1] = c_runs + tu;
+      }
+    }
+    __syncthreads();
+    if (t < n_tiles) offs[t] = TileOff{w_rows[wid] + ir - ts.kept, w_runs[wid] + iu - runs, prev_ev, has_prev ? 1 : 0};
+    // the round's last key: the last thread's inclusive max
+    if (threadIdx.x == kRecScanThreads - 1) {
+      const int64_t incl = wl > wprev ? wl : wprev;
+      carry_sh[2] = incl > c_last ? incl : c_last;
+    }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    counts[0] = carry_rows;
-    counts[1] = carry_runs;
-    if (run_start) run_start[carry_runs] = carry_rows;
+    counts[0] = carry_sh[0];
+    counts[1] = carry_sh[1];
+    if (run_start) run_start[carry_sh[1]] = carry_sh[0];
   }
 }
 
