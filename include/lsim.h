@@ -341,6 +341,31 @@ int lsim_hit_records(const LsimParams *p, float adc_lowest, const LsimHitColumns
 
 /* ---------------------------------------------------------------- input side */
 
+/* Gather n_rows rows (row indices `rows`, device int64) of a (n_table,
+ * n_fields <= 96) float32 track table resident in device memory into out
+ * (n_rows, n_fields); with event_values non-NULL, column event_col of row r
+ * becomes event_values[r] (the batch-local event id).  Replaces the row
+ * selection and remap_event_ids_to_local of TracksDataset.__getitem__,
+ * optimize/dataio.py:378-395 and :47-61 (the host computes the local ids
+ * once per batch, as the reference does).  A row index outside the table
+ * sets *status_dev (int32, device memory, zeroed by the caller) to
+ * LSIM_ERR_INVALID and that row is not written. */
+int lsim_gather_tracks(const float *table, int64_t n_table, int32_t n_fields, const int64_t *rows, int64_t n_rows,
+                       int32_t event_col, const float *event_values, float *out, int32_t *status_dev, void *stream);
+
+/* Pad a batch of n_rows rows in place to target_rows rows (the buffer holds
+ * max(n_rows, target_rows) rows) and invalidate rows, as TracksDataset.pad_batch
+ * / _invalidate_rows do (optimize/dataio.py:347-373): an invalidated row gets
+ * eventID -1 in event_col, 0 in the columns whose col_roles entry is 1
+ * (n_electrons, dE, dEdx, dx, long_diff, tran_diff) and -1 in those with 2
+ * (trackID, pixel_plane); other columns keep their values, and are 0 in the
+ * padding rows [n_rows, target_rows).  With n_local_events >= 0 the rows
+ * [0, n_rows) whose eventID is >= 0 and whose integer part (truncated, like
+ * numpy's astype(int64)) is not in [0, n_local_events) are invalidated too.
+ * col_roles is a HOST array of n_fields entries in {0, 1, 2}, or NULL. */
+int lsim_pad_tracks(float *batch, int64_t n_rows, int64_t target_rows, int32_t n_fields, int32_t event_col,
+                    const int8_t *col_roles, int64_t n_local_events, void *stream);
+
 /* Workspace bytes of lsim_chop_tracks for n_rows input tracks. */
 size_t lsim_chop_workspace_bytes(int64_t n_rows);
 

@@ -473,6 +473,34 @@ int lsim_chamfer_3d(const float *x, const float *y, const float *z, const int32_
               "lsim_chamfer_3d");
 }
 
+int lsim_gather_tracks(const float *table, int64_t n_table, int32_t n_fields, const int64_t *rows, int64_t n_rows,
+                       int32_t event_col, const float *event_values, float *out, int32_t *status_dev, void *stream) {
+  g_err.clear();
+  if (n_table < 0 || n_rows < 0 || n_fields <= 0 || n_fields > 96 || !status_dev ||
+      (n_rows > 0 && (!table || !rows || !out)))
+    return fail(LSIM_ERR_INVALID, "lsim_gather_tracks: bad arguments");
+  if (event_values && (event_col < 0 || event_col >= n_fields))
+    return fail(LSIM_ERR_INVALID, "lsim_gather_tracks: event column %d outside [0, %d)", event_col, n_fields);
+  return wrap(run_gather_tracks(table, n_table, n_fields, rows, n_rows, event_col, event_values, out, status_dev,
+                                (cudaStream_t)stream),
+              "lsim_gather_tracks");
+}
+
+int lsim_pad_tracks(float *batch, int64_t n_rows, int64_t target_rows, int32_t n_fields, int32_t event_col,
+                    const int8_t *col_roles, int64_t n_local_events, void *stream) {
+  g_err.clear();
+  if (n_rows < 0 || n_fields <= 0 || n_fields > 96 || event_col < 0 || event_col >= n_fields ||
+      (target_rows > 0 && !batch))
+    return fail(LSIM_ERR_INVALID, "lsim_pad_tracks: bad arguments");
+  if (col_roles)
+    for (int c = 0; c < n_fields; ++c)
+      if (col_roles[c] < 0 || col_roles[c] > 2) return fail(LSIM_ERR_INVALID, "lsim_pad_tracks: column role %d", col_roles[c]);
+  const int64_t rows = target_rows > n_rows ? target_rows : n_rows;
+  return wrap(run_pad_tracks(batch, n_rows, rows, n_fields, event_col, col_roles, n_local_events,
+                             (cudaStream_t)stream),
+              "lsim_pad_tracks");
+}
+
 size_t lsim_chop_workspace_bytes(int64_t n_rows) { return n_rows < 0 ? 0 : chop_workspace_bytes(n_rows); }
 
 int lsim_chop_tracks(const LsimFieldMap *f, const float *tracks, int64_t n_rows, double precision, float *out,

@@ -98,6 +98,12 @@ int run_records(const LsimParams &p, float adc_lowest, const LsimHitColumns &in,
                 float *out_clean, float *out_q, int32_t *run_event, int64_t *run_start, int64_t *counts, void *ws,
                 cudaStream_t st);
 
+// lsim_tracks.cu
+int run_gather_tracks(const float *table, int64_t n_table, int32_t n_fields, const int64_t *rows, int64_t n_rows,
+                      int32_t event_col, const float *event_values, float *out, int32_t *status, cudaStream_t st);
+int run_pad_tracks(float *batch, int64_t n_rows, int64_t target_rows, int32_t n_fields, int32_t event_col,
+                   const int8_t *col_roles, int64_t n_local_events, cudaStream_t st);
+
 // lsim_chop.cu
 size_t chop_workspace_bytes(int64_t n_rows);
 int run_chop(const LsimFieldMap &f, const float *tracks, int64_t n_rows, double precision, float *out,

@@ -120,6 +120,8 @@ _SIGNATURES = {
     "lsim_hit_records_workspace_bytes": (_sz, [_i64]),
     "lsim_hit_records": (C.c_int, [_PP, C.c_float, C.POINTER(LsimHitColumns), _i64, C.POINTER(LsimHitColumns), _vp,
                                    _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "lsim_gather_tracks": (C.c_int, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _vp, _vp, _vp]),
+    "lsim_pad_tracks": (C.c_int, [_vp, _i64, _i64, _i32, _i32, _vp, _i64, _vp]),
     "lsim_chop_workspace_bytes": (_sz, [_i64]),
     "lsim_chop_tracks": (C.c_int, [_PF, _vp, _i64, C.c_double, _vp, _i64, _vp, _vp, _sz, _vp]),
     "lsim_param_stage1": (C.c_int, [_PP, _PF, _vp, _i64, _i32, _vp, _vp, _sz, _vp, _vp]),

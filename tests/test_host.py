@@ -254,3 +254,14 @@ def test_hit_records_rejects_bad_arguments_without_gpu(lib):
     assert lib.lsim_hit_records(p, 80.0, cols, 10, cols, None, None, None, None, counts, V(256), 8,
                                 None) == _abi.LSIM_ERR_CAPACITY
     assert b"workspace" in lib.lsim_last_error()
+
+
+def test_track_batch_entry_points_reject_bad_arguments_without_gpu(lib):
+    V = ctypes.c_void_p
+    assert lib.lsim_gather_tracks(V(16), 10, 0, V(16), 4, 0, None, V(16), V(16), None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_gather_tracks(V(16), 10, 120, V(16), 4, 0, None, V(16), V(16), None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_gather_tracks(V(16), 10, 26, V(16), 4, 30, V(16), V(16), V(16), None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_gather_tracks(V(16), 10, 26, V(16), 4, 0, None, V(16), None, None) == _abi.LSIM_ERR_INVALID
+    roles = (ctypes.c_int8 * 3)(0, 1, 5)
+    assert lib.lsim_pad_tracks(V(16), 4, 8, 3, 0, roles, -1, None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_pad_tracks(V(16), 4, 8, 3, 3, None, -1, None) == _abi.LSIM_ERR_INVALID

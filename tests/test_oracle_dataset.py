@@ -1,0 +1,61 @@
+"""The batch layout of TracksDataset (optimize/dataio.py:108-424) against
+the reference's own batches (tests/golden/dataset_ref.npz, made by
+tests/golden/make_dataset_golden.py): which rows and events form each
+batch, the padded step count and the total track length.  Host logic only;
+the rows themselves are assembled on the GPU (tests/test_gpu_dataset.py)."""
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from larndsim_gb300 import dataio
+
+GOLD = Path(__file__).resolve().parent / "golden" / "dataset_ref.npz"
+CASES = {
+    "batched": dict(nevents=6, max_batch_len=25.0, chopped=True, pad=True, electron_sampling_resolution=0.1),
+    "one_traj_per_batch": dict(nevents=None, max_batch_len=None, chopped=False, pad=False, max_nbatch=None),
+    "random_live": dict(nevents=5, random_nevents=True, data_seed=7, live_selection=True, track_len_sel=2.0,
+                        max_abs_costheta_sel=0.95, min_abs_segz_sel=20.0, track_z_bound=24.0, max_batch_len=30.0,
+                        chopped=True, pad=True, electron_sampling_resolution=0.2, max_nbatch=2),
+    "no_swap_unpadded": dict(nevents=4, swap_xz=False, max_batch_len=18.0, chopped=True, pad=False,
+                             electron_sampling_resolution=0.25),
+}
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+def make(gold, name):
+    kw = dict(CASES[name])
+    nevents = kw.pop("nevents")
+    return dataio.TracksDataset(gold["segments"], nevents, **kw)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_batch_layout_matches_reference(gold, name):
+    ds = make(gold, name)
+    assert len(ds) == int(gold[f"{name}/n_batches"])
+    assert ds.get_track_fields() == tuple(gold[f"{name}/fields"].tolist())
+    assert ds.max_batch_nsteps == int(gold[f"{name}/max_batch_nsteps"])
+    assert float(ds.tot_data_length) == float(gold[f"{name}/tot_data_length"])
+    for i in range(len(ds)):
+        np.testing.assert_array_equal(ds.get_batch_global_event_ids(i), gold[f"{name}/events_{i}"])
+        np.testing.assert_array_equal(ds.get_batch_row_indices(i), gold[f"{name}/rows_{i}"])
+
+
+def test_remap_event_ids_to_local():
+    arr = np.zeros((4, 2), np.float32)
+    out = dataio.remap_event_ids_to_local(arr, [105, 103, 105, 110], [103, 105, 110], ("x", "eventID"))
+    np.testing.assert_array_equal(out[:, 1], [1, 0, 1, 2])
+    with pytest.raises(ValueError, match="Missing global eventID values: \\[104\\]"):
+        dataio.remap_event_ids_to_local(arr, [104], [103, 105], ("x", "eventID"))
+
+
+def test_errors_like_the_reference(gold):
+    with pytest.raises(ValueError, match="longer than the batch size"):
+        dataio.TracksDataset(gold["segments"], None, max_batch_len=0.01)
+    with pytest.raises(ImportError, match="h5py"):
+        dataio.read_segments("segments.h5")
