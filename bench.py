@@ -893,6 +893,10 @@ def run_chop_reference(args):
 # ---------------------------------------------------------------- output side
 
 RECORDS_HITS, RECORDS_EVENTS, RECORDS_CPU_HITS = 32_000_000, 1000, 4_000_000
+# DRAM bytes per input hit of one lsim_hit_records call (three kernels), from
+# the ncu launch list summarised in profiles/hit_records_8M_hits.md (575.3 MB
+# over 8M hits; traffic scales with the hits)
+RECORDS_DRAM_BYTES_PER_HIT = 575_320_064 / 8_000_000
 
 
 def _records_workload(n, seed=0):
@@ -995,7 +999,8 @@ def run_records(args):
            "roofline": {"bound": "hbm", "kernel": "lsim_hit_records (3 launches timed together)",
                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "algorithmic_bytes": algo,
-                        "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None},
+                        "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                        "traffic": int(RECORDS_DRAM_BYTES_PER_HIT * n)},
            "gpu_launches": 3 * args.steps, "clocks": clk}
     if not args.no_cpu_baseline:
         from oracle import reference_np as R
