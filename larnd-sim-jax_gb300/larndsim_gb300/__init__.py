@@ -13,7 +13,7 @@ from .sim import (average_hit_values, get_adc_values, get_adc_values_average_noi
                   simulate_probabilistic, simulate_stochastic, simulate_wfs)
 from .fee import digitize  # noqa: F401
 from .losses import adc2charge, chamfer_3d, mse_adc, nll_loss  # noqa: F401
-from .dataio import DataLoader, TracksDataset, chop_tracks  # noqa: F401
+from .dataio import DataLoader, TgtTracksDataset, TracksDataset, chop_tracks  # noqa: F401
 from .output import hit_records, write_hits_groups_npz, write_hits_h5, write_hits_npz  # noqa: F401
 
 __all__ = [
@@ -22,5 +22,5 @@ __all__ = [
     "simulate_parametrized", "simulate_stochastic", "simulate_wfs", "digitize", "adc2charge", "chop_tracks",
     "simulate_probabilistic", "get_adc_values_average_noise_vmap", "get_average_hit_values", "average_hit_values",
     "mse_adc", "nll_loss", "chamfer_3d", "hit_records", "write_hits_npz", "write_hits_h5", "write_hits_groups_npz",
-    "TracksDataset", "DataLoader",
+    "TracksDataset", "TgtTracksDataset", "DataLoader",
 ]

@@ -105,7 +105,76 @@ def _swap_xz(tracks):
         tracks[b] = xa
 
 
-class TracksDataset:
+class _DeviceBatches:
+    """Device assembly shared by the two datasets: the table in HBM as
+    float32, the batch rows gathered with their local event ids, chopped and
+    padded with the reference's invalidated rows."""
+
+    def _init_device(self, fields):
+        self._evt_col = fields.index("eventID")
+        self._roles = np.zeros(len(fields), dtype=np.int8)
+        for name in _ZERO_PAD_FIELDS:
+            if name in fields:
+                self._roles[fields.index(name)] = 1
+        for name in _NEG_ONE_PAD_FIELDS:
+            if name in fields:
+                self._roles[fields.index(name)] = 2
+        self._table = None
+        self._batch_dev = {}
+
+    def _device_table(self):
+        if self._table is None:
+            self._table = torch.from_numpy(np_from_structured(self.tracks_struct)).to(sim._device())
+        return self._table
+
+    def _batch_index(self, idx):
+        if idx not in self._batch_dev:
+            rows = np.asarray(self.batch_row_indices[idx], dtype=np.int64)
+            local = _local_event_ids(self.tracks_struct[rows]["eventID"].astype(np.int64),
+                                     self.batch_event_global_ids[idx])
+            dev = sim._device()
+            self._batch_dev[idx] = (torch.from_numpy(rows).to(dev),
+                                    torch.from_numpy(local.astype(np.float32)).to(dev))
+        return self._batch_dev[idx]
+
+    def _assemble(self, idx, fields):
+        lib = _abi.load()
+        table = self._device_table()
+        rows, local = self._batch_index(idx)
+        n, nf = rows.numel(), len(fields)
+        out = torch.empty((n, nf), dtype=torch.float32, device=table.device)
+        status = torch.zeros(1, dtype=torch.int32, device=table.device)
+        _abi.check(lib, lib.lsim_gather_tracks(sim._ptr(table), table.shape[0], nf, sim._ptr(rows), n,
+                                               self._evt_col, sim._ptr(local), sim._ptr(out), sim._ptr(status),
+                                               sim._stream()))
+        if self.chopped and n > 0:
+            out = chop_tracks(out, fields, precision=self.electron_sampling_resolution)
+        if int(status.item()) != 0:
+            raise ValueError("batch row index outside the track table")
+        if self.pad and self.max_batch_nsteps > 0 and out.shape[0] < self.max_batch_nsteps:
+            out = self.pad_batch(out, self.max_batch_nsteps, idx)
+        return out
+
+    def pad_batch(self, batch_arr, target_len, idx=None):
+        """Pad to ``target_len`` rows with invalidated rows and invalidate rows
+        whose event is not a local event of batch ``idx`` (dataio.py:357-373,
+        :525-542).  Returns a new float32 CUDA tensor."""
+        lib = _abi.load()
+        b = torch.as_tensor(batch_arr).to(device=sim._device(), dtype=torch.float32)
+        cur = b.shape[0]
+        out = torch.empty((max(cur, int(target_len)), b.shape[1]), dtype=torch.float32, device=b.device)
+        out[:cur].copy_(b)
+        n_local = len(self.batch_event_global_ids[idx]) if idx is not None else -1
+        roles = self._roles.ctypes.data_as(_abi.C.c_void_p)
+        _abi.check(lib, lib.lsim_pad_tracks(sim._ptr(out), cur, int(target_len), b.shape[1], self._evt_col, roles,
+                                            n_local, sim._stream()))
+        return out
+
+    def get_batch_global_event_ids(self, idx=None):
+        return self.batch_event_global_ids if idx is None else self.batch_event_global_ids[idx]
+
+
+class TracksDataset(_DeviceBatches):
     """Batches of whole events from a segments table
     (TracksDataset, optimize/dataio.py:108-424).
 
@@ -160,16 +229,7 @@ class TracksDataset:
         self.chopped, self.pad, self.print_input = chopped, pad, print_input
         self.electron_sampling_resolution = electron_sampling_resolution
         self.tot_data_length = tot
-        self._evt_col = self.track_fields.index("eventID")
-        self._roles = np.zeros(len(self.track_fields), dtype=np.int8)
-        for name in _ZERO_PAD_FIELDS:
-            if name in self.track_fields:
-                self._roles[self.track_fields.index(name)] = 1
-        for name in _NEG_ONE_PAD_FIELDS:
-            if name in self.track_fields:
-                self._roles[self.track_fields.index(name)] = 2
-        self._table = None
-        self._batch_dev = {}
+        self._init_device(self.track_fields)
 
     # -- layout (host)
 
@@ -251,23 +311,6 @@ class TracksDataset:
         batches = [[t for k in range(splits[i], splits[i + 1]) for t in groups[k]] for i in range(len(splits) - 1)]
         return batches, cum[splits[-1] - 1]
 
-    # -- device assembly
-
-    def _device_table(self):
-        if self._table is None:
-            self._table = torch.from_numpy(np_from_structured(self.tracks_struct)).to(sim._device())
-        return self._table
-
-    def _batch_index(self, idx):
-        if idx not in self._batch_dev:
-            rows = self.batch_row_indices[idx]
-            local = _local_event_ids(self.tracks_struct[rows]["eventID"].astype(np.int64),
-                                     self.batch_event_global_ids[idx])
-            dev = sim._device()
-            self._batch_dev[idx] = (torch.from_numpy(rows).to(dev),
-                                    torch.from_numpy(local.astype(np.float32)).to(dev))
-        return self._batch_dev[idx]
-
     def __len__(self):
         return len(self.batch_traj_indices)
 
@@ -275,49 +318,103 @@ class TracksDataset:
         """Batch ``idx`` as an (n, F) float32 CUDA tensor (dataio.py:378-406)."""
         if idx < 0 or idx >= len(self):
             raise IndexError("Batch index out of range")
-        lib = _abi.load()
-        table = self._device_table()
-        rows, local = self._batch_index(idx)
-        n, nf = rows.numel(), len(self.track_fields)
-        out = torch.empty((n, nf), dtype=torch.float32, device=table.device)
-        status = torch.zeros(1, dtype=torch.int32, device=table.device)
-        _abi.check(lib, lib.lsim_gather_tracks(sim._ptr(table), table.shape[0], nf, sim._ptr(rows), n,
-                                               self._evt_col, sim._ptr(local), sim._ptr(out), sim._ptr(status),
-                                               sim._stream()))
-        if self.chopped:
-            out = chop_tracks(out, self.track_fields, precision=self.electron_sampling_resolution)
-        if int(status.item()) != 0:
-            raise ValueError("batch row index outside the track table")
-        if self.pad and self.max_batch_nsteps > 0 and out.shape[0] < self.max_batch_nsteps:
-            out = self.pad_batch(out, self.max_batch_nsteps, idx)
-        return out
-
-    def pad_batch(self, batch_arr, target_len, idx=None):
-        """Pad to ``target_len`` rows with invalidated rows and invalidate rows
-        whose event is not a local event of batch ``idx`` (dataio.py:357-373).
-        Returns a new float32 CUDA tensor."""
-        lib = _abi.load()
-        b = torch.as_tensor(batch_arr).to(device=sim._device(), dtype=torch.float32)
-        cur = b.shape[0]
-        out = torch.empty((max(cur, int(target_len)), b.shape[1]), dtype=torch.float32, device=b.device)
-        out[:cur].copy_(b)
-        n_local = len(self.batch_event_global_ids[idx]) if idx is not None else -1
-        roles = self._roles.ctypes.data_as(_abi.C.c_void_p)
-        _abi.check(lib, lib.lsim_pad_tracks(sim._ptr(out), cur, int(target_len), b.shape[1], self._evt_col, roles,
-                                            n_local, sim._stream()))
-        return out
+        return self._assemble(idx, self.track_fields)
 
     def get_track_fields(self):
         return self.track_fields
-
-    def get_batch_global_event_ids(self, idx=None):
-        return self.batch_event_global_ids if idx is None else self.batch_event_global_ids[idx]
 
     def get_batch_row_keys(self):
         return self.batch_row_keys
 
     def get_batch_row_indices(self, idx=None):
         return self.batch_row_indices if idx is None else self.batch_row_indices[idx]
+
+
+def _pack_keys(event_ids, track_ids):
+    """(eventID, trackID) pairs as uint64 keys, event in the high 32 bits."""
+    e = np.asarray(event_ids, dtype=np.int64).astype(np.uint64)
+    t = np.asarray(track_ids, dtype=np.int64).astype(np.uint64)
+    return (e << np.uint64(32)) | (t & np.uint64(0xFFFFFFFF))
+
+
+class TgtTracksDataset(_DeviceBatches):
+    """Target batches matched to a simulation dataset's batches
+    (TgtTracksDataset, optimize/dataio.py:426-640): batch i holds every
+    target row whose (eventID, trackID) key is one of the keys of the
+    simulation dataset's batch i, in table order, with the simulation
+    batch's local event ids; chopped and padded like TracksDataset, on the
+    GPU.  ``filename`` may be the structured target segments array."""
+
+    def __init__(self, filename, dataset_sim, swap_xz=True, chopped=True, pad=True, electron_sampling_resolution=0.1,
+                 print_input=False):
+        self.chopped, self.pad, self.print_input = chopped, pad, print_input
+        self.electron_sampling_resolution = electron_sampling_resolution
+        self.swap_xz = swap_xz
+        self.sim_track_fields = dataset_sim.get_track_fields()
+        tracks = read_segments(filename)
+        if "t0" not in tracks.dtype.names:
+            tracks = rfn.append_fields(tracks, "t0", np.zeros(tracks.shape[0]), usemask=False)
+        self.tgt_track_fields = tuple(_RENAME.get(f, f) for f in tracks.dtype.names)
+        tracks.dtype.names = self.tgt_track_fields
+        if swap_xz:
+            _swap_xz(tracks)
+        self.tracks_struct = tracks
+        keys = _pack_keys(tracks["eventID"], tracks["trackID"])
+        order = np.argsort(keys)
+        self._key_order = order
+        self._keys, self._key_starts = np.unique(keys[order], return_index=True)
+        self._key_ends = np.append(self._key_starts[1:], len(order))
+        self.batch_keys = dataset_sim.get_batch_row_keys()
+        self.batch_event_global_ids = dataset_sim.get_batch_global_event_ids()
+        self.batch_row_indices, self.batch_nsteps = [], []
+        self.tot_data_length = 0
+        for keys_b in self.batch_keys:
+            if keys_b.size == 0:
+                self.batch_row_indices.append(np.empty((0,), dtype=int))
+                self.batch_nsteps.append(0)
+                continue
+            rows = self._rows_for_key_ids(np.unique(_pack_keys(keys_b["eventID"], keys_b["trackID"])))
+            self.batch_row_indices.append(rows)
+            if rows.size == 0:
+                self.batch_nsteps.append(0)
+            else:
+                dx = tracks[rows]["dx"]
+                self.batch_nsteps.append(int(np.sum(np.maximum(np.ceil(dx / electron_sampling_resolution), 1)
+                                                    .astype(int))))
+                self.tot_data_length += np.sum(dx)
+        self.max_batch_nsteps = int(max(self.batch_nsteps)) if self.batch_nsteps else 0
+        self.n_batches = len(self.batch_keys)
+        self._init_device(self.tgt_track_fields)
+
+    def _rows_for_key_ids(self, key_ids):
+        """Sorted target rows of the given keys; every key must be present
+        (dataio.py:577-599)."""
+        left = np.searchsorted(self._keys, key_ids, side="left")
+        right = np.searchsorted(self._keys, key_ids, side="right")
+        missing = left == right
+        if missing.any():
+            miss = key_ids[missing][:16]
+            pairs = list(zip((miss >> np.uint64(32)).astype(np.int64).tolist(),
+                             (miss & np.uint64(0xFFFFFFFF)).astype(np.int64).tolist()))
+            raise ValueError(f"{int(missing.sum())} of {len(key_ids)} sim key(s) are absent from the target file. "
+                             f"Missing (eventID, trackID) sample: {pairs}")
+        chunks = [self._key_order[self._key_starts[u]:self._key_ends[u]] for lo, hi in zip(left, right)
+                  for u in range(lo, hi)]
+        return np.sort(np.concatenate(chunks)) if chunks else np.empty((0,), dtype=int)
+
+    def __len__(self):
+        return self.n_batches
+
+    def __getitem__(self, idx):
+        """Target batch ``idx`` as an (n, F) float32 CUDA tensor (dataio.py:604-626)."""
+        if idx < 0 or idx >= self.n_batches:
+            raise IndexError("TgtTracksDataset index out of range")
+        if self.batch_row_indices[idx].size == 0:
+            return torch.empty((0, len(self.tgt_track_fields)), dtype=torch.float32, device=sim._device())
+        return self._assemble(idx, self.tgt_track_fields)
+
+    def get_track_fields(self):
+        return self.tgt_track_fields
 
 
 class DataLoader:

@@ -6,8 +6,11 @@ array (the reference reads that dataset and nothing else), builds the
 dataset under several option sets and stores, per case, every batch
 ``ds[i]``, the per-batch global event ids and source rows, the padded
 step count, the total track length and one ``pad_batch`` call, in
-dataset_ref.npz.  The structured array itself is stored too, so the test
-feeds the same rows to the GB300 implementation.  Generated with NumPy 2.
+dataset_ref.npz; and the target batches of TgtTracksDataset (:426-640) for
+a second seeded table (other energy deposits, shuffled rows, one extra
+event) matched to two of those cases.  Both structured arrays are stored
+too, so the tests feed the same rows to the GB300 implementation.
+Generated with NumPy 2.
 
 Usage: python tests/golden/make_dataset_golden.py [/path/to/larnd-sim-jax]
 """
@@ -71,12 +74,24 @@ CASES = {
 }
 
 
-def load_reference(segments):
+def make_target(seg, seed=1):
+    """Target segments for TgtTracksDataset: the same trajectories with other
+    energy deposits, rows in another order, plus one extra event."""
+    rng = np.random.default_rng(seed)
+    tgt = seg.copy()
+    tgt["dE"] = (tgt["dE"] * rng.uniform(0.8, 1.2, tgt.shape[0])).astype(np.float32)
+    extra = seg[seg["event_id"] == seg["event_id"][0]].copy()
+    extra["event_id"] = 999
+    tgt = np.concatenate([tgt, extra])
+    return tgt[rng.permutation(tgt.shape[0])]
+
+
+def load_reference(segments, target=None):
     fake = types.ModuleType("h5py")
 
     class File:
         def __init__(self, name, mode="r"):
-            pass
+            self.table = target if str(name).startswith("target") else segments
 
         def __enter__(self):
             return self
@@ -86,7 +101,7 @@ def load_reference(segments):
 
         def __getitem__(self, key):
             assert key == "segments"
-            return segments.copy()
+            return self.table.copy()
 
     fake.File = File
     sys.modules["h5py"] = fake
@@ -96,10 +111,29 @@ def load_reference(segments):
     return mod
 
 
+TARGET_CASES = {
+    "tgt_batched": ("batched", dict(chopped=True, pad=True, electron_sampling_resolution=0.1)),
+    "tgt_unchopped": ("no_swap_unpadded", dict(swap_xz=False, chopped=False, pad=True)),
+}
+
+
 def main():
     seg = make_segments()
-    mod = load_reference(seg)
-    arrays = {"segments": seg}
+    tgt = make_target(seg)
+    mod = load_reference(seg, tgt)
+    arrays = {"segments": seg, "target_segments": tgt}
+    for name, (sim_case, kw) in TARGET_CASES.items():
+        skw = dict(CASES[sim_case])
+        nevents = skw.pop("nevents")
+        sim = mod.TracksDataset("segments.h5", nevents, **skw)
+        ds = mod.TgtTracksDataset("target.h5", sim, **kw)
+        arrays[f"{name}/n_batches"] = np.array(len(ds))
+        arrays[f"{name}/fields"] = np.array(ds.get_track_fields())
+        arrays[f"{name}/max_batch_nsteps"] = np.array(ds.max_batch_nsteps)
+        arrays[f"{name}/tot_data_length"] = np.array(ds.tot_data_length, dtype=np.float64)
+        for i in range(len(ds)):
+            arrays[f"{name}/batch_{i}"] = ds[i]
+            arrays[f"{name}/rows_{i}"] = np.asarray(ds.batch_row_indices[i])
     for name, kw in CASES.items():
         kw = dict(kw)
         nevents = kw.pop("nevents")

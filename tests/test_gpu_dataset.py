@@ -110,3 +110,14 @@ def test_data_loader_stacks_padded_batches(cuda, gold):
     stacks = list(dl)
     assert len(dl) == len(stacks) == 2 and stacks[0].shape == (3, ds.max_batch_nsteps, len(ds.get_track_fields()))
     np.testing.assert_array_equal(_bits(stacks[1][0].cpu().numpy()), _bits(ds[3].cpu().numpy()))
+
+
+@pytest.mark.parametrize("name", ["tgt_batched", "tgt_unchopped"])
+def test_target_batches_bitwise(cuda, gold, name):
+    """Target batches (rows found by key and sorted: the same on every
+    platform) against the reference's, bit for bit."""
+    from test_oracle_dataset import make_target
+    ds = make_target(gold, name)
+    for i in range(len(ds)):
+        got = ds[i].cpu().numpy()
+        np.testing.assert_array_equal(_bits(got), _bits(gold[f"{name}/batch_{i}"]), err_msg=f"batch {i}")

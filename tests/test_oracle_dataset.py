@@ -82,3 +82,35 @@ def test_errors_like_the_reference(gold):
         dataio.TracksDataset(gold["segments"], None, max_batch_len=0.01)
     with pytest.raises(ImportError, match="h5py"):
         dataio.read_segments("segments.h5")
+
+
+TARGET_CASES = {
+    "tgt_batched": ("batched", dict(chopped=True, pad=True, electron_sampling_resolution=0.1)),
+    "tgt_unchopped": ("no_swap_unpadded", dict(swap_xz=False, chopped=False, pad=True)),
+}
+
+
+def make_target(gold, name):
+    sim_case, kw = TARGET_CASES[name]
+    return dataio.TgtTracksDataset(gold["target_segments"], make(gold, sim_case), **kw)
+
+
+@pytest.mark.parametrize("name", list(TARGET_CASES))
+def test_target_layout_matches_reference(gold, name):
+    """Target rows are looked up by key and sorted, so this layout does not
+    depend on the platform's argsort."""
+    ds = make_target(gold, name)
+    assert len(ds) == int(gold[f"{name}/n_batches"])
+    assert ds.get_track_fields() == tuple(gold[f"{name}/fields"].tolist())
+    assert ds.max_batch_nsteps == int(gold[f"{name}/max_batch_nsteps"])
+    assert float(ds.tot_data_length) == float(gold[f"{name}/tot_data_length"])
+    for i in range(len(ds)):
+        np.testing.assert_array_equal(ds.batch_row_indices[i], gold[f"{name}/rows_{i}"])
+
+
+def test_target_missing_key_raises(gold):
+    seg = gold["target_segments"]
+    sim = make(gold, "batched")
+    gone = seg["event_id"] == sim.get_batch_global_event_ids(0)[0]
+    with pytest.raises(ValueError, match="absent from the target file"):
+        dataio.TgtTracksDataset(seg[~gone], sim)
