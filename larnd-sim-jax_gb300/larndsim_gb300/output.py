@@ -38,6 +38,8 @@ class HitRecords(dict):
     def by_event(self, global_event_ids=None):
         """One group per local event id >= 0, keyed by its global id, with the
         reference's dataset names (simulate.py:139-156).  Host arrays."""
+        if "run_start" not in self:
+            raise ValueError("these records were made with runs=False: no event runs to split by")
         starts = self["run_start"].cpu().numpy()
         events = self["run_event"].cpu().numpy()
         host = {k: self[k].cpu().numpy() for k in ("adc_clean", "adc", "Q", "pixels", "ticks", "pix_x", "pix_y",

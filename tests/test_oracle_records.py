@@ -115,3 +115,9 @@ def test_h5_writer_needs_h5py(params, tmp_path):
         pass
     with pytest.raises(ImportError, match="h5py"):
         output.write_hits_h5(tmp_path / "x.h5", [])
+
+
+def test_by_event_needs_runs(params):
+    rec = output.HitRecords({"adc": torch.zeros(0)})
+    with pytest.raises(ValueError, match="runs=False"):
+        rec.by_event()
