@@ -10,9 +10,9 @@
 //   k_rec_tiles  reads adc and event and summarises each tile: kept rows,
 //                run heads whose previous kept row is in the tile, first
 //                and last kept event;
-//   k_rec_scan   one CTA, 4 tiles per thread: exclusive row and run
-//                offsets per tile and the last kept event before it (kept
-//                and run totals to counts, run_start[n_runs] = n_kept);
+//   k_rec_scan   one CTA: exclusive row and run offsets per tile and the
+//                last kept event before it (kept and run totals to counts,
+//                run_start[n_runs] = n_kept);
 //   k_rec_write  loads all requested columns of its tile up front, ranks the
 //                kept rows and the run heads (ballots, one warp combining the
 //                32 warp-parts of the tile) and stores both.
@@ -167,23 +167,16 @@ __device__ __forceinline__ int64_t pack_last(int64_t tile, int32_t ev) {
   return (int64_t)((uint64_t)tile << 32 | (uint32_t)ev);
 }
 
-// One CTA over all tiles, kScanPer consecutive tiles per thread and 4096
-// tiles per round.  A thread first folds its tiles into one summary (kept
-// rows, run heads after its first kept row, first and last kept event),
-// which composes exactly like a tile's; the block then runs a max-scan for
-// the last kept event before each thread and sum-scans of kept rows and
-// runs (warp shuffles plus one warp scanning the 32 warp totals, four
-// barriers per round), and each thread walks its tiles again to write their
-// offsets.  The next round's summaries are loaded ahead.
-constexpr int kScanPer = 4;
-
+// One CTA over all tiles, 1024 tiles per round: a max-scan for the last
+// kept event before each tile, then sum-scans of its kept rows and runs.
+// Every scan is warp shuffles plus one warp scanning the 32 warp totals;
+// four barriers per round, the next round's summaries loaded ahead.
 __global__ void __launch_bounds__(kRecScanThreads) k_rec_scan(const TileSum *__restrict__ sums, int64_t n_tiles,
                                                               TileOff *__restrict__ offs,
                                                               int64_t *__restrict__ counts,
                                                               int64_t *__restrict__ run_start) {
   constexpr int kW = kRecScanThreads / 32;
   static_assert(kW == 32, "one lane of warp 0 per warp");
-  constexpr int64_t kPerRound = (int64_t)kRecScanThreads * kScanPer;
   __shared__ int64_t w_last[kW], w_rows[kW], w_runs[kW];
   __shared__ int64_t carry_sh[3];  // rows, runs and last key before the round
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -193,43 +186,16 @@ __global__ void __launch_bounds__(kRecScanThreads) k_rec_scan(const TileSum *__r
     carry_sh[1] = 0;
     carry_sh[2] = kNone;
   }
-  TileSum next[kScanPer];
-#pragma unroll
-  for (int j = 0; j < kScanPer; ++j) {
-    const int64_t t = (int64_t)threadIdx.x * kScanPer + j;
-    next[j] = t < n_tiles ? sums[t] : TileSum{0, 0, 0, 0};
-  }
+  TileSum next = threadIdx.x < n_tiles ? sums[threadIdx.x] : TileSum{0, 0, 0, 0};
   __syncthreads();
-  for (int64_t base = 0; base < n_tiles; base += kPerRound) {
-    const int64_t t0 = base + (int64_t)threadIdx.x * kScanPer;
-    TileSum ts[kScanPer];
-#pragma unroll
-    for (int j = 0; j < kScanPer; ++j) {
-      ts[j] = next[j];
-      const int64_t tn = t0 + kPerRound + j;
-      next[j] = tn < n_tiles ? sums[tn] : TileSum{0, 0, 0, 0};
-    }
-    // the thread's tiles folded into one summary
-    int64_t kept = 0, internal = 0, key = kNone;
-    int32_t first = 0, last = 0;
-    bool any = false;
-#pragma unroll
-    for (int j = 0; j < kScanPer; ++j) {
-      kept += ts[j].kept;
-      internal += ts[j].heads;
-      if (ts[j].kept > 0) {
-        if (any) {
-          internal += ts[j].first_ev != last ? 1 : 0;
-        } else {
-          first = ts[j].first_ev;
-        }
-        any = true;
-        last = ts[j].last_ev;
-        key = pack_last(t0 + j, last);
-      }
-    }
+  for (int64_t base = 0; base < n_tiles; base += kRecScanThreads) {
+    const int64_t t = base + threadIdx.x;
+    const TileSum ts = next;
+    const int64_t tn = t + kRecScanThreads;
+    next = tn < n_tiles ? sums[tn] : TileSum{0, 0, 0, 0};
     const int64_t c_rows = carry_sh[0], c_runs = carry_sh[1], c_last = carry_sh[2];
-    // last kept event before the thread's tiles
+    // last kept event before the tile
+    const int64_t key = ts.kept > 0 ? pack_last(t, ts.last_ev) : kNone;
     const int64_t wl = warp_incl_max(key);
     if (lane == 31) w_last[wid] = wl;
     __syncthreads();
@@ -245,9 +211,9 @@ __global__ void __launch_bounds__(kRecScanThreads) k_rec_scan(const TileSum *__r
     const int64_t prev = lane == 0 ? wprev : (lprev > wprev ? lprev : wprev);
     const bool has_prev = prev != kNone;
     const int32_t prev_ev = has_prev ? (int32_t)(uint32_t)(uint64_t)prev : 0;
-    const int64_t runs = any ? internal + ((!has_prev || first != prev_ev) ? 1 : 0) : 0;
+    const int64_t runs = ts.kept > 0 ? ts.heads + ((!has_prev || ts.first_ev != prev_ev) ? 1 : 0) : 0;
     // row and run offsets
-    const int64_t ir = warp_incl_sum64(kept);
+    const int64_t ir = warp_incl_sum64(ts.kept);
     const int64_t iu = warp_incl_sum64(runs);
     if (lane == 31) {
       w_rows[wid] = ir;
@@ -266,21 +232,7 @@ __global__ void __launch_bounds__(kRecScanThreads) k_rec_scan(const TileSum *__r
       }
     }
     __syncthreads();
-    int64_t row = w_rows[wid] + ir - kept, run = w_runs[wid] + iu - runs;
-    bool p_has = has_prev;
-    int32_t p_ev = prev_ev;
-#pragma unroll
-    for (int j = 0; j < kScanPer; ++j) {
-      const int64_t t = t0 + j;
-      const int64_t r = ts[j].kept > 0 ? ts[j].heads + ((!p_has || ts[j].first_ev != p_ev) ? 1 : 0) : 0;
-      if (t < n_tiles) offs[t] = TileOff{row, run, p_ev, p_has ? 1 : 0};
-      row += ts[j].kept;
-      run += r;
-      if (ts[j].kept > 0) {
-        p_has = true;
-        p_ev = ts[j].last_ev;
-      }
-    }
+    if (t < n_tiles) offs[t] = TileOff{w_rows[wid] + ir - ts.kept, w_runs[wid] + iu - runs, prev_ev, has_prev ? 1 : 0};
     // the round's last key: the last thread's inclusive max
     if (threadIdx.x == kRecScanThreads - 1) {
       const int64_t incl = wl > wprev ? wl : wprev;
