@@ -6,7 +6,8 @@
 // and list the runs of equal event id in the kept rows (start offset and
 // event of each run), which is what splitting the output per event needs.
 //
-// Three launches over tiles of 1024 hits (256 threads x 4 sub-tiles):
+// Three launches over tiles of 4096 hits (a block of 256 threads walks four
+// chunks of 1024 hits, 4 sub-tiles each, carrying the tile's state):
 //   k_rec_tiles  reads adc and event and summarises each tile: kept rows,
 //                run heads whose previous kept row is in the tile, first
 //                and last kept event;
@@ -27,8 +28,10 @@ namespace lsim {
 namespace {
 
 constexpr int kRecThreads = 256;                   // threads per block
-constexpr int kRecSub = 4;                         // sub-tiles of kRecThreads rows per tile
-constexpr int kRecTile = kRecThreads * kRecSub;    // 1024 rows per tile
+constexpr int kRecSub = 4;                         // sub-tiles of kRecThreads rows per chunk
+constexpr int kRecChunk = kRecThreads * kRecSub;   // 1024 rows per chunk
+constexpr int kRecChunks = 4;                      // chunks per tile, in order, with a carry
+constexpr int kRecTile = kRecChunk * kRecChunks;   // 4096 rows per tile
 constexpr int kRecWarps = kRecThreads / kWarp;     // 8
 constexpr int kRecParts = kRecSub * kRecWarps;     // 32 warp-parts of 32 rows, one lane of a warp each
 constexpr int kRecScanThreads = 1024;
@@ -111,35 +114,50 @@ __global__ void __launch_bounds__(kRecThreads) k_rec_tiles(const float *__restri
                                                            float adc_lowest, TileSum *__restrict__ sums) {
   __shared__ Part parts[kRecParts];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t base = (int64_t)blockIdx.x * kRecTile + threadIdx.x;
-  float a[kRecSub];
-  int e[kRecSub];
+  // carried by warp 0 from chunk to chunk: the tile's summary so far
+  int kept = 0, heads = 0, first = 0, last = 0;
+  bool any = false;
+#pragma unroll 1
+  for (int c = 0; c < kRecChunks; ++c) {
+    const int64_t base = (int64_t)blockIdx.x * kRecTile + (int64_t)c * kRecChunk + threadIdx.x;
+    float a[kRecSub];
+    int e[kRecSub];
 #pragma unroll
-  for (int s = 0; s < kRecSub; ++s) {
-    const int64_t i = base + s * kRecThreads;
-    a[s] = i < n ? adc[i] : adc_lowest;
-    e[s] = i < n ? event[i] : -1;
-  }
+    for (int s = 0; s < kRecSub; ++s) {
+      const int64_t i = base + s * kRecThreads;
+      a[s] = i < n ? adc[i] : adc_lowest;
+      e[s] = i < n ? event[i] : -1;
+    }
 #pragma unroll
-  for (int s = 0; s < kRecSub; ++s) {
-    unsigned bal;
-    bool hp;
-    int pe;
-    const Part q = warp_part(rec_keep(a[s], e[s], adc_lowest), e[s], bal, hp, pe);
-    if (lane == 0) parts[s * kRecWarps + wid] = q;
+    for (int s = 0; s < kRecSub; ++s) {
+      unsigned bal;
+      bool hp;
+      int pe;
+      const Part q = warp_part(rec_keep(a[s], e[s], adc_lowest), e[s], bal, hp, pe);
+      if (lane == 0) parts[s * kRecWarps + wid] = q;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      const Part q = parts[lane];
+      int prior_last;
+      const bool has_prior = prior_part(q, prior_last);
+      // the previous kept row: in this chunk, else the tile's last so far
+      const bool pp_has = has_prior || any;
+      const int pp_ev = has_prior ? prior_last : last;
+      const int boundary = q.kept > 0 && pp_has && q.first_ev != pp_ev;
+      kept += __reduce_add_sync(kFull, (unsigned)q.kept);
+      heads += __reduce_add_sync(kFull, (unsigned)(q.heads + boundary));
+      const unsigned kb = __ballot_sync(kFull, q.kept > 0);
+      if (kb) {
+        const int cf = __shfl_sync(kFull, q.first_ev, __ffs(kb) - 1);
+        if (!any) first = cf;
+        last = __shfl_sync(kFull, q.last_ev, 31 - __clz(kb));
+        any = true;
+      }
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  if (wid != 0) return;
-  const Part q = parts[lane];
-  int prior_last;
-  const bool has_prior = prior_part(q, prior_last);
-  const int boundary = q.kept > 0 && has_prior && q.first_ev != prior_last;
-  const int kept = __reduce_add_sync(kFull, (unsigned)q.kept);
-  const int heads = __reduce_add_sync(kFull, (unsigned)(q.heads + boundary));
-  const unsigned kb = __ballot_sync(kFull, q.kept > 0);
-  const int first = __shfl_sync(kFull, q.first_ev, kb ? __ffs(kb) - 1 : 0);
-  const int last = __shfl_sync(kFull, q.last_ev, kb ? 31 - __clz(kb) : 0);
-  if (lane == 0) sums[blockIdx.x] = TileSum{kept, heads, first, last};
+  if (threadIdx.x == 0) sums[blockIdx.x] = TileSum{kept, heads, first, last};
 }
 
 // Inclusive warp scans (max, sum) of one int64 per lane.
@@ -247,7 +265,7 @@ __global__ void __launch_bounds__(kRecScanThreads) k_rec_scan(const TileSum *__r
   }
 }
 
-__global__ void __launch_bounds__(kRecThreads) k_rec_write(LsimParams p, LsimHitColumns in, int64_t n,
+__global__ void __launch_bounds__(kRecThreads, 4) k_rec_write(LsimParams p, LsimHitColumns in, int64_t n,
                                                            float adc_lowest, const TileOff *__restrict__ offs,
                                                            LsimHitColumns out, float *__restrict__ out_clean,
                                                            float *__restrict__ out_q, int32_t *__restrict__ run_event,
@@ -256,68 +274,83 @@ __global__ void __launch_bounds__(kRecThreads) k_rec_write(LsimParams p, LsimHit
   __shared__ int part_row[kRecParts], part_run[kRecParts], part_prev_ev[kRecParts];
   __shared__ bool part_prev_has[kRecParts];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t base = (int64_t)blockIdx.x * kRecTile + threadIdx.x;
-  float a[kRecSub], x[kRecSub], y[kRecSub], z[kRecSub], tk[kRecSub], hp[kRecSub];
-  int ev[kRecSub], px[kRecSub];
-#pragma unroll
-  for (int s = 0; s < kRecSub; ++s) {
-    const int64_t i = base + s * kRecThreads;
-    const bool in_range = i < n;
-    a[s] = in_range ? in.adc[i] : adc_lowest;
-    ev[s] = in_range ? in.event[i] : -1;
-    x[s] = in_range && out.pixel_x ? in.pixel_x[i] : 0.f;
-    y[s] = in_range && out.pixel_y ? in.pixel_y[i] : 0.f;
-    z[s] = in_range && out.pixel_z ? in.pixel_z[i] : 0.f;
-    tk[s] = in_range && out.ticks ? in.ticks[i] : 0.f;
-    hp[s] = in_range && out.hit_prob ? in.hit_prob[i] : 0.f;
-    px[s] = in_range && out.pixels ? in.pixels[i] : 0;
-  }
-  unsigned bal[kRecSub];
-  bool has_prev[kRecSub];
-  int prev_ev[kRecSub];
-#pragma unroll
-  for (int s = 0; s < kRecSub; ++s) {
-    const Part q = warp_part(rec_keep(a[s], ev[s], adc_lowest), ev[s], bal[s], has_prev[s], prev_ev[s]);
-    if (lane == 0) parts[s * kRecWarps + wid] = q;
-  }
   const TileOff to = offs[blockIdx.x];
-  __syncthreads();
-  if (wid == 0) {
-    const Part q = parts[lane];
-    int prior_last;
-    const bool has_prior = prior_part(q, prior_last);
-    const bool pp_has = has_prior || to.has_prev;
-    const int pp_ev = has_prior ? prior_last : to.prev_ev;
-    const int heads = q.heads + (q.kept > 0 && (!pp_has || q.first_ev != pp_ev) ? 1 : 0);
-    part_row[lane] = warp_incl_sum(q.kept) - q.kept;
-    part_run[lane] = warp_incl_sum(heads) - heads;
-    part_prev_has[lane] = pp_has;
-    part_prev_ev[lane] = pp_ev;
-  }
-  __syncthreads();
+  // carried by warp 0 from chunk to chunk: rows and runs of the tile so far
+  // and the last kept event before the next chunk
+  int c_row = 0, c_run = 0, c_ev = to.prev_ev;
+  bool c_has = to.has_prev != 0;
+#pragma unroll 1
+  for (int c = 0; c < kRecChunks; ++c) {
+    const int64_t base = (int64_t)blockIdx.x * kRecTile + (int64_t)c * kRecChunk + threadIdx.x;
+    float a[kRecSub], x[kRecSub], y[kRecSub], z[kRecSub], tk[kRecSub], hp[kRecSub];
+    int ev[kRecSub], px[kRecSub];
 #pragma unroll
-  for (int s = 0; s < kRecSub; ++s) {
-    const int pi = s * kRecWarps + wid;
-    const bool keep = (bal[s] >> lane) & 1u;
-    const bool head = keep && (has_prev[s] ? ev[s] != prev_ev[s]
-                                           : (part_prev_has[pi] ? ev[s] != part_prev_ev[pi] : true));
-    const unsigned hb = __ballot_sync(kFull, head);
-    if (!keep) continue;
-    const int64_t o = to.row + part_row[pi] + __popc(bal[s] & lanes_below());
-    out.event[o] = ev[s];
-    if (out.adc) out.adc[o] = a[s];
-    if (out_clean) out_clean[o] = __fsub_rn(a[s], adc_lowest);
-    if (out_q) out_q[o] = adc_to_charge(p, a[s]);
-    if (out.pixel_x) out.pixel_x[o] = x[s];
-    if (out.pixel_y) out.pixel_y[o] = y[s];
-    if (out.pixel_z) out.pixel_z[o] = z[s];
-    if (out.ticks) out.ticks[o] = tk[s];
-    if (out.hit_prob) out.hit_prob[o] = hp[s];
-    if (out.pixels) out.pixels[o] = px[s];
-    if (head && run_start) {
-      const int64_t k = to.run + part_run[pi] + __popc(hb & lanes_below());
-      run_start[k] = o;
-      if (run_event) run_event[k] = ev[s];
+    for (int s = 0; s < kRecSub; ++s) {
+      const int64_t i = base + s * kRecThreads;
+      const bool in_range = i < n;
+      a[s] = in_range ? in.adc[i] : adc_lowest;
+      ev[s] = in_range ? in.event[i] : -1;
+      x[s] = in_range && out.pixel_x ? in.pixel_x[i] : 0.f;
+      y[s] = in_range && out.pixel_y ? in.pixel_y[i] : 0.f;
+      z[s] = in_range && out.pixel_z ? in.pixel_z[i] : 0.f;
+      tk[s] = in_range && out.ticks ? in.ticks[i] : 0.f;
+      hp[s] = in_range && out.hit_prob ? in.hit_prob[i] : 0.f;
+      px[s] = in_range && out.pixels ? in.pixels[i] : 0;
+    }
+    unsigned bal[kRecSub];
+    bool has_prev[kRecSub];
+    int prev_ev[kRecSub];
+#pragma unroll
+    for (int s = 0; s < kRecSub; ++s) {
+      const Part q = warp_part(rec_keep(a[s], ev[s], adc_lowest), ev[s], bal[s], has_prev[s], prev_ev[s]);
+      if (lane == 0) parts[s * kRecWarps + wid] = q;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      const Part q = parts[lane];
+      int prior_last;
+      const bool has_prior = prior_part(q, prior_last);
+      const bool pp_has = has_prior || c_has;
+      const int pp_ev = has_prior ? prior_last : c_ev;
+      const int heads = q.heads + (q.kept > 0 && (!pp_has || q.first_ev != pp_ev) ? 1 : 0);
+      const int ir = warp_incl_sum(q.kept), iu = warp_incl_sum(heads);
+      part_row[lane] = c_row + ir - q.kept;
+      part_run[lane] = c_run + iu - heads;
+      part_prev_has[lane] = pp_has;
+      part_prev_ev[lane] = pp_ev;
+      c_row += __shfl_sync(kFull, ir, 31);
+      c_run += __shfl_sync(kFull, iu, 31);
+      const unsigned kb = __ballot_sync(kFull, q.kept > 0);
+      if (kb) {
+        c_ev = __shfl_sync(kFull, q.last_ev, 31 - __clz(kb));
+        c_has = true;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < kRecSub; ++s) {
+      const int pi = s * kRecWarps + wid;
+      const bool keep = (bal[s] >> lane) & 1u;
+      const bool head = keep && (has_prev[s] ? ev[s] != prev_ev[s]
+                                             : (part_prev_has[pi] ? ev[s] != part_prev_ev[pi] : true));
+      const unsigned hb = __ballot_sync(kFull, head);
+      if (!keep) continue;
+      const int64_t o = to.row + part_row[pi] + __popc(bal[s] & lanes_below());
+      out.event[o] = ev[s];
+      if (out.adc) out.adc[o] = a[s];
+      if (out_clean) out_clean[o] = __fsub_rn(a[s], adc_lowest);
+      if (out_q) out_q[o] = adc_to_charge(p, a[s]);
+      if (out.pixel_x) out.pixel_x[o] = x[s];
+      if (out.pixel_y) out.pixel_y[o] = y[s];
+      if (out.pixel_z) out.pixel_z[o] = z[s];
+      if (out.ticks) out.ticks[o] = tk[s];
+      if (out.hit_prob) out.hit_prob[o] = hp[s];
+      if (out.pixels) out.pixels[o] = px[s];
+      if (head && run_start) {
+        const int64_t k = to.run + part_run[pi] + __popc(hb & lanes_below());
+        run_start[k] = o;
+        if (run_event) run_event[k] = ev[s];
+      }
     }
   }
 }
