@@ -242,7 +242,8 @@ def test_hit_records_rejects_bad_arguments_without_gpu(lib):
     cols = _abi.LsimHitColumns(16, 16, 16, 16, 16, 16, 16, 16)
     no_pix = _abi.LsimHitColumns(16, 16, 16, 16, 16, 16, 16, None)
     counts = V(64)
-    assert lib.lsim_hit_records_workspace_bytes(3_000_000) >= 2 * 8 * (3_000_000 // 1024)
+    # a 16-byte summary and a 24-byte offset record per tile of 4096 hits
+    assert lib.lsim_hit_records_workspace_bytes(3_000_000) >= 40 * (3_000_000 // 4096)
     assert lib.lsim_hit_records(None, 80.0, cols, 10, cols, None, None, None, None, counts, V(256), 1 << 20,
                                 None) == _abi.LSIM_ERR_INVALID
     assert lib.lsim_hit_records(p, 80.0, cols, 10, cols, None, None, None, None, None, V(256), 1 << 20,
