@@ -4,7 +4,6 @@ jax.scipy.special.logsumexp, lax.top_k and the reference's log_diff_ndtr,
 fee_jax.py:13-53) against float64 / arbitrary-precision values: the
 accuracy the probabilistic parity tests rest on."""
 
-import mpmath
 import numpy as np
 import pytest
 from scipy import special
@@ -69,6 +68,7 @@ def test_top_k_order_matches_lax_top_k():
 
 @pytest.mark.parametrize("a,b", [(0.3, -0.4), (2.0, 1.0), (-3.0, -3.6), (-9.0, -11.0), (6.0, -1.0), (1.5, 1.0)])
 def test_log_diff_ndtr_where_the_clamps_are_inactive(a, b):
+    mpmath = pytest.importorskip("mpmath")
     mpmath.mp.dps = 50
     exact = float(mpmath.log(mpmath.ncdf(a) - mpmath.ncdf(b)))
     got = float(R.log_diff_ndtr32(F(a), F(b)))
