@@ -858,8 +858,9 @@ def top_k_indices(x, k):
 
 def find_one_hit_step(q_sum, charges, log_probs, sigma, threshold, interval, n_values):
     """fee_jax.py:334-384 for P pixels at once: q_sum (P, T), charges and
-    log_probs (P, K).  Returns (charges', log_probs') and the step outputs
-    (log_total_hit_dist_tick (P, T-1), esperance_value (P, T-1))."""
+    log_probs (P, K).  Returns (charges', log_probs'), the step outputs
+    (log_total_hit_dist_tick (P, T-1), esperance_value (P, T-1)) and the
+    top-K tick choices (P, K)."""
     P, T = q_sum.shape
     z = F32(1.0 / sigma)
     thr = F32(threshold)
@@ -888,14 +889,16 @@ def find_one_hit_step(q_sum, charges, log_probs, sigma, threshold, interval, n_v
     new_lp = np.take_along_axis(dist, top, axis=1)
     best = np.clip(sh[top] + 1, 0, T - 1)
     new_c = np.take_along_axis(q_sum, best, axis=1)
-    return (new_c.astype(F32), new_lp.astype(F32)), (hit, esp)
+    return (new_c.astype(F32), new_lp.astype(F32)), (hit, esp), top
 
 
-def get_adc_values_average_noise(params, wfs, stop_threshold=1e-9):
+def get_adc_values_average_noise(params, wfs, stop_threshold=1e-9, return_choices=False):
     """fee_jax.py:386-461: beam search over MAX_ADC_VALUES hits with
     fee_paths_scaling paths, stopped for the whole batch once no pixel keeps
     a total path probability above stop_threshold.  Returns
-    (log_prob (P, H, T-1), charge (P, H, T-1))."""
+    (log_prob (P, H, T-1), charge (P, H, T-1)); with return_choices also
+    the top-K tick choices of every executed step (P, H, K) and the number
+    of executed steps, the inputs of beam_search64."""
     wfs = np.asarray(wfs, F32)
     P, T = wfs.shape
     K = int(params.fee_paths_scaling)
@@ -909,14 +912,19 @@ def get_adc_values_average_noise(params, wfs, stop_threshold=1e-9):
     out_lp = np.full((P, H, T - 1), F32(-1000))
     out_q = np.zeros((P, H, T - 1), F32)
     active = True
+    top = np.zeros((P, H, K), np.int64)
+    n_exec = 0
     for h in range(H):
         if not active:
             break
-        (c, lp), (hit, esp) = find_one_hit_step(q_sum, c, lp, params.RESET_NOISE_CHARGE,
-                                                 params.DISCRIMINATION_THRESHOLD, interval, K)
+        (c, lp), (hit, esp), top[:, h] = find_one_hit_step(q_sum, c, lp, params.RESET_NOISE_CHARGE,
+                                                            params.DISCRIMINATION_THRESHOLD, interval, K)
+        n_exec = h + 1
         out_lp[:, h] = hit
         out_q[:, h] = esp
         active = bool(np.any(logsumexp32(lp, axis=1) > log_stop))
+    if return_choices:
+        return out_lp, out_q, top, n_exec
     return out_lp, out_q
 
 

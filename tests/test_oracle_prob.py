@@ -85,3 +85,31 @@ def test_log_diff_ndtr_clamps():
     # so the result is log(1e-30 + log(2) * 1e-10) (the reference's own clamp)
     v = float(R.log_diff_ndtr32(F(12.0), F(11.5)))
     assert v == pytest.approx(np.log(1e-30 + np.log(2) * 1e-10), abs=1e-4)
+
+
+def _waveforms(seed, P=6, T=401):
+    rng = np.random.default_rng(seed)
+    w = np.full((P, T), 2.0, np.float32)             # small pedestal: no flat stretches
+    for p in range(P):
+        for _ in range(int(rng.integers(1, 4))):
+            t0 = int(rng.integers(20, T - 80))
+            w[p, t0:t0 + 30] += rng.uniform(300, 3000)
+    return w
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_float32_beam_search_agrees_with_float64(seed):
+    """The float32 restatement (the probabilistic parity reference) against
+    the float64 one with the same top-K choices: the two share no code."""
+    from larndsim_gb300 import consts
+    p = consts.Params(RESET_NOISE_CHARGE=900.0, MAX_ADC_VALUES=4)
+    w = _waveforms(seed)
+    lp32, q32, top, n_exec = R.get_adc_values_average_noise(p, w, return_choices=True)
+    lp64, q64 = R.beam_search64(p, w, top, n_exec)
+    assert n_exec >= 1
+    pr32, pr64 = np.exp(lp32.astype(np.float64)), np.exp(lp64)
+    assert np.abs(pr32 - pr64).max() < 5e-5
+    hi = lp64 > -5
+    assert np.abs(lp32[hi] - lp64[hi]).max() < 5e-4
+    scale = np.abs(q64).max(axis=-1, keepdims=True) + 1.0
+    assert (np.abs(q32 - q64) / scale).max() < 1e-5
