@@ -121,3 +121,36 @@ def test_target_batches_bitwise(cuda, gold, name):
     for i in range(len(ds)):
         got = ds[i].cpu().numpy()
         np.testing.assert_array_equal(_bits(got), _bits(gold[f"{name}/batch_{i}"]), err_msg=f"batch {i}")
+
+
+def test_driver_loop_end_to_end(cuda, gold, tmp_path):
+    """The simulate driver's loop (optimize/simulate.py:91-179) on the GPU:
+    dataset batches, the id checks, simulate_wfs + simulate_stochastic, the
+    hit records and the --out_np archive, each batch's hits equal to the
+    oracle's chain on the same batch."""
+    from larndsim_gb300 import consts, detsim, output, sim, workloads
+    params = consts.Params(number_pix_neighbors=1, RESET_NOISE_CHARGE=0, UNCORRELATED_NOISE_CHARGE=0,
+                           long_diff_template=consts.jax_linspace_f32(0.001, 10, 10))
+    tmpl = R.load_lut_templates(workloads.synthetic_response(seed=0, nx=15, ny=15), params)
+    ds = make(gold, "batched")
+    fields = ds.get_track_fields()
+    recs = []
+    sim.reset_size_history()
+    hist = {}                                   # the oracle's pad_size history, in step with the GPU's
+    for i in range(len(ds)):
+        batch = ds[i]
+        ev = batch[:, fields.index("eventID")].cpu().numpy()
+        detsim.validate_local_event_ids(ev, context=f"batch {i}")
+        detsim.validate_event_ids_for_packing(params, ev, kind="pixel")
+        wfs, unique = sim.simulate_wfs(params, torch.from_numpy(tmpl).cuda(), batch, fields)
+        out = sim.simulate_stochastic(params, wfs, unique, i)
+        rec = output.hit_records(params, out)
+        recs.append(rec)
+        wo, uo = R.simulate_wfs(params, tmpl, batch.cpu().numpy(), fields, history=hist)
+        ref = R.simulate_stochastic(params, wo, uo)
+        assert rec["adc"].numel() <= ref["nb_valid"]
+        np.testing.assert_array_equal(unique.cpu().numpy(), uo)
+    path = tmp_path / "hits.npz"
+    output.write_hits_npz(path, recs)
+    d = np.load(path)
+    assert d["adcs"].shape[0] == sum(r["adc"].numel() for r in recs)
