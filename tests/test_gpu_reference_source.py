@@ -1,0 +1,83 @@
+"""The CUDA LUT path against outputs of the reference's own source code.
+
+tests/golden/lut_ref.npz holds what larnd-sim-jax's load_lut,
+simulate_wfs, get_adc_values, digitize and simulate_stochastic return on
+seeded events (made by tests/golden/make_lut_golden.py, which runs the
+reference's modules with a numpy stand-in for jax; the oracle reproduces
+them, tests/test_oracle_lut_golden.py).  Here the same inputs go through
+this package's load_lut, simulate_wfs, get_adc_values and
+simulate_stochastic on the GPU, at the tolerances of the other parity
+tests: template bank within 2e-5 relative (2e-6 of its largest value),
+unique_pixels identical, waveforms within 1e-5 of each simulated row's
+largest |w|, hit ticks identical except near-threshold crossings (under
+0.5 % of the hit slots), ADCs within 1e-5 relative.  The waveform and hit
+comparisons use the oracle's template bank, as the other parity tests do.
+The cases at signal_length 150 run here; the signal_length 100 case is
+checked by the oracle test only.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_common import ADC_RTOL, WFS_RTOL, compare_fee, compare_wfs
+from test_oracle_lut_golden import GOLD, HIT_KEYS, _cases, _dense_wfs, _setup
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+def _gpu_cases():
+    with np.load(GOLD) as g:
+        import json
+        return [n for n in _cases() if json.loads(str(g[f"{n}/config"]))["L"] == 150]
+
+
+@pytest.mark.parametrize("name", _gpu_cases())
+def test_cuda_lut_path_matches_reference_source(cuda, gold, name):
+    from larndsim_gb300 import sim
+    from oracle import reference_np as R
+    cfg, p, resp, tracks, fields = _setup(gold, name, strict=False)
+
+    tmpl_gpu, _ = sim.load_lut(resp, p)
+    got = tmpl_gpu.cpu().numpy().ravel()[gold[f"{name}/tmpl_index"]]
+    ref = gold[f"{name}/tmpl_value"]
+    np.testing.assert_allclose(got, ref, rtol=2e-5, atol=2e-6 * np.abs(ref).max())
+
+    tmpl = torch.from_numpy(R.load_lut_templates(resp, p)).cuda()
+    sim.reset_size_history()
+    wfs, unique = sim.simulate_wfs(p, tmpl, tracks, fields)
+    w, u = wfs.cpu().numpy(), unique.cpu().numpy()
+    ref_w = _dense_wfs(gold, name)
+    assert compare_wfs(w, u, ref_w, gold[f"{name}/unique_pixels"]) < WFS_RTOL
+    assert np.all(w[u < 0] == 0)          # rows of negative pixel id are zero here by design
+
+    # the front end on the reference's own waveforms
+    integral, ticks = sim.get_adc_values(p, torch.from_numpy(ref_w).cuda())
+    frac, err = compare_fee(integral.cpu().numpy(), ticks.cpu().numpy(), gold[f"{name}/integral"],
+                            gold[f"{name}/ticks"], p)
+    assert frac < 0.005 and err < ADC_RTOL, (frac, err)
+
+    # the whole chain, on the simulated rows (parse_output drops the rows of
+    # negative pixel id, which are zero here and hold the reference's
+    # unmatched neighbour charge there)
+    out, (grid_adcs, grid_ticks) = sim.simulate_stochastic(p, wfs, unique, 0, return_grids=True)
+    v = u >= 0
+    frac, err = compare_fee(grid_adcs.cpu().numpy()[v], grid_ticks.cpu().numpy()[v], gold[f"{name}/grid_adcs"][v],
+                            gold[f"{name}/ticks"][v])
+    assert frac < 0.005 and err < ADC_RTOL, (frac, err)
+    if frac == 0:
+        hits = {k: v.cpu().numpy() for k, v in zip(HIT_KEYS, out)}
+        ref_hits = {k: gold[f"{name}/hits_{k}"] for k in HIT_KEYS}
+        assert hits["adcs"].shape == ref_hits["adcs"].shape
+        for k in ("pixels", "event", "ticks", "hit_prob"):
+            np.testing.assert_array_equal(hits[k], ref_hits[k], err_msg=k)
+        np.testing.assert_allclose(hits["adcs"], ref_hits["adcs"], rtol=ADC_RTOL)
+        for k in ("pixel_x", "pixel_y", "pixel_z"):
+            np.testing.assert_allclose(hits[k], ref_hits[k], rtol=3e-7, atol=3e-6, err_msg=k)
