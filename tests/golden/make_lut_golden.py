@@ -76,17 +76,26 @@ def response_checksum(resp):
     return int(zlib.crc32(np.ascontiguousarray(resp, np.float32).tobytes()))
 
 
-def main():
+def load_reference(ref=REF):
+    """The reference's consts_jax, fee_jax and sim_jax modules imported
+    with the numpy stand-in, and its module0 parameters (no gradient
+    fields) from its own YAML files."""
     jax_numpy_standin.install(yaml_lite.loads)
-    sys.path[:0] = [str(REF / "src"), str(REF)]
+    sys.path[:0] = [str(ref / "src"), str(ref)]
     from larndsim import consts_jax as C
     from larndsim import fee_jax as F
     from larndsim import sim_jax as S
-    import jax.numpy as jnp
 
     Params = C.build_params_class([])
-    base = C.load_detector_properties(Params, str(REF / "src/larndsim/detector_properties/module0.yaml"),
-                                      str(REF / "src/larndsim/pixel_layouts/multi_tile_layout-2.4.16_v4.yaml"))
+    base = C.load_detector_properties(Params, str(ref / "src/larndsim/detector_properties/module0.yaml"),
+                                      str(ref / "src/larndsim/pixel_layouts/multi_tile_layout-2.4.16_v4.yaml"))
+    return C, F, S, base
+
+
+def main():
+    C, F, S, base = load_reference()
+    import jax.numpy as jnp
+
     out = {}
     tmp = Path(tempfile.mkdtemp())
     for name, case in CASES.items():

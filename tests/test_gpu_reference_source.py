@@ -1,4 +1,5 @@
-"""The CUDA LUT path against outputs of the reference's own source code.
+"""The CUDA LUT and parametrised paths against outputs of the reference's
+own source code.
 
 tests/golden/lut_ref.npz holds what larnd-sim-jax's load_lut,
 simulate_wfs, get_adc_values, digitize and simulate_stochastic return on
@@ -13,7 +14,9 @@ largest |w|, hit ticks identical except near-threshold crossings (under
 0.5 % of the hit slots), ADCs within 1e-5 relative.  The waveform and hit
 comparisons use the oracle's template bank, as the other parity tests do.
 The cases at signal_length 150 run here; the signal_length 100 case is
-checked by the oracle test only.
+checked by the oracle test only.  The parametrised-mode cases
+(tests/golden/param_ref.npz, tests/golden/make_param_golden.py) run
+simulate_parametrized with the diffusion draws the reference made.
 """
 
 from __future__ import annotations
@@ -24,6 +27,8 @@ import torch
 
 from gpu_common import ADC_RTOL, WFS_RTOL, compare_fee, compare_wfs
 from test_oracle_lut_golden import GOLD, HIT_KEYS, _cases, _dense_wfs, _setup
+from test_oracle_param_golden import GOLD as PARAM_GOLD
+from test_oracle_param_golden import param_cases, param_dense_wfs, param_setup
 
 pytestmark = pytest.mark.gpu
 
@@ -81,3 +86,34 @@ def test_cuda_lut_path_matches_reference_source(cuda, gold, name):
         np.testing.assert_allclose(hits["adcs"], ref_hits["adcs"], rtol=ADC_RTOL)
         for k in ("pixel_x", "pixel_y", "pixel_z"):
             np.testing.assert_allclose(hits[k], ref_hits[k], rtol=3e-7, atol=3e-6, err_msg=k)
+
+
+@pytest.mark.parametrize("name", param_cases())
+def test_cuda_parametrized_path_matches_reference_source(cuda, name):
+    """simulate_parametrized on the GPU with the diffusion draws the
+    reference used (tests/golden/param_ref.npz)."""
+    from larndsim_gb300 import sim
+    pgold = np.load(PARAM_GOLD)
+    p, tracks, fields, draws = param_setup(pgold, name)
+    sim.reset_size_history()
+    out, wfs, unique = sim.simulate_parametrized(p, tracks, fields, offsets=torch.from_numpy(draws).cuda(),
+                                                 return_wfs=True)
+    w, u = wfs.cpu().numpy(), unique.cpu().numpy()
+    ref_w = param_dense_wfs(pgold, name)
+    assert compare_wfs(w, u, ref_w, pgold[f"{name}/unique_pixels"]) < WFS_RTOL
+    integral, ticks = sim.get_adc_values(p, torch.from_numpy(ref_w).cuda())
+    frac, err = compare_fee(integral.cpu().numpy(), ticks.cpu().numpy(), pgold[f"{name}/integral"],
+                            pgold[f"{name}/ticks"], p)
+    assert frac < 0.005 and err < ADC_RTOL, (frac, err)
+    hits = {k: v.cpu().numpy() for k, v in zip(HIT_KEYS, out)}
+    ref_hits = {k: pgold[f"{name}/hits_{k}"] for k in HIT_KEYS}
+    if hits["adcs"].shape == ref_hits["adcs"].shape and np.array_equal(hits["ticks"], ref_hits["ticks"]):
+        for k in ("pixels", "event", "hit_prob"):
+            np.testing.assert_array_equal(hits[k], ref_hits[k], err_msg=k)
+        np.testing.assert_allclose(hits["adcs"], ref_hits["adcs"], rtol=ADC_RTOL)
+        for k in ("pixel_x", "pixel_y", "pixel_z"):
+            np.testing.assert_allclose(hits[k], ref_hits[k], rtol=3e-7, atol=3e-6, err_msg=k)
+    else:
+        # a near-threshold crossing moved: at most a few hit slots differ
+        n_ref = ref_hits["adcs"].shape[0]
+        assert abs(hits["adcs"].shape[0] - n_ref) <= max(1, n_ref // 200)
