@@ -16,7 +16,10 @@ comparisons use the oracle's template bank, as the other parity tests do.
 The cases at signal_length 150 run here; the signal_length 100 case is
 checked by the oracle test only.  The parametrised-mode cases
 (tests/golden/param_ref.npz, tests/golden/make_param_golden.py) run
-simulate_parametrized with the diffusion draws the reference made.
+simulate_parametrized with the diffusion draws the reference made.  The
+probabilistic front end (tests/golden/prob_ref.npz,
+tests/golden/make_prob_golden.py) runs at the default 20 paths with the
+tolerances of tests/test_gpu_fee_prob.py.
 """
 
 from __future__ import annotations
@@ -29,6 +32,8 @@ from gpu_common import ADC_RTOL, WFS_RTOL, compare_fee, compare_wfs
 from test_oracle_lut_golden import GOLD, HIT_KEYS, _cases, _dense_wfs, _setup
 from test_oracle_param_golden import GOLD as PARAM_GOLD
 from test_oracle_param_golden import param_cases, param_dense_wfs, param_setup
+from test_oracle_prob_golden import GOLD as PROB_GOLD
+from test_oracle_prob_golden import check_distributions, check_expected, prob_cases, prob_setup
 
 pytestmark = pytest.mark.gpu
 
@@ -117,3 +122,29 @@ def test_cuda_parametrized_path_matches_reference_source(cuda, name):
         # a near-threshold crossing moved: at most a few hit slots differ
         n_ref = ref_hits["adcs"].shape[0]
         assert abs(hits["adcs"].shape[0] - n_ref) <= max(1, n_ref // 200)
+
+
+def _prob_cases_default_paths():
+    import json
+    with np.load(PROB_GOLD) as g:
+        return [n for n in prob_cases() if json.loads(str(g[f"{n}/config"]))["fee_paths_scaling"] == 20]
+
+
+@pytest.mark.parametrize("name", _prob_cases_default_paths())
+def test_cuda_probabilistic_front_end_matches_reference_source(cuda, name):
+    """The beam search, the fused expected values and
+    simulate_probabilistic on the GPU, on rows of the reference's own
+    waveforms."""
+    from larndsim_gb300 import sim
+    pgold = np.load(PROB_GOLD)
+    cfg, p, rows, pixels, keep = prob_setup(pgold, name)
+    w = torch.from_numpy(rows).cuda()
+    log_prob, charge = sim.get_adc_values_average_noise_vmap(p, w)
+    check_distributions(log_prob.cpu().numpy(), charge.cpu().numpy(), pgold, name, keep, cfg, charge_rtol=1e-5,
+                        support_margin=(20.0, 20.0))
+    e_tick, e_adc, lam = (t.cpu().numpy() for t in sim.average_hit_values(p, w))
+    check_expected(e_tick, e_adc, lam, pgold, name, rtol=1e-3)
+    _, px, py, _, event = sim.simulate_probabilistic(p, w, torch.from_numpy(pixels).cuda())
+    np.testing.assert_allclose(px.cpu().numpy(), pgold[f"{name}/pixel_x"], rtol=3e-7, atol=3e-6)
+    np.testing.assert_allclose(py.cpu().numpy(), pgold[f"{name}/pixel_y"], rtol=3e-7, atol=3e-6)
+    np.testing.assert_array_equal(event.cpu().numpy(), pgold[f"{name}/event"])
