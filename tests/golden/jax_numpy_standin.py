@@ -6,7 +6,8 @@ Test infrastructure only: nothing in the package imports it.  It encodes
 JAX's documented semantics with 64-bit types disabled (the reference never
 enables them):
 
-* every array is 32-bit: float64 / int64 results, numpy float64 inputs and
+* every array is 32-bit (unless installed with x64=True, JAX's
+  jax_enable_x64): float64 / int64 results, numpy float64 inputs and
   ``astype(int)`` / ``astype(float)`` narrow to float32 / int32, while
   Python scalars stay weakly typed (numpy 2 follows the same promotion rule
   for them, NEP 50), except that an integer array met by a Python float,
@@ -45,9 +46,12 @@ _NARROW = {np.dtype(np.float64): np.dtype(np.float32), np.dtype(np.int64): np.dt
            np.dtype(np.uint64): np.dtype(np.uint32), np.dtype(np.complex128): np.dtype(np.complex64)}
 
 
+_X64 = [False]      # install(x64=True): JAX with jax_enable_x64, nothing narrowed
+
+
 def _narrow_dtype(dt):
     dt = np.dtype(dt)
-    return _NARROW.get(dt, dt)
+    return dt if _X64[0] else _NARROW.get(dt, dt)
 
 
 class JArr(np.ndarray):
@@ -58,7 +62,7 @@ class JArr(np.ndarray):
             raise TypeError("JAX arrays are immutable: no out= arguments")
         args = [_plain(_x32(x)) for x in inputs]
         res = getattr(ufunc, method)(*args, **kwargs)
-        if any(np.asarray(r).dtype == np.float64 for r in (res if isinstance(res, tuple) else (res,))):
+        if not _X64[0] and any(np.asarray(r).dtype == np.float64 for r in (res if isinstance(res, tuple) else (res,))):
             # numpy promotes an int32 operand with a Python float (or a true
             # division of integers) to float64; JAX converts the integer
             # operand to float32 and computes in float32
@@ -289,13 +293,14 @@ def _wrap_np(fn):
 def linspace(start, stop, num=50, endpoint=True, retstep=False, dtype=None, axis=0):
     if not endpoint or retstep or axis != 0:
         raise NotImplementedError("linspace with endpoint=False, retstep or axis")
-    s, e = np.float32(start), np.float32(stop)
+    ft = np.float64 if _X64[0] else np.float32
+    s, e = ft(start), ft(stop)
     if num == 1:
-        return _x32(np.array([s], np.float32))
+        return _x32(np.array([s], ft))
     div = num - 1
-    step = (np.arange(div, dtype=np.float32) / np.float32(div)).astype(np.float32)
-    body = (s * (np.float32(1) - step) + e * step).astype(np.float32)
-    return _x32(np.concatenate([body, np.array([e], np.float32)]))
+    step = (np.arange(div, dtype=ft) / ft(div)).astype(ft)
+    body = (s * (ft(1) - step) + e * step).astype(ft)
+    return _x32(np.concatenate([body, np.array([e], ft)]))
 
 
 def where(condition, x=None, y=None, *, size=None, fill_value=None):
@@ -495,9 +500,12 @@ def _module(name, **attrs):
     return m
 
 
-def install(yaml_loads):
+def install(yaml_loads, x64=False):
     """Register jax, flax, yaml (parsed with ``yaml_loads(text)``) and an
-    empty h5py in sys.modules.  Call before importing the reference."""
+    empty h5py in sys.modules.  Call before importing the reference.
+    ``x64``: JAX's semantics with jax_enable_x64 (64-bit types kept, float64
+    linspace); a float32 input array then still computes in float32."""
+    _X64[0] = bool(x64)
     jnp = _make_jnp()
     lax = _module("jax.lax", scan=scan, cummax=cummax, top_k=top_k, cond=cond, fori_loop=fori_loop,
                   stop_gradient=_identity)

@@ -76,11 +76,11 @@ def response_checksum(resp):
     return int(zlib.crc32(np.ascontiguousarray(resp, np.float32).tobytes()))
 
 
-def load_reference(ref=REF):
+def load_reference(ref=REF, x64=False):
     """The reference's consts_jax, fee_jax and sim_jax modules imported
-    with the numpy stand-in, and its module0 parameters (no gradient
-    fields) from its own YAML files."""
-    jax_numpy_standin.install(yaml_lite.loads)
+    with the numpy stand-in (``x64``: with 64-bit types enabled), and its
+    module0 parameters (no gradient fields) from its own YAML files."""
+    jax_numpy_standin.install(yaml_lite.loads, x64=x64)
     sys.path[:0] = [str(ref / "src"), str(ref)]
     from larndsim import consts_jax as C
     from larndsim import fee_jax as F

@@ -19,7 +19,12 @@ checked by the oracle test only.  The parametrised-mode cases
 simulate_parametrized with the diffusion draws the reference made.  The
 probabilistic front end (tests/golden/prob_ref.npz,
 tests/golden/make_prob_golden.py) runs at the default 20 paths with the
-tolerances of tests/test_gpu_fee_prob.py.
+tolerances of tests/test_gpu_fee_prob.py.  The gradient
+(tests/golden/grad_ref.npz, tests/golden/make_grad_golden.py: central
+differences of the reference's own chain in float64 at fixed decisions)
+is compared as the vector-Jacobian product for the reference's cotangent,
+within 2e-4 relative per component (the GPU-against-oracle bound of
+tests/test_gpu_grad.py, 1e-4, plus the oracle's observed 4.3e-5).
 """
 
 from __future__ import annotations
@@ -34,6 +39,8 @@ from test_oracle_param_golden import GOLD as PARAM_GOLD
 from test_oracle_param_golden import param_cases, param_dense_wfs, param_setup
 from test_oracle_prob_golden import GOLD as PROB_GOLD
 from test_oracle_prob_golden import check_distributions, check_expected, prob_cases, prob_setup
+from test_oracle_grad_golden import GOLD as GRAD_GOLD
+from test_oracle_grad_golden import grad_cases, grad_setup
 
 pytestmark = pytest.mark.gpu
 
@@ -148,3 +155,23 @@ def test_cuda_probabilistic_front_end_matches_reference_source(cuda, name):
     np.testing.assert_allclose(px.cpu().numpy(), pgold[f"{name}/pixel_x"], rtol=3e-7, atol=3e-6)
     np.testing.assert_allclose(py.cpu().numpy(), pgold[f"{name}/pixel_y"], rtol=3e-7, atol=3e-6)
     np.testing.assert_array_equal(event.cpu().numpy(), pgold[f"{name}/event"])
+
+
+@pytest.mark.parametrize("name", grad_cases())
+def test_cuda_gradient_matches_reference_central_differences(cuda, name):
+    from larndsim_gb300 import grad
+    ggold = np.load(GRAD_GOLD)
+    cfg, p, tmpl, tracks, fields = grad_setup(ggold, name)
+    chain = grad.LUTChain(p, torch.from_numpy(tmpl).cuda(), tracks, fields)
+    adc, ticks, pids = (t.cpu().numpy() for t in chain.adc(p))
+    ref_ticks = ggold[f"{name}/ticks32"]
+    accepted = ref_ticks < 1998                 # crossings the front end accepted
+    if not (np.array_equal(pids, ggold[f"{name}/pixels32"]) and np.array_equal(ticks[accepted], ref_ticks[accepted])):
+        pytest.skip("the GPU's float32 forward took another crossing decision than the reference's 32-bit run")
+    cot = torch.from_numpy(ggold[f"{name}/cotangent"].astype(np.float32)).cuda()
+    got = dict(zip(grad.GRAD_PARAMS, [float(v) for v in chain.vjp(p, cot)]))
+    for k, r in zip(cfg["grad_params"], ggold[f"{name}/fd_vjp"]):
+        if r == 0.0:
+            assert got[k] == 0.0, k
+        else:
+            assert abs(got[k] - r) <= 2e-4 * abs(r), (k, got[k], r)
