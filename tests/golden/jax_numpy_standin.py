@@ -514,7 +514,7 @@ def install(yaml_loads, x64=False):
     stats = _module("jax.scipy.stats", norm=_Norm())
     scipy_mod = _module("jax.scipy", special=special, stats=stats)
     nn = _module("jax.nn", sigmoid=_wrap_np(scipy.special.expit), softplus=lambda x: _x32(np.logaddexp(0, _arg(x))),
-                 logsumexp=_wrap_np(scipy.special.logsumexp))
+                 logsumexp=_wrap_np(scipy.special.logsumexp), softmax=_wrap_np(scipy.special.softmax))
     ops = _module("jax.ops", segment_sum=segment_sum)
     profiler = _module("jax.profiler", annotate_function=lambda f=None, **k: f if f is not None else _identity)
     debug = _module("jax.debug", print=lambda *a, **k: None)
@@ -522,7 +522,8 @@ def install(yaml_loads, x64=False):
     tree_util = _module("jax.tree_util")
     jax = _module("jax", numpy=jnp, lax=lax, random=random, scipy=scipy_mod, nn=nn, ops=ops, profiler=profiler,
                   debug=debug, experimental=experimental, tree_util=tree_util, jit=jit, vmap=vmap,
-                  checkpoint=lambda f=None, **k: f if f is not None else _identity, Array=np.ndarray)
+                  checkpoint=lambda f=None, **k: f if f is not None else _identity, Array=np.ndarray,
+                  named_scope=lambda name: _identity)
     struct = _module("flax.struct", field=struct_field, dataclass=struct_dataclass)
     flax = _module("flax", struct=struct)
 

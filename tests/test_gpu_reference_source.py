@@ -24,7 +24,10 @@ tolerances of tests/test_gpu_fee_prob.py.  The gradient
 differences of the reference's own chain in float64 at fixed decisions)
 is compared as the vector-Jacobian product for the reference's cotangent,
 within 2e-4 relative per component (the GPU-against-oracle bound of
-tests/test_gpu_grad.py, 1e-4, plus the oracle's observed 4.3e-5).
+tests/test_gpu_grad.py, 1e-4, plus the oracle's observed 4.3e-5).  The fit losses
+(tests/golden/loss_ref.npz, tests/golden/make_loss_golden.py) are compared
+at the tolerances of tests/test_gpu_losses.py: values within 1e-5
+relative, gradients within 1e-4 of the largest central difference.
 """
 
 from __future__ import annotations
@@ -41,6 +44,8 @@ from test_oracle_prob_golden import GOLD as PROB_GOLD
 from test_oracle_prob_golden import check_distributions, check_expected, prob_cases, prob_setup
 from test_oracle_grad_golden import GOLD as GRAD_GOLD
 from test_oracle_grad_golden import grad_cases, grad_setup
+from test_oracle_loss_golden import GOLD as LOSS_GOLD
+from test_oracle_loss_golden import COLS as LOSS_COLS
 
 pytestmark = pytest.mark.gpu
 
@@ -175,3 +180,23 @@ def test_cuda_gradient_matches_reference_central_differences(cuda, name):
             assert got[k] == 0.0, k
         else:
             assert abs(got[k] - r) <= 2e-4 * abs(r), (k, got[k], r)
+
+
+@pytest.mark.parametrize("name", ["mse_adc", "chamfer_3d", "nll_loss"])
+def test_cuda_losses_match_reference_source(cuda, name):
+    from larndsim_gb300 import consts, losses, sim
+    lgold = np.load(LOSS_GOLD)
+    pred = {k: torch.from_numpy(lgold[f"pred_{k}"]).cuda() for k in LOSS_COLS}
+    ref = {k: torch.from_numpy(lgold[f"ref_{k}"]).cuda() for k in LOSS_COLS}
+    wrt = ("Q", "z", "hit_prob") if name == "nll_loss" else ("Q", "z")
+    for k in wrt:
+        pred[k] = pred[k].clone().requires_grad_(True)
+    sim.reset_size_history()
+    loss, _ = getattr(losses, name)(consts.Params(), *[pred[k] for k in LOSS_COLS], *[ref[k] for k in LOSS_COLS])
+    loss.backward()
+    value = float(loss.detach())
+    assert abs(value - float(lgold[f"{name}/loss64"])) <= 1e-5 * abs(float(lgold[f"{name}/loss64"]))
+    for k in wrt:
+        fd = lgold[f"{name}/fd_{k}"]
+        g = pred[k].grad.cpu().numpy()[:fd.shape[0]]
+        assert np.abs(g - fd).max() <= 1e-4 * np.abs(fd).max(), k
