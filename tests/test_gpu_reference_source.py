@@ -70,7 +70,7 @@ def test_cuda_lut_path_matches_reference_source(cuda, gold, name):
     tmpl_gpu, _ = sim.load_lut(resp, p)
     got = tmpl_gpu.cpu().numpy().ravel()[gold[f"{name}/tmpl_index"]]
     ref = gold[f"{name}/tmpl_value"]
-    np.testing.assert_allclose(got, ref, rtol=2e-5, atol=2e-6 * np.abs(ref).max())
+    np.testing.assert_allclose(got, ref, rtol=2e-5, atol=2e-6 * float(tmpl_gpu.abs().max()))
 
     tmpl = torch.from_numpy(R.load_lut_templates(resp, p)).cuda()
     sim.reset_size_history()
@@ -157,9 +157,10 @@ def test_cuda_probabilistic_front_end_matches_reference_source(cuda, name):
     e_tick, e_adc, lam = (t.cpu().numpy() for t in sim.average_hit_values(p, w))
     check_expected(e_tick, e_adc, lam, pgold, name, rtol=1e-3)
     _, px, py, _, event = sim.simulate_probabilistic(p, w, torch.from_numpy(pixels).cuda())
-    np.testing.assert_allclose(px.cpu().numpy(), pgold[f"{name}/pixel_x"], rtol=3e-7, atol=3e-6)
-    np.testing.assert_allclose(py.cpu().numpy(), pgold[f"{name}/pixel_y"], rtol=3e-7, atol=3e-6)
-    np.testing.assert_array_equal(event.cpu().numpy(), pgold[f"{name}/event"])
+    real = pixels >= 0                      # the all-zero row carries pixel id -1
+    np.testing.assert_allclose(px.cpu().numpy()[real], pgold[f"{name}/pixel_x"][real], rtol=3e-7, atol=3e-6)
+    np.testing.assert_allclose(py.cpu().numpy()[real], pgold[f"{name}/pixel_y"][real], rtol=3e-7, atol=3e-6)
+    np.testing.assert_array_equal(event.cpu().numpy()[real], pgold[f"{name}/event"][real])
 
 
 @pytest.mark.parametrize("name", grad_cases())
