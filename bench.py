@@ -49,9 +49,9 @@ CPU_CHUNK = 150          # segments per CPU reference sample (one run per proces
 KERNELS_PER_STEP = 20   # stage 1: reset, segments, 3 scan, scatter, 2 sort; gradient: 3 template-order kernels,
                         # main records, heavy-pixel list, target index, pixels, main adjoint, 2 record reductions,
                         # target-only, finalize (counted in the launch list of the step)
-# DRAM bytes per simulated pixel of one k_lut_pixels<grad> launch, from the
-# ncu capture summarised in profiles/k_lut_pixels_grad_8events.md (8 events,
-# 22,066 pixels; traffic scales with the pixel count)
+# DRAM bytes per simulated pixel of one k_lut_pixels<grad> launch, from an
+# ncu capture of the 8-event case of this workload (22,066 pixels; traffic
+# scales with the pixel count)
 PIXEL_KERNEL_DRAM_BYTES_PER_PIXEL = 13968   # 308.2 MB over 22,066 pixels
 
 
@@ -293,8 +293,14 @@ def run_ours(args):
         "wall_s_timed": wall,
         "loss": float(out[0].item()), "grad_norm": float(out[1:].norm().item()),
     }
+    # ---- the plain forward drop-in on the same batch (after the timed region)
+    fwd, (wfs_f, unique_f) = lut_forward_record(args, params, tmpl, tracks, fields, dev, flush)
+    rec["forward"] = fwd
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rec["cpu_baseline"] = cpu_baseline(tracks, fields, params, pp, resp, sample_events=1)
+        # the oracle reads the template bank the GPU built (the builder itself is
+        # compared with the oracle's load_lut in the tests)
+        rec["parity"] = forward_parity(params, tmpl.cpu().numpy(), tracks, fields, wfs_f, unique_f)
     if rank == 0:
         print(json.dumps(rec), flush=True)
     if pg:
@@ -327,20 +333,83 @@ def _event_sample(tracks, fields, k, chunk=None):
     return out
 
 
-def _cpu_step(args_tuple):
-    """Oracle forward + FP64 loss and reverse-mode gradient of one sample."""
-    tmpl_path, tracks, fields, params, pp = args_tuple
-    from oracle import grad64, reference_np as R
+def _cpu_target(args_tuple):
+    """Target of one sample: the oracle's ADC grid at nominal parameters
+    (made once, outside the timed region, as the GPU step's target is)."""
+    tmpl_path, tracks, fields, params = args_tuple
+    from oracle import reference_np as R
     tmpl = np.load(tmpl_path, mmap_mode="r")
-    t0 = time.perf_counter()
     w, u = R.simulate_wfs(params, tmpl, tracks, fields, history={})
     o = R.simulate_stochastic(params, w, u)
     v = u >= 0
-    fr = grad64.Frozen(pp, tmpl, tracks, fields, u[v], o["grid_adcs"][v])
-    th = grad64.theta_dict(pp)
-    grad64.loss64(fr, th)
-    grad64.adjoint64(fr, th)
+    return u[v], o["grid_adcs"][v]
+
+
+def _cpu_step(args_tuple):
+    """One fwd+bwd of a sample in the reference's arithmetic type: the
+    float32 forward of the oracle (waveforms, front end, digitisation, with
+    the discrete decisions recorded), the SSE-ADC loss, and the reverse pass
+    in float32 down to the 8 parameters."""
+    tmpl_path, tracks, fields, pp, tgt_pids, tgt_adc = args_tuple
+    from oracle import grad64, reference_np as R
+    tmpl = np.load(tmpl_path, mmap_mode="r")
+    t0 = time.perf_counter()
+    fr = grad64.Frozen(pp, tmpl, tracks, fields, tgt_pids, tgt_adc)
+    adc = R.digitize(pp, fr.adc_f32[fr.valid])
+    resid = adc - fr.tgt.astype(np.float32)
+    float((resid * resid).sum(dtype=np.float32))
+    grad64.adjoint64(fr, grad64.theta_dict(pp), g_adc=(2 * resid).astype(np.float32), dtype=np.float32)
     return time.perf_counter() - t0, tracks.shape[0]
+
+
+def _cpu_jobs(path, sample, fields, params, pp, pool=None):
+    targets = (pool.map if pool else map)(_cpu_target, [(path, s, fields, params) for s in sample])
+    return [(path, s, fields, pp, tp, ta) for s, (tp, ta) in zip(sample, list(targets))]
+
+
+def forward_parity(params, tmpl, tracks, fields, wfs, unique, n_events=2):
+    """The oracle's forward on the smallest events of the batch against the
+    CUDA rows of the same events (events are independent): largest waveform
+    deviation relative to each row's scale, and the fraction of front-end
+    hit slots whose crossing tick differs (near-threshold crossings) with
+    the largest ADC deviation where the ticks agree."""
+    import torch
+    from larndsim_gb300 import sim
+    from oracle import reference_np as R
+    col = fields.index("eventID")
+    ev = tracks[:, col].astype(np.int64)
+    order = np.argsort(np.bincount(ev), kind="stable")[:n_events]
+    u = unique.cpu().numpy()
+    px, py, plane, pev = R.id2pixel(params, np.maximum(u, 0))
+    w_err = a_err = 0.0
+    slots = diff = segs = pixels = 0
+    for e in order:
+        sel = (u >= 0) & (pev == e)
+        rows = wfs.index_select(0, torch.from_numpy(np.nonzero(sel)[0]).to(wfs.device))
+        one = tracks[ev == e].copy()
+        one[:, col] = 0
+        wo, uo = R.simulate_wfs(params, tmpl, one, fields, history={})
+        v = uo >= 0
+        if not np.array_equal(R.pixel2id(params, px[sel], py[sel], plane[sel], 0), uo[v]):
+            return {"events": [int(x) for x in order], "unique_pixels_equal": False}
+        r_g = rows.cpu().numpy()
+        scale = np.abs(wo[v]).max(axis=1, keepdims=True)
+        w_err = max(w_err, float((np.abs(r_g - wo[v]) / np.where(scale > 0, scale, 1.0)).max()))
+        integral, ticks = sim.get_adc_values(params, rows)
+        adc_g, tick_g = R.digitize(params, integral.cpu().numpy()), ticks.cpu().numpy()
+        io, to = R.get_adc_values(params, wo[v])
+        adc_o = R.digitize(params, io)
+        same = np.cumprod(tick_g == to, axis=1).astype(bool)
+        slots += same.size
+        diff += int((~same).sum())
+        if same.any():
+            a_err = max(a_err, float((np.abs(adc_g - adc_o) / np.maximum(np.abs(adc_o), 1e-6))[same].max()))
+        segs += int(one.shape[0])
+        pixels += int(v.sum())
+    return {"events": [int(x) for x in order], "segments": segs, "pixels": pixels, "unique_pixels_equal": True,
+            "max_wfs_rel": w_err, "hit_slots": slots, "tick_mismatch_slots": diff,
+            "tick_mismatch_frac": diff / max(slots, 1), "max_adc_rel_where_ticks_agree": a_err,
+            "tolerance": "waveforms 1e-5 of the row scale; ADC 1e-5 relative where the crossing tick agrees"}
 
 
 def cpu_baseline(tracks, fields, params, pp, resp, sample_events=2, processes=1):
@@ -351,7 +420,7 @@ def cpu_baseline(tracks, fields, params, pp, resp, sample_events=2, processes=1)
     np.save(path, tmpl)
     del tmpl
     sample = _event_sample(tracks, fields, sample_events)
-    jobs = [(path, s, fields, params, pp) for s in sample]
+    jobs = _cpu_jobs(path, sample, fields, params, pp)
     t0 = time.perf_counter()
     if processes > 1:
         import multiprocessing as mp
@@ -364,8 +433,8 @@ def cpu_baseline(tracks, fields, params, pp, resp, sample_events=2, processes=1)
     segs = sum(r[1] for r in res)
     return {"value": segs / wall, "unit": UNIT, "cores": processes, "kind": "port",
             "sample": f"{len(sample)} smallest events ({segs} segments): numpy float32 forward "
-                      f"(simulate_wfs + simulate_stochastic restatement) + FP64 frozen-decision loss "
-                      f"and its reverse-mode gradient in the 8 parameters, {wall:.1f} s"}
+                      f"(waveforms, front end, digitisation) + SSE-ADC loss and its float32 reverse-mode "
+                      f"gradient in the 8 parameters, {wall:.1f} s; target made outside the timing"}
 
 
 def run_reference(args):
@@ -386,9 +455,9 @@ def run_reference(args):
     np.save(path, tmpl)
     del tmpl
     sample = _event_sample(tracks, fields, procs, chunk=CPU_CHUNK)
-    jobs = [(path, s, fields, params, pp) for s in sample]
     times = []
     with mp.get_context("spawn").Pool(procs) as pool:
+        jobs = _cpu_jobs(path, sample, fields, params, pp, pool)
         for i in range(args.warmup + args.steps):
             t0 = time.perf_counter()
             res = pool.map(_cpu_step, jobs)
@@ -408,9 +477,10 @@ def run_reference(args):
                       "segments_per_step": segs, "samples_per_step": len(sample)},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
                             "sample": f"{len(sample)} runs of {CPU_CHUNK} consecutive segments of the smallest "
-                                      f"events, {segs} segments per step, one process per run: float32 numpy "
-                                      "restatement forward + FP64 frozen-decision loss and reverse-mode "
-                                      "gradient in the 8 parameters"},
+                                      f"events, {segs} segments per step, one process per run: numpy "
+                                      "restatement, float32 forward (waveforms, front end, digitisation) + "
+                                      "SSE-ADC loss + float32 reverse-mode gradient in the 8 parameters "
+                                      "(the reference's arithmetic type); targets made outside the timing"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(rec), flush=True)
 
@@ -630,6 +700,73 @@ def _timed(step, steps, warmup, flush):
     return float(np.mean([a.elapsed_time(b) for a, b in zip(starts, ends)])), clk
 
 
+def lut_forward_record(args, params, tmpl, tracks, fields, dev, flush):
+    """The plain LUT-mode forward drop-in, simulate_wfs + simulate_stochastic
+    (sim_jax.py:689-769), through the public functions with the reference's
+    device-to-host synchronisation points: device-resident ms per step,
+    e2e from pinned host tracks to host hits, and the roofline of the
+    waveform kernel k_lut_pixels<wfs> (CUDA events around its launch)
+    against the fixed forward formula.  Returns the record and the last
+    step's (wfs, unique)."""
+    import torch
+    from larndsim_gb300 import _abi, grad, sim
+    n_seg = tracks.shape[0]
+    t_dev = torch.from_numpy(tracks).to(dev)
+
+    def step(tr=t_dev):
+        wfs, unique = sim.simulate_wfs(params, tmpl, tr, fields)
+        return sim.simulate_stochastic(params, wfs, unique), wfs, unique
+
+    ms, clk = _timed(step, args.steps, args.warmup, flush)
+    rec = {"metric": "forward segments/s", "value": n_seg / (ms * 1e-3), "unit": "segments/s",
+           "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup,
+           "workload": f"simulate_wfs + simulate_stochastic (n_neighbors=4, L=150, 100x45x45x1950 templates) on "
+                       f"the same batch ({n_seg} segments), noise off",
+           "step": "public functions, eager, with the reference's device-to-host syncs; L2 flushed between "
+                   "timed steps (512 MiB write)",
+           "clocks": clk}
+    host = torch.from_numpy(tracks).pin_memory()
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(e2e_steps):
+        out = step(host.to(dev, non_blocking=True))[0]
+        cpu = [o.cpu() for o in out]
+        d2h = sum(c.numel() * 4 for c in cpu)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    rec["e2e"] = {"value": n_seg / e2e_s, "unit": "segments/s", "ms_per_step": e2e_s * 1e3,
+                  "h2d_bytes_per_step": int(tracks.nbytes), "d2h_bytes_per_step": int(d2h)}
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+    for e in kev:
+        flush.fill_(1.0)
+        _abi.set_kernel_events(*e)
+        _, wfs, unique = step()
+    torch.cuda.synchronize()
+    _abi.set_kernel_events(None, None)
+    k_ms = float(np.mean([a.elapsed_time(b) for a, b in kev]))
+    n_valid = int((unique >= 0).sum())
+    T = wfs.shape[1]
+    # the waveform kernel's share of the fixed forward formula: the rows it
+    # writes (4 T P), their pixel ids (8 P) and the distinct LUT floats
+    chain = grad.LUTChain(params, tmpl, tracks, fields)
+    st = chain.stage1(params)
+    seg_rec = st.ws[256:256 + 96 * n_seg].view(torch.int32).view(n_seg, 24).cpu().numpy()
+    ne = seg_rec[:, 0].view(np.float32)
+    lut = chain.lut
+    w_lut = lut_bytes_touched(seg_rec[ne > 0, 6], lut.n_templates, lut.shape[1], lut.shape[2], SIG_LEN,
+                              lut.shape[3])
+    algo = 4 * T * n_valid + 8 * n_valid + 4 * w_lut
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = algo / (k_ms * 1e-3) / 1e9
+    rec["roofline"] = {"bound": "hbm", "kernel": "k_lut_pixels<wfs> (pixel-major waveform accumulation)",
+                       "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                       "algorithmic_bytes": int(algo), "kernel_ms": k_ms, "pixels": n_valid,
+                       "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None}
+    return rec, (wfs, unique)
+
+
 def run_forward(args, param_mode=False):
     """The plain forward drop-in on the 64-event batch: simulate_wfs +
     simulate_stochastic (sim_jax.py:689-769), or simulate_parametrized
@@ -638,7 +775,7 @@ def run_forward(args, param_mode=False):
     synchronisation points.  LUT mode also reports the roofline of the
     waveform kernel k_lut_pixels<wfs> (CUDA events around its launch)."""
     import torch
-    from larndsim_gb300 import _abi, sim, workloads
+    from larndsim_gb300 import sim, workloads
     rank, world, local = dist_env()
     if rank != 0:
         return
@@ -646,76 +783,46 @@ def run_forward(args, param_mode=False):
     dev = torch.device("cuda", local)
     tracks, fields = workload(0, args.seed)
     n_seg = tracks.shape[0]
-    t_dev = torch.from_numpy(tracks).to(dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    if param_mode:
-        params = nominal_params().replace(number_pix_neighbors=0, mc_diff=True)
-        offsets = sim.draw_offsets(n_seg, 7, dev)
-
-        def step(tr=t_dev, off=offsets):
-            return sim.simulate_parametrized(params, tr, fields, offsets=off)
-    else:
+    base = {"metric": "forward segments/s", "unit": "segments/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded tracks and LUT)"}
+    if not param_mode:
         params = nominal_params()
         tmpl, params = sim.load_lut(workloads.synthetic_response(seed=0), params)
+        fwd, _ = lut_forward_record(args, params, tmpl, tracks, fields, dev, flush)
+        rec = dict(base, value=fwd["value"], ms_per_step=fwd["ms_per_step"],
+                   config={"workload": fwd["workload"], "segments": n_seg,
+                           "l2": "flushed between timed steps (512 MiB write)", "step": fwd["step"]},
+                   clocks=fwd["clocks"], e2e=fwd["e2e"], roofline=fwd["roofline"], gpu_launches=None)
+        print(json.dumps(rec), flush=True)
+        return
+    t_dev = torch.from_numpy(tracks).to(dev)
+    params = nominal_params().replace(number_pix_neighbors=0, mc_diff=True)
+    offsets = sim.draw_offsets(n_seg, 7, dev)
 
-        def step(tr=t_dev):
-            wfs, unique = sim.simulate_wfs(params, tmpl, tr, fields)
-            return sim.simulate_stochastic(params, wfs, unique), wfs, unique
+    def step(tr=t_dev, off=offsets):
+        return sim.simulate_parametrized(params, tr, fields, offsets=off)
+
     ms, clk = _timed(step, args.steps, args.warmup, flush)
-    rec = {"metric": "forward segments/s", "value": n_seg / (ms * 1e-3), "unit": "segments/s", "n_gpus": 1,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tracks and LUT)",
-           "config": {"workload": ("simulate_parametrized (n_neighbors=0, mc_diff offsets supplied)" if param_mode
-                                   else "simulate_wfs + simulate_stochastic (n_neighbors=4, L=150, "
-                                        "100x45x45x1950 templates)") +
-                                  f" on the 64-event batch ({n_seg} segments), noise off",
-                      "segments": n_seg, "l2": "flushed between timed steps (512 MiB write)",
-                      "step": "public functions, eager, with the reference's device-to-host syncs"},
-           "clocks": clk}
+    rec = dict(base, value=n_seg / (ms * 1e-3), ms_per_step=ms,
+               config={"workload": f"simulate_parametrized (n_neighbors=0, mc_diff offsets supplied) on the "
+                                   f"64-event batch ({n_seg} segments), noise off",
+                       "segments": n_seg, "l2": "flushed between timed steps (512 MiB write)",
+                       "step": "public functions, eager, with the reference's device-to-host syncs"},
+               clocks=clk)
     host = torch.from_numpy(tracks).pin_memory()
     e2e_steps = max(3, min(args.steps, 10))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     d2h = 0
     for _ in range(e2e_steps):
-        if param_mode:
-            out = step(host.to(dev, non_blocking=True), offsets)
-        else:
-            out = step(host.to(dev, non_blocking=True))[0]
+        out = step(host.to(dev, non_blocking=True), offsets)
         cpu = [o.cpu() for o in out]
         d2h = sum(c.numel() * 4 for c in cpu)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     rec["e2e"] = {"value": n_seg / e2e_s, "unit": "segments/s", "ms_per_step": e2e_s * 1e3,
                   "h2d_bytes_per_step": int(tracks.nbytes), "d2h_bytes_per_step": int(d2h)}
-    if not param_mode:
-        kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
-        for e in kev:
-            flush.fill_(1.0)
-            _abi.set_kernel_events(*e)
-            _, wfs, unique = step()
-        torch.cuda.synchronize()
-        _abi.set_kernel_events(None, None)
-        k_ms = float(np.mean([a.elapsed_time(b) for a, b in kev]))
-        n_valid = int((unique >= 0).sum())
-        T = wfs.shape[1]
-        # the waveform kernel's share of the fixed forward formula: the rows it
-        # writes (4 T P), their pixel ids (8 P) and the distinct LUT floats
-        from larndsim_gb300 import grad
-        chain = grad.LUTChain(params, tmpl, tracks, fields)
-        st = chain.stage1(params)
-        seg_rec = st.ws[256:256 + 96 * n_seg].view(torch.int32).view(n_seg, 24).cpu().numpy()
-        ne = seg_rec[:, 0].view(np.float32)
-        lut = chain.lut
-        w_lut = lut_bytes_touched(seg_rec[ne > 0, 6], lut.n_templates, lut.shape[1], lut.shape[2], SIG_LEN,
-                                  lut.shape[3])
-        algo = 4 * T * n_valid + 8 * n_valid + 4 * w_lut
-        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-        peak = peaks.get("hbm_gbs", 6800.0)
-        achieved = algo / (k_ms * 1e-3) / 1e9
-        rec["roofline"] = {"bound": "hbm", "kernel": "k_lut_pixels<wfs> (pixel-major waveform accumulation)",
-                           "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                           "algorithmic_bytes": int(algo), "kernel_ms": k_ms, "pixels": n_valid,
-                           "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None}
     rec["gpu_launches"] = None
     print(json.dumps(rec), flush=True)
 
@@ -894,8 +1001,7 @@ def run_chop_reference(args):
 
 RECORDS_HITS, RECORDS_EVENTS, RECORDS_CPU_HITS = 32_000_000, 1000, 4_000_000
 # DRAM bytes per input hit of one lsim_hit_records call (three kernels), from
-# the ncu launch list summarised in profiles/hit_records_8M_hits.md (575.3 MB
-# over 8M hits; traffic scales with the hits)
+# an ncu capture of an 8M-hit case (575.3 MB; traffic scales with the hits)
 RECORDS_DRAM_BYTES_PER_HIT = 575_320_064 / 8_000_000
 
 

@@ -286,16 +286,25 @@ int lsim_hits(const LsimParams *p, const float *adc, const float *ticks, const i
  * process can fail), or code running under a fixed device-memory budget.
  * No counterpart in the reference (larnd-sim-jax allocates through XLA).
  * Instead of a workspace it uses a fixed scratch array compiled into the
- * library (64 KiB, held on every device that loads the library until the
- * process exits), so it accepts at most 16384 * 1024 = 16,777,216 hit
- * slots (n_pix * max_adc_values) and returns LSIM_ERR_CAPACITY beyond that.
- * It calls no cudaMalloc/cudaFree.  The first call on each device looks up
- * the scratch's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  Every call on a
- * device shares the one scratch array: calls that overlap on the GPU (for
- * example on two streams) race and must be serialised by the caller.  The
- * scratch needs no clearing between calls: every entry a call reads is
- * written by the same call first. */
+ * library (64 KiB), so it accepts at most lsim_hits_noalloc_max_slots() =
+ * 16384 * 1024 = 16,777,216 hit slots (n_pix * max_adc_values) and returns
+ * LSIM_ERR_CAPACITY beyond that (max_adc_values outside 1..LSIM_MAX_HITS is
+ * LSIM_ERR_INVALID).  It calls no cudaMalloc/cudaFree.
+ * The scratch is reserved in a CUDA context when this library's module is
+ * loaded there: under CUDA's default lazy module loading that is the first
+ * call of lsim_fee, lsim_hits or lsim_hits_noalloc in the context, so a
+ * process that will later give all free memory to another allocator should
+ * make one such call first (or run with CUDA_MODULE_LOADING=EAGER).  The
+ * first call in each context (the device's primary context, a context made
+ * with cuCtxCreate, or a primary context re-created after cudaDeviceReset)
+ * looks up the scratch's device address (cudaGetSymbolAddress) with that
+ * context current and caches it by the context's id; make that first call
+ * before any stream capture.  Every call in a context shares the one
+ * scratch array: calls that overlap on the GPU (for example on two streams)
+ * race and must be serialised by the caller.  The scratch needs no clearing
+ * between calls: every entry a call reads is written by the same call
+ * first. */
+int64_t lsim_hits_noalloc_max_slots(void);
 int lsim_hits_noalloc(const LsimParams *p, const float *adc, const float *ticks, const int32_t *unique_pixels,
                       int64_t n_pix, int32_t tick_limit, float *out_adc, float *out_x, float *out_y,
                       float *out_z, float *out_ticks, float *out_hit_prob, int32_t *out_event,

@@ -554,6 +554,11 @@ int lsim_hits(const LsimParams *p, const float *adc, const float *ticks, const i
   if (!nb_valid_dev || (n_pix > 0 && (!adc || !ticks || !unique_pixels || !out_adc || !out_x || !out_y || !out_z ||
                                       !out_ticks || !out_hit_prob || !out_event || !out_pixels || !ws)))
     return fail(LSIM_ERR_INVALID, "lsim_hits: null pointer");
+  if (n_pix < 0) return fail(LSIM_ERR_INVALID, "lsim_hits: negative pixel count");
+  if (p->max_adc_values < 1 || p->max_adc_values > LSIM_MAX_HITS)
+    return fail(LSIM_ERR_INVALID, "lsim_hits: max_adc_values outside 1..LSIM_MAX_HITS");
+  // the kept count and the hit slots are indexed in int32
+  if (n_pix > INT32_MAX / p->max_adc_values) return fail(LSIM_ERR_CAPACITY, "lsim_hits: more than 2^31 - 1 hit slots");
   if (ws_bytes < hits_ws_bytes(n_pix * (int64_t)p->max_adc_values))
     return fail(LSIM_ERR_CAPACITY, "lsim_hits: workspace too small");
   return wrap(run_hits(*p, adc, ticks, unique_pixels, n_pix, tick_limit, out_adc, out_x, out_y, out_z, out_ticks,

@@ -6,6 +6,8 @@
 // current_mc / current_model_diff / integrated_expon_diff / emg_pdf
 // (detsim_jax.py:440-474, :581-639) and accumulate_signals_parametrized
 // (detsim_jax.py:207-228).
+#include <cuda.h>
+
 #include <cstdio>
 #include <mutex>
 
@@ -154,15 +156,27 @@ __global__ void k_hits_count(LsimParams p, const float *ticks, const int32_t *un
   }
 }
 
-__global__ void k_hits_scan(int32_t *block_counts, int64_t nblocks, int32_t *total) {
-  if (threadIdx.x != 0) return;
-  int run = 0;
-  for (int64_t b = 0; b < nblocks; ++b) {
-    const int c = block_counts[b];
-    block_counts[b] = run;
-    run += c;
+// Exclusive scan of the per-tile kept counts, one CTA of kHitsScanThreads:
+// each thread owns a contiguous run of tiles (scanned serially in
+// registers), the run totals are scanned across the block, and each thread
+// writes its run's offsets.  *total gets the kept count.
+constexpr int kHitsScanThreads = 1024;
+__global__ void __launch_bounds__(kHitsScanThreads) k_hits_scan(int32_t *block_counts, int64_t nblocks,
+                                                                 int32_t *total) {
+  __shared__ int64_t warp_tot[kHitsScanThreads / kWarp];
+  __shared__ int64_t all;
+  const int64_t per = (nblocks + kHitsScanThreads - 1) / kHitsScanThreads;
+  const int64_t lo = min(nblocks, (int64_t)threadIdx.x * per), hi = min(nblocks, lo + per);
+  int64_t run = 0;
+  for (int64_t b = lo; b < hi; ++b) run += block_counts[b];
+  const int64_t incl = block_scan_i64(run, warp_tot, &all);
+  int64_t off = incl - run;
+  for (int64_t b = lo; b < hi; ++b) {
+    const int32_t c = block_counts[b];
+    block_counts[b] = (int32_t)off;
+    off += c;
   }
-  *total = run;
+  if (threadIdx.x == 0) *total = (int32_t)all;
 }
 
 // Row-major compaction (parse_output) with the coordinates of
@@ -237,7 +251,7 @@ int run_hits(const LsimParams &p, const float *adc, const float *ticks, const in
   int32_t *blocks = (int32_t *)ws;
   if (n == 0) return cudaMemsetAsync(nb_valid_dev, 0, 4, st) == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
   k_hits_count<<<(unsigned)nb, kHitTile, 0, st>>>(p, ticks, unique_pixels, n, H, tick_limit, blocks);
-  k_hits_scan<<<1, 32, 0, st>>>(blocks, nb, nb_valid_dev);
+  k_hits_scan<<<1, kHitsScanThreads, 0, st>>>(blocks, nb, nb_valid_dev);
   k_hits_write<<<(unsigned)nb, kHitTile, 0, st>>>(p, adc, ticks, unique_pixels, n, H, tick_limit, blocks, out_adc,
                                                   out_x, out_y, out_z, out_ticks, out_hit_prob, out_event, out_pixels);
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
@@ -246,28 +260,71 @@ int run_hits(const LsimParams &p, const float *adc, const float *ticks, const in
 // ---------------------------------------------------------------- hits without allocation
 
 // Fixed scratch for lsim_hits_noalloc: one int per 1024 hit slots (the
-// per-tile counts of the two-pass compaction).  64 KiB, resident on every
-// device that loads the library until the process exits.
+// per-tile counts of the two-pass compaction).  64 KiB per CUDA context that
+// loads this module (with lazy module loading: on the first use of any kernel
+// of this file in that context), held until the context is destroyed.
 constexpr int64_t kHitsStaticTiles = 16384;
 static __device__ __align__(256) int32_t g_hits_static_scratch[kHitsStaticTiles];
 
-constexpr int kMaxDevices = 64;
+// The array's device address belongs to the module as loaded in one CUDA
+// context, so the lookup is cached per context, keyed by the context's
+// process-unique id (cuCtxGetId): a context made with cuCtxCreate, or the
+// primary context re-created after cudaDeviceReset, gets its own lookup.
+// The two driver calls are fetched through the runtime, so the library does
+// not link libcuda itself.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+constexpr int kMaxContexts = 64;
 static std::mutex g_hits_static_mu;
-static int32_t *g_hits_static_ptr[kMaxDevices] = {};
+static unsigned long long g_hits_ctx_id[kMaxContexts] = {};
+static int32_t *g_hits_ctx_ptr[kMaxContexts] = {};
+static int g_hits_ctx_n = 0;
 
-// Device address of g_hits_static_scratch on the current device, looked up
-// once per device (cudaGetSymbolAddress with that device current).
-static int hits_static_scratch(int32_t **out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return LSIM_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxDevices) return LSIM_ERR_UNSUPPORTED;
-  std::lock_guard<std::mutex> lock(g_hits_static_mu);
-  if (!g_hits_static_ptr[dev]) {
-    void *ptr = nullptr;
-    if (cudaGetSymbolAddress(&ptr, g_hits_static_scratch) != cudaSuccess || !ptr) return LSIM_ERR_CUDA;
-    g_hits_static_ptr[dev] = (int32_t *)ptr;
+static int current_context_id(unsigned long long *id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+    void *f1 = nullptr, *f2 = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return LSIM_ERR_CUDA;
+    get_current = (CtxGetCurrentFn)f1;
+    get_id = (CtxGetIdFn)f2;
   }
-  *out = g_hits_static_ptr[dev];
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS) return LSIM_ERR_CUDA;
+  if (!ctx) {
+    // no context current yet on this thread: make the current device's
+    // primary context current, as the runtime's first call would
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaSetDevice(dev) != cudaSuccess) return LSIM_ERR_CUDA;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return LSIM_ERR_CUDA;
+  }
+  return get_id(ctx, id) == CUDA_SUCCESS ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
+// Device address of g_hits_static_scratch in the current context: looked
+// up once per context (cudaGetSymbolAddress with that context current).
+static int hits_static_scratch(int32_t **out) {
+  unsigned long long id = 0;
+  std::lock_guard<std::mutex> lock(g_hits_static_mu);
+  if (current_context_id(&id) != LSIM_OK) return LSIM_ERR_CUDA;
+  for (int i = 0; i < g_hits_ctx_n; ++i)
+    if (g_hits_ctx_id[i] == id) {
+      *out = g_hits_ctx_ptr[i];
+      return LSIM_OK;
+    }
+  void *ptr = nullptr;
+  if (cudaGetSymbolAddress(&ptr, g_hits_static_scratch) != cudaSuccess || !ptr) return LSIM_ERR_CUDA;
+  // a full table starts over (a process that made more than kMaxContexts
+  // contexts); entries are only a cache of the lookup
+  if (g_hits_ctx_n == kMaxContexts) g_hits_ctx_n = 0;
+  g_hits_ctx_id[g_hits_ctx_n] = id;
+  g_hits_ctx_ptr[g_hits_ctx_n] = (int32_t *)ptr;
+  ++g_hits_ctx_n;
+  *out = (int32_t *)ptr;
   return LSIM_OK;
 }
 
@@ -569,6 +626,8 @@ int run_param_accum(const LsimParams &p, const Workspace &w, const Grid &g, int3
 
 }  // namespace lsim
 
+extern "C" int64_t lsim_hits_noalloc_max_slots(void) { return lsim::kHitsStaticTiles * (int64_t)lsim::kHitTile; }
+
 extern "C" int lsim_hits_noalloc(const LsimParams *p, const float *adc, const float *ticks,
                                  const int32_t *unique_pixels, int64_t n_pix, int32_t tick_limit, float *out_adc,
                                  float *out_x, float *out_y, float *out_z, float *out_ticks, float *out_hit_prob,
@@ -580,13 +639,17 @@ extern "C" int lsim_hits_noalloc(const LsimParams *p, const float *adc, const fl
                                       !out_ticks || !out_hit_prob || !out_event || !out_pixels)))
     return set_error(LSIM_ERR_INVALID, "lsim_hits_noalloc: null pointer");
   if (n_pix < 0) return set_error(LSIM_ERR_INVALID, "lsim_hits_noalloc: negative pixel count");
-  const int64_t slots = n_pix * (int64_t)p->max_adc_values;
-  if (slots > kHitsStaticTiles * (int64_t)kHitTile) {
+  if (p->max_adc_values < 1 || p->max_adc_values > LSIM_MAX_HITS)
+    return set_error(LSIM_ERR_INVALID, "lsim_hits_noalloc: max_adc_values outside 1..LSIM_MAX_HITS");
+  // compare before multiplying, so a huge pixel count cannot wrap past the limit
+  const int64_t max_slots = kHitsStaticTiles * (int64_t)kHitTile;
+  const int64_t slots = n_pix > max_slots / p->max_adc_values ? max_slots + 1 : n_pix * (int64_t)p->max_adc_values;
+  if (slots > max_slots) {
     char msg[256];
     snprintf(msg, sizeof(msg),
              "lsim_hits_noalloc: %lld hit slots (%lld pixels x %d hits) exceed the fixed scratch limit of %lld "
              "slots; use lsim_hits with a caller-allocated workspace",
-             (long long)slots, (long long)n_pix, p->max_adc_values, (long long)(kHitsStaticTiles * kHitTile));
+             (long long)n_pix * p->max_adc_values, (long long)n_pix, p->max_adc_values, (long long)max_slots);
     return set_error(LSIM_ERR_CAPACITY, msg);
   }
   int32_t *scratch = nullptr;

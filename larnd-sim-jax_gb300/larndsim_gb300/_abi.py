@@ -100,6 +100,7 @@ _SIGNATURES = {
     "lsim_hits_workspace_bytes": (_sz, [_i64, _i32]),
     "lsim_hits": (C.c_int, [_PP, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz,
                             _vp]),
+    "lsim_hits_noalloc_max_slots": (_i64, []),
     "lsim_hits_noalloc": (C.c_int, [_PP, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                     _vp]),
     "lsim_pixel_coords": (C.c_int, [_PP, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),

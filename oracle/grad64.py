@@ -268,21 +268,24 @@ def adc64(fr: Frozen, th: dict):
     return fee64(fr, waveforms64(fr, th))
 
 
-def fee_adjoint64(fr: Frozen, g_adc):
-    """dL/dW for a cotangent on the ADC grid (frozen FEE, reverse mode)."""
+def fee_adjoint64(fr: Frozen, g_adc, dtype=np.float64):
+    """dL/dW for a cotangent on the ADC grid (frozen FEE, reverse mode), in
+    ``dtype`` (float64 by default; float32 is the reference's own type)."""
     p = fr.params
+    ft = np.dtype(dtype)
     P, H = g_adc.shape
     T = fr.masks.shape[2]
     rows = np.arange(P)
-    gint = np.where(fr.dig_lin, g_adc * p.GAIN * p.ADC_COUNTS / (p.V_REF - p.V_CM), 0.0)
-    g = np.zeros((P, T))
+    gint = np.where(fr.dig_lin, np.asarray(g_adc, ft) * ft.type(p.GAIN * p.ADC_COUNTS / (p.V_REF - p.V_CM)),
+                    ft.type(0)).astype(ft)
+    g = np.zeros((P, T), ft)
     for h in range(H - 1, -1, -1):
         m = fr.masks[h]
         S = (g * m).sum(axis=1)
         g = np.where(m, g, 0.0)
         np.add.at(g, (rows, fr.e2[:, h]), -S)
-        np.add.at(g, (rows, fr.e[:, h]), np.where(fr.cond[:, h], 0.0, gint[:, h]))
-    return np.cumsum(g[:, ::-1], axis=1)[:, ::-1] * p.t_sampling
+        np.add.at(g, (rows, fr.e[:, h]), np.where(fr.cond[:, h], ft.type(0), gint[:, h]))
+    return (np.cumsum(g[:, ::-1], axis=1, dtype=ft)[:, ::-1] * ft.type(p.t_sampling)).astype(ft)
 
 
 def loss_cotangent(fr: Frozen, th: dict):
@@ -338,39 +341,44 @@ def _jacobian(fr: Frozen, th0: dict, h=1e-30):
     return J
 
 
-def adjoint64(fr: Frozen, th: dict, g_adc=None):
+def adjoint64(fr: Frozen, th: dict, g_adc=None, dtype=np.float64):
     """Reverse-mode gradient (same chain rule as the CUDA adjoint, in
     float64): FEE adjoint -> waveform cotangent -> per-contribution partials
     (charge, transverse weights, template weights, sub-tick fraction) ->
     per-segment partials -> parameters.  Without ``g_adc`` the cotangent is
     that of loss64; with ``g_adc`` (valid rows x H) it is the vector-Jacobian
-    product g_adc . dADC/dtheta."""
+    product g_adc . dADC/dtheta.  With ``dtype=np.float32`` (and ``g_adc``
+    given) the reverse pass runs in float32, the reference's own arithmetic
+    type; the per-segment Jacobian and the final parameter sums stay
+    float64."""
     p = fr.params
     d = fr.d
-    ne, sigT, ld, t0 = segment_quantities(fr, th)
+    ft = np.dtype(dtype)
+    ne, sigT, ld, t0 = (q.astype(ft) for q in segment_quantities(fr, th))
     if g_adc is None:
         gw = loss_cotangent(fr, th)
     else:
-        g = np.zeros((fr.unique.shape[0], int(p.MAX_ADC_VALUES)))
+        g = np.zeros((fr.unique.shape[0], int(p.MAX_ADC_VALUES)), ft)
         g[fr.valid] = g_adc
-        gw = fee_adjoint64(fr, g)
+        gw = fee_adjoint64(fr, g, ft)
     P = gw.shape[0]
     Nticks = R.n_ticks(p)
-    gwc = np.zeros((P, Nticks))
+    gwc = np.zeros((P, Nticks), ft)
     gwc[:, 1:] = gw
     Tb = fr.T
     Ntemp, Nx, Ny, Nt = Tb.shape
     L = int(p.signal_length)
     S = ne.shape[0]
     rows = np.arange(S)
-    ex = _weights(fr.edges, fr.x0, sigT)
-    ey = _weights(fr.edges, fr.y0, sigT)
-    hs = 1e-30 * np.maximum(sigT, 1e-300)
-    dex = _weights(fr.edges, fr.x0, sigT + 1j * hs).imag / hs[:, None]
-    dey = _weights(fr.edges, fr.y0, sigT + 1j * hs).imag / hs[:, None]
-    frac = t0 / p.t_sampling - fr.cath
+    s64 = sigT.astype(np.float64)
+    ex = _weights(fr.edges, fr.x0, s64).astype(ft)
+    ey = _weights(fr.edges, fr.y0, s64).astype(ft)
+    hs = 1e-30 * np.maximum(s64, 1e-300)
+    dex = (_weights(fr.edges, fr.x0, s64 + 1j * hs).imag / hs[:, None]).astype(ft)
+    dey = (_weights(fr.edges, fr.y0, s64 + 1j * hs).imag / hs[:, None]).astype(ft)
+    frac = (t0 / ft.type(p.t_sampling) - fr.cath.astype(ft)).astype(ft)
     i = fr.tidx
-    x0, x1, x2 = fr.tmpl[i - 1], fr.tmpl[i], fr.tmpl[i + 1]
+    x0, x1, x2 = (fr.tmpl[j].astype(ft) for j in (i - 1, i, i + 1))
     a = (ld - x1) * (ld - x2) / ((x0 - x1) * (x0 - x2))
     b = (ld - x0) * (ld - x2) / ((x1 - x0) * (x1 - x2))
     c = (ld - x0) * (ld - x1) / ((x2 - x0) * (x2 - x1))
@@ -385,12 +393,12 @@ def adjoint64(fr: Frozen, th: dict, g_adc=None):
     col1 = np.where((tt1 <= 0) | (tt1 >= Nticks - 1), 0, tt1 + 1)
     cc0 = np.where((st0 <= 0) | (st0 >= Nticks - 1), 0, st0)
     cc1 = np.where((st0 - 1 <= 0) | (st0 - 1 >= Nticks - 1), 0, st0 - 1)
-    A_ne = np.zeros(S)
-    A_sig = np.zeros(S)
-    A_a = np.zeros(S)
-    A_b = np.zeros(S)
-    A_c = np.zeros(S)
-    A_fr = np.zeros(S)
+    A_ne = np.zeros(S, ft)
+    A_sig = np.zeros(S, ft)
+    A_a = np.zeros(S, ft)
+    A_b = np.zeros(S, ft)
+    A_c = np.zeros(S, ft)
+    A_fr = np.zeros(S, ft)
 
     def renum(pids, neigh):
         r = np.searchsorted(fr.unique, pids)
@@ -402,7 +410,7 @@ def adjoint64(fr: Frozen, th: dict, g_adc=None):
         ok = r >= 0
         rr = np.where(ok, r, 0)
         g = gwc[rr[:, None], cols] if cols.ndim == 2 else gwc[rr, cols]
-        return np.where(ok[:, None] if cols.ndim == 2 else ok, g, 0.0)
+        return np.where(ok[:, None] if cols.ndim == 2 else ok, g, ft.type(0))
 
     ci = d["currents_idx"].reshape(S, 25, 2)
     pix = d["pixels"].reshape(S, 25)
@@ -410,14 +418,14 @@ def adjoint64(fr: Frozen, th: dict, g_adc=None):
     dwts = (dex[:, :, None] * ey[:, None, :] + ex[:, :, None] * dey[:, None, :]).reshape(S, 25)
     for k in range(25):
         r = renum(pix[:, k], False)
-        vi = Tb[i, ci[:, k, 0], ci[:, k, 1], Nt - L:].astype(np.float64)
-        vm = Tb[i - 1, ci[:, k, 0], ci[:, k, 1], Nt - L:].astype(np.float64)
-        vp = Tb[i + 1, ci[:, k, 0], ci[:, k, 1], Nt - L:].astype(np.float64)
+        vi = Tb[i, ci[:, k, 0], ci[:, k, 1], Nt - L:].astype(ft)
+        vm = Tb[i - 1, ci[:, k, 0], ci[:, k, 1], Nt - L:].astype(ft)
+        vp = Tb[i + 1, ci[:, k, 0], ci[:, k, 1], Nt - L:].astype(ft)
         B = vi * b[:, None] + vm * a[:, None] + vp * c[:, None]
         q = wts[:, k] * ne
         G0, G1 = gather(r, col0), gather(r, col1)
         gv = G0 * (1 - frac)[:, None] + G1 * frac[:, None]
-        cum = np.cumsum(Tb[i, ci[:, k, 0], ci[:, k, 1], :], axis=-1, dtype=np.float64)
+        cum = np.cumsum(Tb[i, ci[:, k, 0], ci[:, k, 1], :], axis=-1, dtype=ft)
         c0v, c1v = cum[rows, fr.cath], cum[rows, np.minimum(fr.cath + 1, Nt - 1)]
         D = cum[rows, Nt - L] - (c0v * (1 - frac) + c1v * frac)
         Gc0, Gc1 = gather(r, cc0), gather(r, cc1)
@@ -432,10 +440,10 @@ def adjoint64(fr: Frozen, th: dict, g_adc=None):
     nn = (2 * p.number_pix_neighbors + 1) ** 2
     cin = d["currents_idx_neigh"].reshape(S, nn, 2)
     pid = d["pIDs_neigh"].reshape(S, nn)
-    cum0 = np.cumsum(Tb[0], axis=-1, dtype=np.float64)
+    cum0 = np.cumsum(Tb[0], axis=-1, dtype=ft)
     for k in range(nn):
         r = renum(pid[:, k], True)
-        T0 = Tb[0, cin[:, k, 0], cin[:, k, 1], Nt - L:].astype(np.float64)
+        T0 = Tb[0, cin[:, k, 0], cin[:, k, 1], Nt - L:].astype(ft)
         G0, G1 = gather(r, col0), gather(r, col1)
         gv = G0 * (1 - frac)[:, None] + G1 * frac[:, None]
         cr = cum0[cin[:, k, 0], cin[:, k, 1]]
@@ -445,8 +453,8 @@ def adjoint64(fr: Frozen, th: dict, g_adc=None):
         gd = Gc0 * (1 - frac) + Gc1 * frac
         A_ne += (T0 * gv).sum(1) + gd * D
         A_fr += (T0 * ne[:, None] * (G1 - G0)).sum(1) + D * ne * (Gc1 - Gc0) + gd * ne * (c0v - c1v)
-    A_ld = A_a * da + A_b * db + A_c * dc
-    A_t0 = A_fr / p.t_sampling
+    A_ld = A_a * da.astype(ft) + A_b * db.astype(ft) + A_c * dc.astype(ft)
+    A_t0 = A_fr / ft.type(p.t_sampling)
     J = _jacobian(fr, th)
     return {k: float((A_ne * J[k][0] + A_sig * J[k][1] + A_ld * J[k][2] + A_t0 * J[k][3]).sum()) for k in GRAD_PARAMS}
 

@@ -10,16 +10,21 @@ dataio.py:111; and 0.04 cm), zero-length tracks, tracks shorter than one
 step, tracks of an exact multiple of the step, axis-aligned tracks and
 negative coordinates.  Generated with NumPy 2.
 
-Usage: python tests/golden/make_chop_golden.py [/path/to/larnd-sim-jax]
+Usage: python tests/golden/make_chop_golden.py /path/to/larnd-sim-jax   (or LARNDSIM_JAX_SRC=/path/to/larnd-sim-jax)
 """
 
+import os
 import sys
 import types
 from pathlib import Path
 
 import numpy as np
 
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+# the larnd-sim-jax source tree: the first argument, or LARNDSIM_JAX_SRC
+REF = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LARNDSIM_JAX_SRC", ""))
+if not (REF / "src" / "larndsim").is_dir():
+    raise SystemExit(f"{Path(__file__).name}: give the larnd-sim-jax source tree as the first argument "
+                     "or in LARNDSIM_JAX_SRC")
 OUT = Path(__file__).resolve().parent / "chop_ref.npz"
 
 FIELDS = ("eventID", "trackID", "x_start", "y_start", "z_start", "x_end", "y_end", "z_end", "x", "y", "z",

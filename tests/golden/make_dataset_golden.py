@@ -12,17 +12,22 @@ event) matched to two of those cases.  Both structured arrays are stored
 too, so the tests feed the same rows to the GB300 implementation.
 Generated with NumPy 2.
 
-Usage: python tests/golden/make_dataset_golden.py [/path/to/larnd-sim-jax]
+Usage: python tests/golden/make_dataset_golden.py /path/to/larnd-sim-jax   (or LARNDSIM_JAX_SRC=/path/to/larnd-sim-jax)
 """
 
 import importlib.util
+import os
 import sys
 import types
 from pathlib import Path
 
 import numpy as np
 
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+# the larnd-sim-jax source tree: the first argument, or LARNDSIM_JAX_SRC
+REF = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LARNDSIM_JAX_SRC", ""))
+if not (REF / "src" / "larndsim").is_dir():
+    raise SystemExit(f"{Path(__file__).name}: give the larnd-sim-jax source tree as the first argument "
+                     "or in LARNDSIM_JAX_SRC")
 OUT = Path(__file__).resolve().parent / "dataset_ref.npz"
 
 # HDF5 field names of the reference's segments dataset (event_id / traj_id

@@ -7,15 +7,20 @@ centres (get_pixel_coordinates), hit z (get_hit_z with get_vdrift), the
 digitisation of zero charge and the ADC->charge inverse (adc2charge) of
 the reference as XLA compiled them.
 
-Usage: python tests/golden/make_golden.py [/path/to/larnd-sim-jax]
+Usage: python tests/golden/make_golden.py /path/to/larnd-sim-jax   (or LARNDSIM_JAX_SRC=/path/to/larnd-sim-jax)
 """
 
+import os
 import sys
 from pathlib import Path
 
 import numpy as np
 
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+# the larnd-sim-jax source tree: the first argument, or LARNDSIM_JAX_SRC
+REF = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LARNDSIM_JAX_SRC", ""))
+if not (REF / "src" / "larndsim").is_dir():
+    raise SystemExit(f"{Path(__file__).name}: give the larnd-sim-jax source tree as the first argument "
+                     "or in LARNDSIM_JAX_SRC")
 OUT = Path(__file__).resolve().parent / "jax_ref_hits.npz"
 
 

@@ -34,7 +34,7 @@ target's pixel ids and float64 ADC grid, the loss at the perturbed
 parameters, the steps and the central-difference gradient, in
 grad_ref.npz.
 
-Usage: python tests/golden/make_grad_golden.py [/path/to/larnd-sim-jax]
+Usage: python tests/golden/make_grad_golden.py /path/to/larnd-sim-jax   (or LARNDSIM_JAX_SRC=/path/to/larnd-sim-jax)
 """
 
 import json

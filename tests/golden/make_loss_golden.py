@@ -15,7 +15,7 @@ float32 rounding.  The 64-bit run also gives central differences with
 respect to Q and z of the first 12 predicted hits (and hit_prob for
 nll_loss), step 1e-6 max(|v|, 1).
 
-Usage: python tests/golden/make_loss_golden.py [/path/to/larnd-sim-jax]
+Usage: python tests/golden/make_loss_golden.py /path/to/larnd-sim-jax   (or LARNDSIM_JAX_SRC=/path/to/larnd-sim-jax)
 """
 
 import json

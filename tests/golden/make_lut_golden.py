@@ -17,10 +17,11 @@ bank, the waveforms (non-zero entries as row, tick, value), the pixel ids,
 the front end's integral and tick grids, the digitised grid and the 8
 compacted outputs of simulate_stochastic, in lut_ref.npz.
 
-Usage: python tests/golden/make_lut_golden.py [/path/to/larnd-sim-jax]
+Usage: python tests/golden/make_lut_golden.py /path/to/larnd-sim-jax   (or LARNDSIM_JAX_SRC=/path/to/larnd-sim-jax)
 """
 
 import json
+import os
 import sys
 import tempfile
 import zlib
@@ -30,7 +31,11 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parents[1]
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+# the larnd-sim-jax source tree: the first argument, or LARNDSIM_JAX_SRC
+REF = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LARNDSIM_JAX_SRC", ""))
+if not (REF / "src" / "larndsim").is_dir():
+    raise SystemExit(f"{Path(__file__).name}: give the larnd-sim-jax source tree as the first argument "
+                     "or in LARNDSIM_JAX_SRC")
 OUT = HERE / "lut_ref.npz"
 
 sys.path[:0] = [str(HERE), str(REPO / "larnd-sim-jax_gb300")]

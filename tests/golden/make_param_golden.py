@@ -19,7 +19,7 @@ the pixel ids, the waveforms (non-zero entries), the front end's integral
 and tick grids, and the 8 outputs of simulate_parametrized, in
 param_ref.npz.
 
-Usage: python tests/golden/make_param_golden.py [/path/to/larnd-sim-jax]
+Usage: python tests/golden/make_param_golden.py /path/to/larnd-sim-jax   (or LARNDSIM_JAX_SRC=/path/to/larnd-sim-jax)
 """
 
 import json

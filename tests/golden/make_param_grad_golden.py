@@ -16,7 +16,7 @@ step 1e-6 |theta|, halved until the pixel list and every t0 tick are the
 same on both sides.  The simulated pixel ids at the perturbed parameters
 are stored with the derivatives.  Stored in param_grad_ref.npz.
 
-Usage: python tests/golden/make_param_grad_golden.py [/path/to/larnd-sim-jax]
+Usage: python tests/golden/make_param_grad_golden.py /path/to/larnd-sim-jax   (or LARNDSIM_JAX_SRC=/path/to/larnd-sim-jax)
 """
 
 import json

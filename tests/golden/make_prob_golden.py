@@ -18,7 +18,7 @@ whose log-probability exceeds -60, the digitised distribution's entries
 there, and per (pixel, hit) the expected tick, the expected ADC and the
 total probability, in prob_ref.npz.
 
-Usage: python tests/golden/make_prob_golden.py [/path/to/larnd-sim-jax]
+Usage: python tests/golden/make_prob_golden.py /path/to/larnd-sim-jax   (or LARNDSIM_JAX_SRC=/path/to/larnd-sim-jax)
 """
 
 import json

@@ -2,6 +2,7 @@
 C-ABI library's exported symbols (no GPU needed)."""
 
 import ctypes
+import os
 import re
 from pathlib import Path
 
@@ -11,7 +12,8 @@ import pytest
 from larndsim_gb300 import _abi, consts, yaml_lite
 
 ROOT = Path(__file__).resolve().parent.parent
-REF = Path("/root/reference")
+# the larnd-sim-jax source tree, when one is at hand (its own YAML files)
+REF = Path(os.environ.get("LARNDSIM_JAX_SRC", "/nonexistent"))
 
 DETPROP = """
 tpc_centers: # cm
@@ -84,7 +86,7 @@ def test_unknown_detector_key_raises(tmp_path):
         consts.load_detector_properties(consts.Params, tmp_path / "det.yaml", tmp_path / "lay.yaml")
 
 
-@pytest.mark.skipif(not REF.exists(), reason="reference checkout not present")
+@pytest.mark.skipif(not REF.exists(), reason="set LARNDSIM_JAX_SRC to the larnd-sim-jax source tree")
 def test_reference_yaml_files_give_the_embedded_geometry():
     p = consts.load_detector_properties(
         consts.Params, REF / "src/larndsim/detector_properties/module0.yaml",
@@ -151,7 +153,7 @@ def lib():
 
 def test_library_exports_every_declared_symbol(lib):
     header = (ROOT / "include" / "lsim.h").read_text()
-    names = set(re.findall(r"^\s*(?:int|size_t|void|const char \*)\s*(lsim_\w+)\s*\(", header, re.M))
+    names = set(re.findall(r"^\s*(?:int64_t|int|size_t|void|const char \*)\s*(lsim_\w+)\s*\(", header, re.M))
     assert len(names) >= 15
     for n in names:
         assert hasattr(lib, n), n
@@ -266,3 +268,26 @@ def test_track_batch_entry_points_reject_bad_arguments_without_gpu(lib):
     roles = (ctypes.c_int8 * 3)(0, 1, 5)
     assert lib.lsim_pad_tracks(V(16), 4, 8, 3, 0, roles, -1, None) == _abi.LSIM_ERR_INVALID
     assert lib.lsim_pad_tracks(V(16), 4, 8, 3, 3, None, -1, None) == _abi.LSIM_ERR_INVALID
+
+
+def test_noalloc_refuses_sizes_beyond_its_scratch_before_any_cuda_call(lib):
+    """The size checks of lsim_hits_noalloc come before any CUDA call, so the
+    refusals are tested here without a GPU.  On a machine with a visible GPU
+    the test is skipped: its pointers are host placeholders that must never
+    reach a kernel."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("placeholder pointers are only passed where no GPU is visible")
+    cap = lib.lsim_hits_noalloc_max_slots()
+    assert cap == 16384 * 1024
+    p = _abi.make_params(consts.Params())
+    H = int(p.max_adc_values)
+    buf = np.zeros(16, np.float32)
+    ph = ctypes.c_void_p(buf.ctypes.data)
+    for n_pix in (cap // H + 1, 1 << 62):          # just past the limit, and a count whose product would wrap
+        rc = lib.lsim_hits_noalloc(p, ph, ph, ph, n_pix, 1997, *([ph] * 8), ph, None)
+        assert rc == _abi.LSIM_ERR_CAPACITY
+        assert b"fixed scratch limit" in lib.lsim_last_error()
+    p.max_adc_values = 0
+    assert lib.lsim_hits_noalloc(p, ph, ph, ph, 4, 1997, *([ph] * 8), ph, None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_hits(p, ph, ph, ph, 4, 1997, *([ph] * 8), ph, ph, 1 << 20, None) == _abi.LSIM_ERR_INVALID

@@ -71,13 +71,40 @@ def test_noalloc_matches_workspace_entry_point_on_consecutive_calls(cuda):
             np.testing.assert_array_equal(a, b)
 
 
+def _synthetic_grids(n_pix, H, seed=5):
+    """Random ADC and tick grids over n_pix sorted pixel ids (a few -1 rows
+    first, as simulate_wfs orders them), on the device."""
+    rng = np.random.default_rng(seed)
+    adc = torch.from_numpy(rng.uniform(70.0, 130.0, (n_pix, H)).astype(np.float32)).cuda()
+    ticks = torch.from_numpy(rng.integers(0, 2000, (n_pix, H)).astype(np.float32)).cuda()
+    pids = np.sort(rng.integers(0, 1 << 30, n_pix).astype(np.int32))
+    pids[:3] = -1
+    return adc, ticks, torch.from_numpy(pids).cuda()
+
+
 @pytest.mark.gpu
-def test_noalloc_rejects_sizes_beyond_its_scratch(cuda):
+def test_noalloc_at_its_slot_limit_matches_workspace_entry_point(cuda):
+    """The largest accepted size, compared bit for bit with lsim_hits; one
+    pixel more is refused.  Every buffer is sized for the refused call too,
+    so no call can reach past an allocation."""
     from larndsim_gb300 import _abi
     lib = _abi.load()
     lp = _abi.make_params(small_params())
-    n_pix = MAX_SLOTS // int(lp.max_adc_values) + 1
-    fake = ctypes.c_void_p(256)        # never dereferenced: the size check comes first
-    rc = lib.lsim_hits_noalloc(lp, fake, fake, fake, n_pix, 1997, *([fake] * 8), fake, None)
+    H = int(lp.max_adc_values)
+    cap = int(lib.lsim_hits_noalloc_max_slots())
+    assert cap == MAX_SLOTS
+    n_pix = cap // H
+    adc, ticks, unique = _synthetic_grids(n_pix + 1, H)
+    ref = _call(lib, lp, adc[:n_pix], ticks[:n_pix], unique[:n_pix], 1997, noalloc=False)
+    got = _call(lib, lp, adc[:n_pix], ticks[:n_pix], unique[:n_pix], 1997, noalloc=True)
+    assert ref[0].shape[0] > 0.9 * (n_pix - 3) * H
+    for a, b in zip(got, ref):
+        np.testing.assert_array_equal(a, b)
+    n = (n_pix + 1) * H
+    outs = [torch.empty(n, dtype=torch.float32, device="cuda") for _ in range(6)] + \
+        [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(2)]
+    nb = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rc = lib.lsim_hits_noalloc(lp, adc.data_ptr(), ticks.data_ptr(), unique.data_ptr(), n_pix + 1, 1997,
+                               *[t.data_ptr() for t in outs], nb.data_ptr(), torch.cuda.current_stream().cuda_stream)
     assert rc == _abi.LSIM_ERR_CAPACITY
     assert b"fixed scratch limit" in lib.lsim_last_error()
