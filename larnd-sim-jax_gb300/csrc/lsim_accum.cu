@@ -79,9 +79,9 @@ __device__ __forceinline__ int list_dy(int cd) { return ((cd >> 4) & 15) - 4; }
 
 // ---------------------------------------------------------------- neighbour batches
 
-// Decode global neighbour-contribution index g into (segment, dx, dy).
-__device__ __forceinline__ bool neigh_lookup(const ListSmem &ls, const int32_t *__restrict__ seg_list, int g, int *s,
-                                             int *dx, int *dy) {
+// Decode global neighbour-contribution index g into its slot-list position
+// and the slot's offset (dx, dy) from the pixel.
+__device__ __forceinline__ bool neigh_lookup(const ListSmem &ls, int g, int *pos, int *dx, int *dy) {
   int lo = 0, hi = ls.n;                 // last entry with pre_n <= g
   while (hi - lo > 1) {
     int mid = (lo + hi) >> 1;
@@ -91,7 +91,7 @@ __device__ __forceinline__ bool neigh_lookup(const ListSmem &ls, const int32_t *
   *dx = list_dx(cd);
   *dy = list_dy(cd);
   if (*dx == 0 && *dy == 0) return false;
-  *s = __ldg(seg_list + ls.off[lo] + (g - ls.pre_n[lo]));
+  *pos = ls.off[lo] + (g - ls.pre_n[lo]);
   return true;
 }
 
@@ -182,30 +182,32 @@ template <bool GRAD>
 __device__ __forceinline__ void neigh_setup(const LsimParams &p, const Tables &tab, const Workspace &w,
                                             const ListSmem &ls, NBatch &nb, int g0, int n_total, int lane) {
   const int g = g0 + lane;
-  int s = 0, dx = 0, dy = 0;
+  int pos = 0, dx = 0, dy = 0;
   NDesc d;
   d.w = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
   d.g0 = make_float4(0.f, 0.f, 0.f, 0.f);
   d.g1 = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (g < n_total && neigh_lookup(ls, w.seg_list, g, &s, &dx, &dy)) {
-    const SegFwd &f = w.segf[s];
-    const float ne = __ldg(&f.ne);
+  if (g < n_total && neigh_lookup(ls, g, &pos, &dx, &dy)) {
+    // the slot lists' compact records: consecutive contributions of a slot
+    // read consecutive 16-byte records, with no segment-index indirection
+    const SegNb q = w.lnb[pos];
+    const float ne = q.ne;
     if (ne != 0.f) {
       constexpr int nbp = kBinsPerPixel;
-      const int cx = lut_index(__ldg(&f.bx), nbp, dx * nbp);
-      const int cy = lut_index(__ldg(&f.by), nbp, dy * nbp);
+      const int cx = lut_index((int)(int16_t)(q.bxy & 0xffff), nbp, dx * nbp);
+      const int cy = lut_index(q.bxy >> 16, nbp, dy * nbp);
       const int row = cx * p.lut_ny + cy;
-      const int cath = __ldg(&f.cath);
-      const float frac = __ldg(&f.frac);
+      const int cath = q.cath;
+      const float frac = q.frac;
       const int cb = p.lut_nt - p.signal_length - cath - 1;
       float dl;
       const float D = cum_terms(tab.c0 + (size_t)row * p.lut_nt, cath, p.lut_nt, p.signal_length, frac, &dl);
       const float pk = pack_window(row, cb, window_interior(cb, p.signal_length, p.n_ticks));
       if (GRAD) {
-        const SegAdj &a = w.sega[s];
+        const SegNbAdj a = w.lna[pos];
         d.w = make_float4(frac, 1.f - frac, D, pk);
-        d.g0 = make_float4(dl, ne * __ldg(&a.dt0) / p.t_sampling, __ldg(&a.dne[4]), 0.f);
-        d.g1 = make_float4(__ldg(&a.dne[0]), __ldg(&a.dne[1]), __ldg(&a.dne[2]), __ldg(&a.dne[3]));
+        d.g0 = make_float4(dl, ne * a.dne4_dt0.y / p.t_sampling, a.dne4_dt0.x, 0.f);
+        d.g1 = a.dne03;
       } else {
         d.w = make_float4(ne * (1.f - frac), ne * frac, D, pk);
       }

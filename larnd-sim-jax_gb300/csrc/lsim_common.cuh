@@ -50,6 +50,23 @@ struct __align__(16) SegAdj {
   float pad[1];
 };
 
+// Compact copy of what the neighbour passes of the pixel kernel read per
+// contribution, one 16-byte load each: electrons, sub-tick fraction, cathode
+// tick, and the sub-pixel bins packed as two int16 (bx in bits 0..15, by in
+// 16..31; stage 1 rejects segments with charge whose bins do not fit).
+struct __align__(16) SegNb {
+  float ne, frac;
+  int cath;
+  int bxy;
+};
+// Compact adjoint partials of the neighbour passes: d ne / d(Ab, kb,
+// eField, lifetime) in the first float4; d ne / d lArDensity and d t0 /
+// d eField in the second.
+struct __align__(16) SegNbAdj {
+  float4 dne03;
+  float4 dne4_dt0;
+};
+
 // Per-segment record of parametrised mode (64 bytes).
 struct __align__(16) SegPar {
   float ne;
@@ -131,6 +148,10 @@ struct Workspace {
   float *main_out;          // per segment: main-bin adjoint [0, 8 gradient terms] (kPixRec floats)
   int32_t *seg_order;       // segments with main-bin records, grouped by template index
   int32_t *tidx_hist;       // kMaxTemplates counts, then kMaxTemplates cursors
+  SegNb *segn;              // per segment: compact neighbour-pass record (LUT mode)
+  SegNbAdj *segna;          // per segment: compact neighbour-pass adjoint partials (LUT mode)
+  SegNb *lnb;               // segn in slot-list order (seg_list positions): a slot's run reads contiguously
+  SegNbAdj *lna;            // segna in slot-list order
   size_t bytes;
 };
 
@@ -173,6 +194,10 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   size_t o_thist = take(4 * (size_t)kMaxTemplates * 2);
   size_t o_fmask = take(4 * (size_t)kFeeMaskWords * kMaxPixelWarps);
   size_t o_tidx = take(4 * (size_t)n_rows);
+  size_t o_segn = take(sizeof(SegNb) * (size_t)n_rows);
+  size_t o_segna = take(sizeof(SegNbAdj) * (size_t)n_rows);
+  size_t o_lnb = take(sizeof(SegNb) * (size_t)n_rows);
+  size_t o_lna = take(sizeof(SegNbAdj) * (size_t)n_rows);
   Workspace w;
   char *b = (char *)base;
   w.counts = (LsimCounts *)(b + o_counts);
@@ -200,6 +225,10 @@ inline Workspace carve_workspace(void *base, const LsimParams &p, int64_t n_rows
   w.tidx_hist = (int32_t *)(b + o_thist);
   w.fee_masks = (uint32_t *)(b + o_fmask);
   w.tgt_index = (int32_t *)(b + o_tidx);
+  w.segn = (SegNb *)(b + o_segn);
+  w.segna = (SegNbAdj *)(b + o_segna);
+  w.lnb = (SegNb *)(b + o_lnb);
+  w.lna = (SegNbAdj *)(b + o_lna);
   w.bytes = off;
   return w;
 }

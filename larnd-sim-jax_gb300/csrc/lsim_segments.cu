@@ -255,6 +255,20 @@ __global__ void k_segments_lut(LsimParams p, LsimFieldMap f, const float *__rest
   a.pad[0] = 0.f;
   w.segf[s] = r;
   w.sega[s] = a;
+  SegNb nbr;
+  nbr.ne = ne;
+  nbr.frac = frac;
+  nbr.cath = cath;
+  nbr.bxy = (int)(((unsigned)bx & 0xffffu) | ((unsigned)by << 16));
+  if (ne != 0.f && (bx < -32768 || bx > 32767 || by < -32768 || by > 32767)) {
+    set_status(w.counts, LSIM_ERR_UNSUPPORTED, (int)s);
+    nbr.ne = 0.f;
+  }
+  w.segn[s] = nbr;
+  SegNbAdj nba;
+  nba.dne03 = make_float4(a.dne[0], a.dne[1], a.dne[2], a.dne[3]);
+  nba.dne4_dt0 = make_float4(a.dne[4], a.dt0, 0.f, 0.f);
+  w.segna[s] = nba;
   // ---- principal pixel, main pixel id, grid slot
   const int nb = p.nb_bins_per_pixel;
   int ppx = ifloordiv(bx, nb), ppy = ifloordiv(by, nb);
@@ -511,8 +525,18 @@ __global__ void k_scatter(const int32_t *__restrict__ key, int64_t n_rows, const
 // every float32 result, is deterministic.  Lists of up to kSortLocal
 // segments are sorted here by one thread; longer ones are queued for
 // k_sort_big_slots.
+// List-ordered copies of the compact neighbour-pass records (LUT mode;
+// lnb null in parametrised mode): entry i of the slot lists gets the record
+// of segment seg_list[i].
+__device__ __forceinline__ void copy_list_records(const Workspace &w, int64_t pos, int32_t s) {
+  if (!w.lnb) return;
+  w.lnb[pos] = w.segn[s];
+  w.lna[pos] = w.segna[s];
+}
+
 __global__ void k_sort_slots(const int32_t *__restrict__ cnt, const int32_t *__restrict__ off, int64_t G,
-                             int32_t *__restrict__ seg_list, int32_t *__restrict__ big_slots, LsimCounts *counts) {
+                             int32_t *__restrict__ seg_list, int32_t *__restrict__ big_slots, LsimCounts *counts,
+                             Workspace w) {
   int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int c = slot < G ? cnt[slot] : 0;
   // one atomic per warp for the largest slot (a shared counter is hot)
@@ -521,8 +545,13 @@ __global__ void k_sort_slots(const int32_t *__restrict__ cnt, const int32_t *__r
     atomicMax(&counts->max_slot, cmax);
     if (cmax > kMaxSlotSegments) atomicCAS(&counts->status, 0, (int)LSIM_ERR_CAPACITY);
   }
-  if (c <= 1) return;
-  int32_t *l = seg_list + off[slot];
+  if (c <= 0) return;
+  const int64_t o = off[slot];
+  int32_t *l = seg_list + o;
+  if (c == 1) {
+    copy_list_records(w, o, l[0]);
+    return;
+  }
   if (c > kSortLocal) {
     big_slots[atomicAdd(&counts->n_big_slots, 1)] = (int32_t)slot;
     return;
@@ -537,7 +566,10 @@ __global__ void k_sort_slots(const int32_t *__restrict__ cnt, const int32_t *__r
       while (j >= 0 && v[j] > x) { v[j + 1] = v[j]; --j; }
       v[j + 1] = x;
     }
-    for (int i = 0; i < c; ++i) l[i] = v[i];
+    for (int i = 0; i < c; ++i) {
+      l[i] = v[i];
+      copy_list_records(w, o + i, v[i]);
+    }
   }
 }
 
@@ -551,7 +583,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_big_slots(const int32_t *
                                                                  const int32_t *__restrict__ off,
                                                                  int32_t *__restrict__ seg_list,
                                                                  const int32_t *__restrict__ big_slots,
-                                                                 const LsimCounts *counts) {
+                                                                 const LsimCounts *counts, Workspace w) {
   __shared__ int32_t sh[kSortBig];
   const int nbig = counts->n_big_slots;
   for (int b = blockIdx.x; b < nbig; b += gridDim.x) {
@@ -575,7 +607,10 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_big_slots(const int32_t *
           }
           __syncthreads();
         }
-      for (int i = threadIdx.x; i < c; i += kSortThreads) l[i] = sh[i];
+      for (int i = threadIdx.x; i < c; i += kSortThreads) {
+        l[i] = sh[i];
+        copy_list_records(w, off[slot] + i, sh[i]);
+      }
     } else {
       for (int phase = 0; phase < c; ++phase) {
         for (int i = 2 * threadIdx.x + (phase & 1); i + 1 < c; i += 2 * kSortThreads) {
@@ -584,6 +619,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_big_slots(const int32_t *
         }
         __syncthreads();
       }
+      for (int i = threadIdx.x; i < c; i += kSortThreads) copy_list_records(w, off[slot] + i, l[i]);
     }
     __syncthreads();
   }
@@ -615,7 +651,10 @@ __global__ void k_fill_unique(LsimParams p, Grid g, const int32_t *__restrict__ 
 
 // ---------------------------------------------------------------- host drivers
 
-int run_pixel_map(const LsimParams &p, const Workspace &w, const Grid &g, int64_t n_rows, cudaStream_t st) {
+int run_pixel_map(const LsimParams &p, const Workspace &w0, const Grid &g, int64_t n_rows, cudaStream_t st,
+                  bool list_records) {
+  Workspace w = w0;
+  if (!list_records) w.lnb = nullptr, w.lna = nullptr;
   int64_t nscan = (g.G + kScanTile - 1) / kScanTile;
   if (nscan > 0) {
     k_scan_reduce<<<(unsigned)nscan, kScanThreads, 0, st>>>(w.cnt, g.G, g, w.scan_blocks);
@@ -627,9 +666,9 @@ int run_pixel_map(const LsimParams &p, const Workspace &w, const Grid &g, int64_
   if (n_rows > 0) k_scatter<<<(unsigned)((n_rows + 255) / 256), 256, 0, st>>>(w.key, n_rows, w.off, w.cursor, w.seg_list);
   if (g.G > 0) {
     k_sort_slots<<<(unsigned)((g.G + 255) / 256), 256, 0, st>>>(w.cnt, w.off, g.G, w.seg_list, w.big_slots,
-                                                                 w.counts);
+                                                                 w.counts, w);
     k_sort_big_slots<<<(unsigned)(device_sm_count() * 4), kSortThreads, 0, st>>>(w.cnt, w.off, w.seg_list,
-                                                                                w.big_slots, w.counts);
+                                                                                w.big_slots, w.counts, w);
   }
   return LSIM_OK;
 }
@@ -649,7 +688,7 @@ int run_stage1(bool param_mode, const LsimParams &p, const LsimFieldMap &f, cons
       k_segments_lut<<<nb, 128, 0, st>>>(p, f, tracks, n_rows, n_events, w, g,
                                          theta_dev ? w.theta_derived : nullptr);
   }
-  return run_pixel_map(p, w, g, n_rows, st);
+  return run_pixel_map(p, w, g, n_rows, st, !param_mode);
 }
 
 int run_fill_unique(const LsimParams &p, const Workspace &w, const Grid &g, int64_t p_pad, int32_t n_em1,

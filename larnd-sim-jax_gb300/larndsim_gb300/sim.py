@@ -182,6 +182,9 @@ class Stage1:
         c = self.counts()
         if c[3] == _abi.LSIM_ERR_CAPACITY:
             raise ValueError(f"{int(c[4])} segments share one principal pixel; at most {(1 << 23) - 1} are supported")
+        if c[3] == _abi.LSIM_ERR_UNSUPPORTED:
+            raise ValueError(f"segment at row {int(c[5])} lies beyond the supported sub-pixel bin range "
+                             "(|bin| < 32768 per axis)")
         if c[3] != 0:
             row = int(c[5])
             raise ValueError(f"invalid track input: eventID outside [-1, {self.n_events}) at row {row} "
