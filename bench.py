@@ -65,7 +65,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--events", type=int, default=N_EVENTS, help="events per batch (profiling runs use fewer)")
     ap.add_argument("--hits", type=int, default=None, help="hits of --path records (profiling runs use fewer)")
-    ap.add_argument("--path", choices=["grad", "forward", "param", "param_grad", "chop", "prob", "loss", "records"],
+    ap.add_argument("--path", choices=["grad", "forward", "param", "param_grad", "chop", "prob", "loss", "records",
+                                       "fit"],
                     default="grad",
                     help="grad: the fwd+bwd step (default); chop: on-device chop_tracks of one 500k-segment event; "
                          "prob: the probabilistic front end on the waveforms of 8 events; loss: mse_adc forward + "
@@ -73,7 +74,9 @@ def parse():
                          "drop-in (LUT mode / parametrised mode) on the 64-event batch; param_grad: the "
                          "parametrised-mode SSE-ADC loss and its gradient (autograd through the waveform, "
                          "front-end and current-model adjoints); records: the driver's hit records (clean "
-                         "mask, compaction, charge, per-event runs) of 32M hits")
+                         "mask, compaction, charge, per-event runs) of 32M hits; fit: 200 steps of the "
+                         "reference's gradient-descent fit (sigmoid normalisation, Adam) on 32 events x 20k "
+                         "segments, one CUDA graph per step")
     return ap.parse_args()
 
 
@@ -827,6 +830,86 @@ def run_forward(args, param_mode=False):
     print(json.dumps(rec), flush=True)
 
 
+# ---------------------------------------------------------------- fit loop
+
+FIT_EVENTS, FIT_SEGMENTS, FIT_STEPS, FIT_LR, FIT_SEED = 32, 20_000, 200, 1e-3, 77
+
+
+def run_fit(args):
+    """The fit loop of the reference's GradientDescentFitter with its default
+    flags (sigmoid normalisation, optax.adam, no clipping; optimize/
+    fit_params.py:781-895, example_run.py) on 32 events x 20k segments: 200
+    steps on the 7 parameters the loss depends on (vdrift does not enter),
+    target simulated at hidden parameters drawn from N(nominal, 5 %) inside
+    the ranges.  value: steps/s of the device-resident loop (stage 1,
+    forward + adjoint, optimiser update replayed as one CUDA graph per
+    step); e2e: pinned host tracks in, the fit set up, 200 steps, the final
+    parameters read back."""
+    import torch
+    from larndsim_gb300 import fit, grad, sim, workloads
+    from larndsim_gb300.grad import GRAD_PARAMS
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    names = tuple(k for k in GRAD_PARAMS if k != "vdrift")
+    params = nominal_params()
+    tmpl, params = sim.load_lut(workloads.synthetic_response(seed=0), params)
+    tracks, fields = workloads.batched_events(seed=FIT_SEED, n_events=FIT_EVENTS, min_segments=FIT_SEGMENTS,
+                                              max_segments=FIT_SEGMENTS + 1)
+    rng = np.random.default_rng(FIT_SEED)
+    hid = {}
+    for k in names:
+        r = fit.RANGES[k]
+        hid[k] = float(np.clip(float(getattr(params, k)) * (1.0 + 0.05 * rng.standard_normal()), r["down"], r["up"]))
+    hidden = params.replace(**hid)
+    t_dev = torch.from_numpy(tracks).cuda()
+    target = grad.LUTChain(params, tmpl, t_dev, fields).target(hidden)
+
+    def make(tr):
+        return fit.DeviceFit(params, tmpl, tr, fields, target, fit_params=names, lr=FIT_LR,
+                             normalization_scheme="sigmoid", max_steps=FIT_STEPS + 8)
+
+    f = make(t_dev)
+    f.capture()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(torch.cuda.current_device())
+    torch.cuda.synchronize()
+    start.record()
+    for _ in range(FIT_STEPS):
+        f.graph.replay()
+    end.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = start.elapsed_time(end) / FIT_STEPS
+    loss, th = f.history()
+    err = {k: float(th[-1, GRAD_PARAMS.index(k)] / hid[k] - 1.0) for k in names}
+    err0 = {k: float(float(getattr(params, k)) / hid[k] - 1.0) for k in names}
+    host = torch.from_numpy(tracks).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g = make(host.to("cuda", non_blocking=True))
+    g.run(FIT_STEPS, graph=True)
+    final = g.theta.cpu()
+    e2e_s = time.perf_counter() - t0
+    rec = {"metric": "fit steps/s", "value": 1e3 / ms, "unit": "steps/s", "n_gpus": 1, "steps": FIT_STEPS,
+           "warmup": 1, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic (seeded tracks and LUT)",
+           "config": {"workload": f"GradientDescentFitter loop, {FIT_EVENTS} events x {FIT_SEGMENTS} segments "
+                                  f"({tracks.shape[0]} segments), n_neighbors=4, L=150, 100x45x45x1950 templates, "
+                                  f"SSE-ADC loss, 7 parameters, sigmoid normalisation, Adam lr {FIT_LR}",
+                      "segments": int(tracks.shape[0]),
+                      "step": "stage 1 + forward + adjoint + optimiser update, one CUDA graph replay per step",
+                      "l2": "inputs and work set larger than L2"},
+           "fit": {"loss_first": float(loss[0]), "loss_last": float(loss[-1]),
+                   "start_rel_error": err0, "final_rel_error": err},
+           "e2e": {"value": FIT_STEPS / e2e_s, "unit": "steps/s", "seconds": e2e_s,
+                   "h2d_bytes_per_step": int(tracks.nbytes) // FIT_STEPS, "d2h_bytes_per_step": 4 * 8 // FIT_STEPS},
+           "gpu_launches": (KERNELS_PER_STEP + 1) * FIT_STEPS, "clocks": clk,
+           "final_theta": [float(x) for x in final]}
+    print(json.dumps(rec), flush=True)
+
+
 def run_param_grad(args):
     """Parametrised mode fwd+bwd on the 64-event batch: waveforms at the
     perturbed parameters (offsets fixed), front end, SSE against the ADCs
@@ -1154,6 +1237,13 @@ def main():
     args = parse()
     if args.path == "records":
         (run_records_reference if args.impl == "reference" else run_records)(args)
+        return
+    if args.path == "fit":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "fit path: its CPU arm is the default path's "
+                                                                  "fwd+bwd restatement"}))
+        else:
+            run_fit(args)
         return
     if args.path == "param_grad":
         if args.impl == "reference":

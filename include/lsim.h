@@ -187,6 +187,47 @@ int lsim_lut_stage1_theta(const LsimParams *p, const LsimFieldMap *f, const floa
 int lsim_adam_step(float *theta_dev, const float *grad_dev, const float *scale_dev, const float *lr_dev,
                    float *state_dev, float beta1, float beta2, float eps, void *stream);
 
+/* Options of the fit step (GradientDescentFitter, optimize/fit_params.py:
+ * 168-199 map_norm_to_phys / map_phys_to_norm, :781-895 the optax chain
+ * and process_grads).  Arrays are indexed in LSIM_NPARAM order. */
+#define LSIM_NORM_SIGMOID 0   /* phys = lo + (hi - lo) sigmoid(k u) (the reference's default) */
+#define LSIM_NORM_EXP_LOG 1   /* phys = nom exp(k u) */
+#define LSIM_NORM_DIVIDE 2    /* phys = u * norm */
+#define LSIM_FIT_STATE 32     /* floats of fit-step state: m[8], v[8], u[8], step count, padding */
+typedef struct LsimFitOptions {
+  int32_t scheme;           /* LSIM_NORM_* */
+  int32_t fit_mask;         /* bit i set: parameter i is fitted; the others never change */
+  int32_t clip_from_range;  /* divide only: clip u to [down, up] / norm after each update */
+  float norm_scale;         /* k: normalization_scale_sigmoid or _exp_log (> 0); 1 for divide */
+  float max_clip_norm;      /* optax.clip_by_global_norm threshold; <= 0 or NaN: no clipping */
+  float beta1, beta2, eps;  /* optax.adam (0.9, 0.999, 1e-8) */
+  float lr[LSIM_NPARAM];
+  float lo[LSIM_NPARAM], hi[LSIM_NPARAM];        /* sigmoid: the ranges' min and max */
+  float nom[LSIM_NPARAM];                        /* exp_log: the ranges' nominal value (> 0) */
+  float norm[LSIM_NPARAM];                       /* divide: params_normalization */
+  float down[LSIM_NPARAM], up[LSIM_NPARAM];      /* clip_from_range: the ranges' down and up */
+} LsimFitOptions;
+
+/* Start a fit: for the fitted parameters, u = map_phys_to_norm(theta)
+ * (optimize/fit_params.py:182-199; divide: u = 1 for non-zero values), and
+ * theta <- map_norm_to_phys(u), the values the reference's first step
+ * evaluates (its loss maps the normalised parameters back,
+ * fit_params.py:713-731); Adam moments and step count cleared.
+ * state_dev holds LSIM_FIT_STATE floats. */
+int lsim_fit_init(float *theta_dev, const LsimFitOptions *opt, float *state_dev, void *stream);
+
+/* One step of the reference's gradient-descent fitter on device, in place,
+ * given grad_dev = dL/dtheta in physical units: the chain rule to the
+ * normalised parameters (jax.value_and_grad with respect to norm_params,
+ * fit_params.py:713-731), the NaN check that skips a step (:873-876), the
+ * extra normalisation factor of the divide scheme (:878-882),
+ * optax.clip_by_global_norm when enabled (:833-838), optax.adam per
+ * parameter with its learning rate, clip_values_from_range (divide and
+ * clip_from_range, :890-891) and the map back to physical values (:894).
+ * Needs no host synchronisation, so it can run inside a captured fit step. */
+int lsim_fit_step(float *theta_dev, const float *grad_dev, const LsimFitOptions *opt, float *state_dev,
+                  void *stream);
+
 /* Stage 2 of simulate_wfs: fill unique_pixels (p_pad rows: n_em1 negative
  * ids, n_m1 = p_pad - n_em1 - n_valid entries of -1, then the valid ids
  * ascending) and the waveforms wfs[p_pad][n_ticks-1] (garbage tick 0

@@ -194,6 +194,41 @@ int lsim_adam_step(float *theta_dev, const float *grad_dev, const float *scale_d
               "lsim_adam_step");
 }
 
+static int check_fit_options(const LsimFitOptions *o, const char *who) {
+  if (!o) return fail(LSIM_ERR_INVALID, "%s: null options", who);
+  if (o->scheme < LSIM_NORM_SIGMOID || o->scheme > LSIM_NORM_DIVIDE)
+    return fail(LSIM_ERR_INVALID, "%s: unknown normalization scheme %d", who, o->scheme);
+  if (!(o->norm_scale > 0.f)) return fail(LSIM_ERR_INVALID, "%s: normalization scale must be > 0", who);
+  for (int i = 0; i < LSIM_NPARAM; ++i) {
+    if (!((o->fit_mask >> i) & 1)) continue;
+    if (o->scheme == LSIM_NORM_EXP_LOG && !(o->nom[i] > 0.f))
+      return fail(LSIM_ERR_INVALID, "%s: exp_log normalization requires a positive nominal value (parameter %d)",
+                  who, i);
+    if (o->scheme == LSIM_NORM_SIGMOID && !(o->hi[i] > o->lo[i]))
+      return fail(LSIM_ERR_INVALID, "%s: sigmoid normalization requires max > min (parameter %d)", who, i);
+    if (o->scheme == LSIM_NORM_DIVIDE && o->clip_from_range && o->norm[i] == 0.f)
+      return fail(LSIM_ERR_INVALID, "%s: clip_from_range with a zero normalization (parameter %d)", who, i);
+  }
+  return LSIM_OK;
+}
+
+int lsim_fit_init(float *theta_dev, const LsimFitOptions *opt, float *state_dev, void *stream) {
+  g_err.clear();
+  int rc = check_fit_options(opt, "lsim_fit_init");
+  if (rc) return rc;
+  if (!theta_dev || !state_dev) return fail(LSIM_ERR_INVALID, "lsim_fit_init: null pointer");
+  return wrap(run_fit_init(theta_dev, *opt, state_dev, (cudaStream_t)stream), "lsim_fit_init");
+}
+
+int lsim_fit_step(float *theta_dev, const float *grad_dev, const LsimFitOptions *opt, float *state_dev,
+                  void *stream) {
+  g_err.clear();
+  int rc = check_fit_options(opt, "lsim_fit_step");
+  if (rc) return rc;
+  if (!theta_dev || !grad_dev || !state_dev) return fail(LSIM_ERR_INVALID, "lsim_fit_step: null pointer");
+  return wrap(run_fit_step(theta_dev, grad_dev, *opt, state_dev, (cudaStream_t)stream), "lsim_fit_step");
+}
+
 int lsim_param_stage1(const LsimParams *p, const LsimFieldMap *f, const float *tracks, int64_t n_rows,
                       int32_t n_events, const float *normals, void *ws, size_t ws_bytes, LsimCounts *counts_dev,
                       void *stream) {

@@ -11,6 +11,8 @@ int run_stage1(bool param_mode, const LsimParams &p, const LsimFieldMap &f, cons
                const float *theta_dev = nullptr);
 int run_adam(float *theta, const float *grad, const float *scale, const float *lr, float *state, float beta1,
              float beta2, float eps, cudaStream_t st);
+int run_fit_init(float *theta, const LsimFitOptions &o, float *state, cudaStream_t st);
+int run_fit_step(float *theta, const float *grad, const LsimFitOptions &o, float *state, cudaStream_t st);
 int run_fill_unique(const LsimParams &p, const Workspace &w, const Grid &g, int64_t p_pad, int32_t n_em1,
                     int32_t n_valid, int32_t *unique_pixels, float *wfs, int32_t nt_out, cudaStream_t st);
 

@@ -736,4 +736,97 @@ int run_adam(float *theta, const float *grad, const float *scale, const float *l
   return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------- fit step
+//
+// The reference's GradientDescentFitter (optimize/fit_params.py:781-895):
+// the optimiser works on normalised parameters u, phys = map_norm_to_phys(u)
+// (:168-179); gradients are taken with respect to u.  One warp, lane i for
+// parameter i; float32 throughout, as the reference computes.
+
+// jax.nn.sigmoid in float32: 1 / (1 + exp(-x)).
+__device__ __forceinline__ float fit_sigmoid(float x) { return 1.f / (1.f + expf(-x)); }
+
+__device__ __forceinline__ float norm_to_phys(const LsimFitOptions &o, int i, float u) {
+  const float k = o.norm_scale;
+  if (o.scheme == LSIM_NORM_SIGMOID) return o.lo[i] + (o.hi[i] - o.lo[i]) * fit_sigmoid(k * u);
+  if (o.scheme == LSIM_NORM_EXP_LOG) return o.nom[i] * expf(k * u);
+  return u * o.norm[i];
+}
+
+// d phys / d u, the chain rule JAX applies through norm_to_phys.
+__device__ __forceinline__ float dphys_du(const LsimFitOptions &o, int i, float u) {
+  const float k = o.norm_scale;
+  if (o.scheme == LSIM_NORM_SIGMOID) {
+    const float sg = fit_sigmoid(k * u);
+    return (o.hi[i] - o.lo[i]) * (sg * (1.f - sg)) * k;
+  }
+  if (o.scheme == LSIM_NORM_EXP_LOG) return o.nom[i] * expf(k * u) * k;
+  return o.norm[i];
+}
+
+// map_phys_to_norm (fit_params.py:182-199) in float32.
+__device__ __forceinline__ float phys_to_norm(const LsimFitOptions &o, int i, float v) {
+  const float k = o.norm_scale;
+  if (o.scheme == LSIM_NORM_SIGMOID) {
+    const float eps = 1.1920928955078125e-07f;   // float32 machine epsilon
+    float fr = (v - o.lo[i]) / (o.hi[i] - o.lo[i]);
+    fr = fminf(fmaxf(fr, eps), 1.f - eps);
+    return logf(fr / (1.f - fr)) / k;
+  }
+  if (o.scheme == LSIM_NORM_EXP_LOG) return logf(fmaxf(v, 1.17549435e-38f) / o.nom[i]) / k;
+  return v != 0.f ? 1.f : 0.f;
+}
+
+constexpr int kFitM = 0, kFitV = LSIM_NPARAM, kFitU = 2 * LSIM_NPARAM, kFitT = 3 * LSIM_NPARAM;
+static_assert(kFitT < LSIM_FIT_STATE, "fit-step state layout");
+
+__global__ void k_fit_init(float *theta, LsimFitOptions o, float *state) {
+  const int i = threadIdx.x;
+  if (i < LSIM_FIT_STATE) state[i] = 0.f;
+  if (i >= LSIM_NPARAM || !((o.fit_mask >> i) & 1)) return;
+  const float u = phys_to_norm(o, i, theta[i]);
+  state[kFitU + i] = u;
+  theta[i] = norm_to_phys(o, i, u);
+}
+
+__global__ void k_fit_step(float *theta, const float *grad, LsimFitOptions o, float *state) {
+  const int i = threadIdx.x;
+  const bool fit = i < LSIM_NPARAM && ((o.fit_mask >> i) & 1);
+  const float u = fit ? state[kFitU + i] : 0.f;
+  float g = fit ? grad[i] * dphys_du(o, i, u) : 0.f;
+  // a NaN gradient skips the whole update (process_grads returns early)
+  if (__any_sync(0xffffffffu, fit && isnan(g))) return;
+  if (o.scheme == LSIM_NORM_DIVIDE) g = g * o.norm[i & (LSIM_NPARAM - 1)];
+  // optax.clip_by_global_norm: scaled to the threshold when the norm reaches it
+  float sq = g * g;
+  for (int off = 16; off > 0; off >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, off);
+  const float gnorm = sqrtf(sq);
+  if (o.max_clip_norm > 0.f && !(gnorm < o.max_clip_norm)) g = (g / gnorm) * o.max_clip_norm;
+  const float t = state[kFitT] + 1.f;
+  __syncwarp();
+  if (i == 0) state[kFitT] = t;
+  if (!fit) return;
+  // optax.adam: bias-corrected moments, eps outside the square root, then -lr
+  const float m = o.beta1 * state[kFitM + i] + (1.f - o.beta1) * g;
+  const float v = o.beta2 * state[kFitV + i] + (1.f - o.beta2) * (g * g);
+  state[kFitM + i] = m;
+  state[kFitV + i] = v;
+  const float mh = m / (1.f - powf(o.beta1, t)), vh = v / (1.f - powf(o.beta2, t));
+  float un = u + (-o.lr[i]) * (mh / (sqrtf(vh) + o.eps));
+  if (o.scheme == LSIM_NORM_DIVIDE && o.clip_from_range)
+    un = fmaxf(o.down[i] / o.norm[i], fminf(o.up[i] / o.norm[i], un));
+  state[kFitU + i] = un;
+  theta[i] = norm_to_phys(o, i, un);
+}
+
+int run_fit_init(float *theta, const LsimFitOptions &o, float *state, cudaStream_t st) {
+  k_fit_init<<<1, 32, 0, st>>>(theta, o, state);
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
+int run_fit_step(float *theta, const float *grad, const LsimFitOptions &o, float *state, cudaStream_t st) {
+  k_fit_step<<<1, 32, 0, st>>>(theta, grad, o, state);
+  return cudaGetLastError() == cudaSuccess ? LSIM_OK : LSIM_ERR_CUDA;
+}
+
 }  // namespace lsim

@@ -37,6 +37,17 @@ class LsimHitColumns(C.Structure):
                                          "pixels")]
 
 
+NORM_SCHEMES = {"sigmoid": 0, "exp_log": 1, "divide": 2}
+FIT_STATE = 32
+
+
+class LsimFitOptions(C.Structure):
+    """Options of lsim_fit_init / lsim_fit_step (arrays in GRAD_PARAMS order)."""
+    _fields_ = [("scheme", C.c_int32), ("fit_mask", C.c_int32), ("clip_from_range", C.c_int32),
+                ("norm_scale", C.c_float), ("max_clip_norm", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float),
+                ("eps", C.c_float)] + [(n, C.c_float * NPARAM) for n in ("lr", "lo", "hi", "nom", "norm", "down", "up")]
+
+
 class LsimParams(C.Structure):
     _fields_ = [
         ("recombination_mode", C.c_int32),
@@ -88,6 +99,8 @@ _SIGNATURES = {
     "lsim_lut_stage1": (C.c_int, [_PP, _PF, _vp, _i64, _i32, _vp, _sz, _vp, _vp]),
     "lsim_lut_stage1_theta": (C.c_int, [_PP, _PF, _vp, _i64, _i32, _vp, _vp, _sz, _vp, _vp]),
     "lsim_adam_step": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_float, C.c_float, C.c_float, _vp]),
+    "lsim_fit_init": (C.c_int, [_vp, C.POINTER(LsimFitOptions), _vp, _vp]),
+    "lsim_fit_step": (C.c_int, [_vp, _vp, C.POINTER(LsimFitOptions), _vp, _vp]),
     "lsim_lut_stage2": (C.c_int, [_PP, _vp, _vp, _i64, _i32, _i64, _i32, _i32, _vp, _vp, _vp]),
     "lsim_valid_pixels": (C.c_int, [_PP, _vp, _i64, _i32, _i32, _vp, _vp]),
     "lsim_lut_adc": (C.c_int, [_PP, _vp, _vp, _i64, _i32, _i32, _vp, _vp, _vp, _vp]),

@@ -1,12 +1,16 @@
-"""Device-resident Adam fit of the physics parameters (the fit loop of
-optimize/fit_params.py:704-731, :872-895 with the "divide" normalisation).
+"""Device-resident fit of the physics parameters: the reference's
+GradientDescentFitter step (optimize/fit_params.py:704-731 the loss and its
+gradient with respect to the normalised parameters, :781-895 the optax
+chain and process_grads, :168-199 the normalisation schemes).
 
 One step is: the segment stage with the fit parameters read from device
 memory (``lsim_lut_stage1_theta``), the forward + adjoint of the SSE-ADC
-loss (``lsim_lut_grad``) and an Adam update of the parameters in place
-(``lsim_adam_step``).  Nothing in a step needs the host, so the step is
-captured once in a CUDA graph and replayed; the loss and the parameters of
-every step are appended to device-side histories inside the graph.
+loss (``lsim_lut_grad``) and the optimiser update of the parameters in place
+(``lsim_fit_step``: chain rule to the normalised parameters, NaN skip,
+optional clip_by_global_norm, Adam, optional clip_values_from_range, map
+back).  Nothing in a step needs the host, so the step is captured once in a
+CUDA graph and replayed; the loss and the parameters of every step are
+appended to device-side histories inside the graph.
 """
 
 from __future__ import annotations
@@ -14,19 +18,71 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from . import _abi, consts, sim
+from . import _abi, sim
 from .grad import GRAD_PARAMS, Target
+
+# The reference's parameter ranges (optimize/ranges.py) for the parameters
+# the gradient covers: nominal value, the soft range (down, up) used by
+# clip_values_from_range, and the hard limits (min, max) of the sigmoid map.
+RANGES = {
+    "Ab": dict(nom=0.8, down=0.78, up=0.88, min=0.75, max=0.9),
+    "kb": dict(nom=0.0486, down=0.04, up=0.07, min=0.03, max=0.08),
+    "eField": dict(nom=0.5, down=0.45, up=0.55, min=0.4, max=0.6),
+    "lifetime": dict(nom=2.2e3, down=500.0, up=5000.0, min=400.0, max=6000.0),
+    "vdrift": dict(nom=0.1596, down=0.1400, up=0.1800, min=0.13, max=0.19),
+    "long_diff": dict(nom=4.0e-6, down=2e-6, up=9e-6, min=1e-6, max=1e-5),
+    "tran_diff": dict(nom=8.8e-6, down=4e-6, up=14e-6, min=3e-6, max=15e-6),
+    "lArDensity": dict(nom=1.38, down=1.37, up=1.41, min=1.35, max=1.43),
+}
+
+
+def fit_options(fit_params, lr, initial, normalization_scheme="sigmoid", normalization_scale=1.0,
+                max_clip_norm_val=None, clip_from_range=False, betas=(0.9, 0.999), eps=1e-8, ranges=None):
+    """The LsimFitOptions block of one fit, with the reference's checks
+    (fit_params.py:255-264, :168-199).  ``lr`` is one learning rate or a
+    dict per parameter; ``initial`` the physical starting values (dict),
+    which set the divide scheme's params_normalization (:443)."""
+    if normalization_scheme not in _abi.NORM_SCHEMES:
+        raise ValueError(f"Unknown normalization_scheme '{normalization_scheme}'. Use one of: sigmoid, exp_log, divide")
+    scale = 1.0 if normalization_scheme == "divide" else float(normalization_scale)
+    if scale <= 0:
+        raise ValueError(f"normalization_scale_{normalization_scheme} must be > 0, got {normalization_scale}")
+    unknown = set(fit_params) - set(GRAD_PARAMS)
+    if unknown:
+        raise ValueError(f"cannot fit {sorted(unknown)}; fit parameters are {GRAD_PARAMS}")
+    rg = dict(RANGES, **(ranges or {}))
+    o = _abi.LsimFitOptions()
+    o.scheme = _abi.NORM_SCHEMES[normalization_scheme]
+    o.fit_mask = sum(1 << GRAD_PARAMS.index(k) for k in fit_params)
+    o.clip_from_range = int(bool(clip_from_range))
+    o.norm_scale = scale
+    o.max_clip_norm = float(max_clip_norm_val) if max_clip_norm_val is not None else 0.0
+    o.beta1, o.beta2, o.eps = float(betas[0]), float(betas[1]), float(eps)
+    for i, k in enumerate(GRAD_PARAMS):
+        r = rg[k]
+        o.lr[i] = (float(lr[k]) if isinstance(lr, dict) else float(lr)) if k in fit_params else 0.0
+        o.lo[i], o.hi[i], o.nom[i], o.down[i], o.up[i] = r["min"], r["max"], r["nom"], r["down"], r["up"]
+        v = float(initial[k])
+        o.norm[i] = v if v != 0.0 else 1.0
+        if k in fit_params and normalization_scheme == "exp_log" and r["nom"] <= 0:
+            raise ValueError(f"exp_log normalization requires positive nominal value for '{k}', got {r['nom']}")
+    return o
 
 
 class DeviceFit:
-    """Adam on ``fit_params`` (a subset of GRAD_PARAMS) against ``target``.
-
-    ``lr`` is the learning rate in normalised units (parameter / scale);
-    ``scale`` defaults to the nominal values of the reference's parameters.
+    """The reference's gradient-descent fit (Adam) of ``fit_params`` (a
+    subset of GRAD_PARAMS) against ``target``, with its normalisation
+    schemes ("sigmoid", the reference's default; "exp_log"; "divide"),
+    optional clip_by_global_norm (``max_clip_norm_val``) and
+    clip_values_from_range (``clip_from_range``, divide scheme).  ``lr`` is
+    the learning rate in normalised units, one value or a dict per
+    parameter; ``normalization_scale`` is normalization_scale_sigmoid or
+    normalization_scale_exp_log.
     """
 
     def __init__(self, params, response_template, tracks, fields, target: Target, fit_params=None, lr=1e-2,
-                 scale=None, betas=(0.9, 0.999), eps=1e-8, n_events=None, max_steps=1000):
+                 normalization_scheme="sigmoid", normalization_scale=1.0, max_clip_norm_val=None,
+                 clip_from_range=False, betas=(0.9, 0.999), eps=1e-8, n_events=None, max_steps=1000, ranges=None):
         self.lib = _abi.load()
         self.lut = sim.prepare_lut(response_template, params)
         self.fields = tuple(fields)
@@ -41,23 +97,20 @@ class DeviceFit:
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
         self.counts = torch.empty(16, dtype=torch.int32, device=dev)
         fit = tuple(fit_params) if fit_params is not None else tuple(k for k in GRAD_PARAMS if k != "vdrift")
-        unknown = set(fit) - set(GRAD_PARAMS)
-        if unknown:
-            raise ValueError(f"cannot fit {sorted(unknown)}; fit parameters are {GRAD_PARAMS}")
-        nominal = consts.Params()
-        sc = [abs(float(getattr(nominal, k))) if scale is None else float(scale[k]) for k in GRAD_PARAMS]
-        self.theta = torch.tensor([float(getattr(params, k)) for k in GRAD_PARAMS], dtype=torch.float32, device=dev)
-        self.scale = torch.tensor(sc, dtype=torch.float32, device=dev)
-        self.lr = torch.tensor([lr if k in fit else 0.0 for k in GRAD_PARAMS], dtype=torch.float32, device=dev)
-        self.state = torch.zeros(2 * _abi.NPARAM + 1, dtype=torch.float32, device=dev)
+        initial = {k: float(getattr(params, k)) for k in GRAD_PARAMS}
+        self.opts = fit_options(fit, lr, initial, normalization_scheme, normalization_scale, max_clip_norm_val,
+                                clip_from_range, betas, eps, ranges)
+        self.theta = torch.tensor([initial[k] for k in GRAD_PARAMS], dtype=torch.float32, device=dev)
+        self.state = torch.zeros(_abi.FIT_STATE, dtype=torch.float32, device=dev)
         self.out = torch.empty(1 + _abi.NPARAM, dtype=torch.float32, device=dev)
-        self.betas, self.eps = (float(betas[0]), float(betas[1])), float(eps)
         self.target = target
         self.max_steps = int(max_steps)
         self.loss_hist = torch.zeros(self.max_steps, dtype=torch.float32, device=dev)
         self.theta_hist = torch.zeros((self.max_steps, _abi.NPARAM), dtype=torch.float32, device=dev)
         self.step_idx = torch.zeros(1, dtype=torch.int64, device=dev)
         self.graph = None
+        _abi.check(self.lib, self.lib.lsim_fit_init(sim._ptr(self.theta), self.opts, sim._ptr(self.state),
+                                                    sim._stream()))
 
     def _launch(self):
         s = sim._stream()
@@ -73,8 +126,7 @@ class DeviceFit:
         self.loss_hist.index_copy_(0, idx, self.out[:1])
         self.theta_hist.index_copy_(0, idx, self.theta.unsqueeze(0))
         self.step_idx.add_(1)
-        _abi.check(lib, lib.lsim_adam_step(p(self.theta), p(self.out[1:]), p(self.scale), p(self.lr), p(self.state),
-                                           self.betas[0], self.betas[1], self.eps, s))
+        _abi.check(lib, lib.lsim_fit_step(p(self.theta), p(self.out[1:]), self.opts, p(self.state), s))
 
     def step(self):
         """One eager step (no graph)."""
@@ -97,8 +149,8 @@ class DeviceFit:
         return self.graph
 
     def run(self, n_steps, graph=True):
-        """n_steps Adam steps; returns (loss history, parameter history) of
-        all steps taken so far, as numpy arrays."""
+        """n_steps optimiser steps; returns (loss history, parameter history)
+        of all steps taken so far, as numpy arrays."""
         if graph and self.graph is None:
             self.capture()
         for _ in range(n_steps):
@@ -111,6 +163,10 @@ class DeviceFit:
     def history(self):
         n = min(int(self.step_idx.item()), self.max_steps)
         return self.loss_hist[:n].cpu().numpy(), self.theta_hist[:n].cpu().numpy()
+
+    def normalised(self):
+        """The current normalised parameters u (GRAD_PARAMS order)."""
+        return self.state[2 * _abi.NPARAM:3 * _abi.NPARAM].cpu().numpy()
 
     def params(self, params):
         """``params`` with the current fit values."""

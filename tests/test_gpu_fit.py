@@ -1,8 +1,10 @@
-"""Device-resident fit loop (optimize/fit_params.py:704-731, :872-895):
-the segment stage with device-side parameters, the gradient and an Adam
-update, captured in one CUDA graph.  The graph replays the eager
-trajectory exactly, the Adam kernel follows optax.adam in the "divide"
-normalisation, and a fit recovers hidden parameters."""
+"""Device-resident fit loop (optimize/fit_params.py:704-731, :781-895):
+the segment stage with device-side parameters, the gradient and the
+optimiser update, captured in one CUDA graph.  The graph replays the eager
+trajectory exactly; the fit step follows the reference's chain (the
+sigmoid, exp_log and divide normalisations, NaN skip, clip_by_global_norm,
+optax.adam, clip_values_from_range) restated below in float64; a fit with
+the reference's default settings recovers hidden parameters."""
 
 from __future__ import annotations
 
@@ -57,6 +59,105 @@ def test_adam_step_matches_optax_formula(cuda):
     assert torch.equal(t_th, before) and state[16].item() == 3
 
 
+# ---- the reference's fit step restated in float64 (fit_params.py:168-199, :833-895)
+
+def _sigmoid(x):
+    return 1.0 / (1.0 + np.exp(-x))
+
+
+def _to_phys(scheme, k, u, o):
+    if scheme == "sigmoid":
+        return o["lo"] + (o["hi"] - o["lo"]) * _sigmoid(k * u)
+    if scheme == "exp_log":
+        return o["nom"] * np.exp(k * u)
+    return u * o["norm"]
+
+
+def _dphys(scheme, k, u, o):
+    if scheme == "sigmoid":
+        s = _sigmoid(k * u)
+        return (o["hi"] - o["lo"]) * s * (1 - s) * k
+    if scheme == "exp_log":
+        return o["nom"] * np.exp(k * u) * k
+    return o["norm"]
+
+
+def _to_norm(scheme, k, v, o):
+    if scheme == "sigmoid":
+        eps = np.finfo(np.float32).eps
+        fr = np.clip((v - o["lo"]) / (o["hi"] - o["lo"]), eps, 1 - eps)
+        return np.log(fr / (1 - fr)) / k
+    if scheme == "exp_log":
+        return np.log(np.maximum(v, np.finfo(np.float32).tiny) / o["nom"]) / k
+    return np.where(v != 0, 1.0, 0.0)
+
+
+def _reference_fit(scheme, k, theta0, grads, mask, lr, o, max_norm=None, clip_range=False, b1=0.9, b2=0.999,
+                   eps=1e-8):
+    """Physical parameters after each step of optax.chain([clip_by_global_norm],
+    adam) on the normalised parameters, as GradientDescentFitter applies it."""
+    u = np.where(mask, _to_norm(scheme, k, theta0, o), 0.0)
+    theta = np.where(mask, _to_phys(scheme, k, u, o), theta0)
+    m = np.zeros(8)
+    v = np.zeros(8)
+    t = 0
+    out = []
+    for g_phys in grads:
+        g = np.where(mask, g_phys * _dphys(scheme, k, u, o), 0.0)
+        if np.isnan(g[mask]).any():
+            out.append(theta.copy())
+            continue
+        if scheme == "divide":
+            g = g * o["norm"]
+        if max_norm is not None:
+            gn = np.sqrt((g[mask] ** 2).sum())
+            if not gn < max_norm:
+                g = g / gn * max_norm
+        t += 1
+        m = b1 * m + (1 - b1) * g
+        v = b2 * v + (1 - b2) * g * g
+        upd = -lr * (m / (1 - b1 ** t)) / (np.sqrt(v / (1 - b2 ** t)) + eps)
+        u = np.where(mask, u + upd, u)
+        if scheme == "divide" and clip_range:
+            u = np.where(mask, np.maximum(o["down"] / o["norm"], np.minimum(o["up"] / o["norm"], u)), u)
+        theta = np.where(mask, _to_phys(scheme, k, u, o), theta0)
+        out.append(theta.copy())
+    return out
+
+
+@pytest.mark.parametrize("scheme,k,max_norm,clip_range", [("sigmoid", 1.0, None, False), ("sigmoid", 2.5, 0.5, False),
+                                                          ("exp_log", 1.0, None, False), ("exp_log", 0.7, 3.0, False),
+                                                          ("divide", 1.0, None, False), ("divide", 1.0, None, True)])
+def test_fit_step_matches_the_reference_chain(cuda, scheme, k, max_norm, clip_range):
+    from larndsim_gb300 import _abi, fit
+    from larndsim_gb300.grad import GRAD_PARAMS
+    lib = _abi.load()
+    rng = np.random.default_rng(3)
+    names = ("Ab", "kb", "eField", "lifetime", "tran_diff", "lArDensity")
+    mask = np.array([n in names for n in GRAD_PARAMS])
+    r = fit.RANGES
+    theta0 = np.array([r[n]["nom"] * (1 + 0.02 * rng.standard_normal()) for n in GRAD_PARAMS], np.float32)
+    lr = {n: float(rng.uniform(0.005, 0.05)) for n in names}
+    o = fit.fit_options(names, lr, dict(zip(GRAD_PARAMS, theta0.tolist())), scheme, k, max_norm, clip_range)
+    arr = {f: np.array(list(getattr(o, f)), np.float64) for f in ("lo", "hi", "nom", "norm", "down", "up", "lr")}
+    # gradients of a size that drives the divide scheme past its soft range
+    scale = np.array([1.0 / max(abs(float(x)), 1e-12) for x in theta0]) * (40.0 if clip_range else 1.0)
+    grads = [(rng.standard_normal(8) * scale).astype(np.float32) for _ in range(5)]
+    grads.insert(3, np.full(8, np.nan, np.float32))          # a NaN gradient skips its step
+    theta = torch.from_numpy(theta0.copy()).cuda()
+    state = torch.zeros(_abi.FIT_STATE, dtype=torch.float32, device="cuda")
+    _abi.check(lib, lib.lsim_fit_init(theta.data_ptr(), o, state.data_ptr(), None))
+    ref = _reference_fit(scheme, k, theta0.astype(np.float64), [g.astype(np.float64) for g in grads], mask,
+                            arr["lr"], arr, max_norm, clip_range)
+    for g, want in zip(grads, ref):
+        tg = torch.from_numpy(g).cuda()
+        _abi.check(lib, lib.lsim_fit_step(theta.data_ptr(), tg.data_ptr(), o, state.data_ptr(), None))
+        got = theta.cpu().numpy()
+        np.testing.assert_allclose(got[mask], want[mask], rtol=5e-6)
+        np.testing.assert_array_equal(got[~mask], theta0[~mask])     # not fitted: untouched
+    assert state[3 * 8].item() == len(grads) - 1                     # the NaN step left the count as it was
+
+
 def test_graph_replays_the_eager_trajectory(cuda, setup):
     from larndsim_gb300 import fit
     p, tmpl, tracks, fields, hidden, target = setup
@@ -70,13 +171,19 @@ def test_graph_replays_the_eager_trajectory(cuda, setup):
     assert la[0] > 0 and not np.array_equal(ta[0], ta[-1])
 
 
-def test_fit_recovers_hidden_parameters(cuda, setup):
+@pytest.mark.parametrize("scheme,lr,steps", [("sigmoid", 1e-2, 400), ("divide", 3e-3, 300)])
+def test_fit_recovers_hidden_parameters(cuda, setup, scheme, lr, steps):
+    """The reference's default settings (sigmoid normalisation, no clipping,
+    the learning rate of its example scripts) and the divide scheme.  The
+    sigmoid map spreads each parameter over its whole hard range, so the
+    same offsets are larger moves in its normalised units."""
     from larndsim_gb300 import fit
     from larndsim_gb300.grad import GRAD_PARAMS
     p, tmpl, tracks, fields, hidden, target = setup
     names = ("lifetime", "long_diff", "tran_diff")
-    f = fit.DeviceFit(p, tmpl, tracks, fields, target, fit_params=names, lr=3e-3, max_steps=400)
-    loss, th = f.run(300, graph=True)
+    f = fit.DeviceFit(p, tmpl, tracks, fields, target, fit_params=names, lr=lr, normalization_scheme=scheme,
+                      max_steps=steps + 8)
+    loss, th = f.run(steps, graph=True)
     assert loss[-1] < 0.05 * loss[0]
     for k in names:
         i = GRAD_PARAMS.index(k)

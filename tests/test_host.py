@@ -291,3 +291,14 @@ def test_noalloc_refuses_sizes_beyond_its_scratch_before_any_cuda_call(lib):
     p.max_adc_values = 0
     assert lib.lsim_hits_noalloc(p, ph, ph, ph, 4, 1997, *([ph] * 8), ph, None) == _abi.LSIM_ERR_INVALID
     assert lib.lsim_hits(p, ph, ph, ph, 4, 1997, *([ph] * 8), ph, ph, 1 << 20, None) == _abi.LSIM_ERR_INVALID
+
+
+def test_fit_options_follow_the_reference_checks():
+    from larndsim_gb300 import fit
+    init = {k: v["nom"] for k, v in fit.RANGES.items()}
+    with pytest.raises(ValueError, match="Unknown normalization_scheme"):
+        fit.fit_options(("Ab",), 0.1, init, "linear")
+    with pytest.raises(ValueError, match="must be > 0"):
+        fit.fit_options(("Ab",), 0.1, init, "sigmoid", 0.0)
+    with pytest.raises(ValueError, match="cannot fit"):
+        fit.fit_options(("shift_x",), 0.1, init)
