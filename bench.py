@@ -669,7 +669,7 @@ def run_prob(args):
                                 "HBM traffic is the waveform read only"},
            "gpu_launches": 2 * args.steps, "clocks": clk,
            "fwd_bwd": {"ms": fb_ms, "pixels_per_s": P / (fb_ms * 1e-3),
-                       "note": "forward with the step paths recorded + lsim_fee_prob_vjp (per-tick reverse pass), "
+                       "note": "forward with the step paths recorded + lsim_fee_prob_vjp (reverse pass per tick class), "
                                "cotangents on the expected tick, ADC and hit probability"}}
     if not args.no_cpu_baseline:
         from oracle import reference_np as R

@@ -549,17 +549,33 @@ struct ProbVjpArgs {
   float *g_wfs;                // [n_pix][T]
 };
 
+// Ticks are grouped into classes as in the forward, here by the five
+// values a tick's hit and dist terms read (the running maximum at t and
+// t + 1, q at t, t + 1 and at the shifted tick; the selection value is not
+// differentiated).  Within a class every per-path partial derivative is the
+// same; the per-tick cotangents (on the hit log-probability and on the dist
+// value) enter linearly, so the partials are evaluated once per class and
+// path, folded into seven per-class coefficients, and spread back to the
+// class's ticks with the ticks' own cotangents.  Classes are also cut at
+// every kVjpSpan ticks, so the per-class loops over ticks stay short (flat
+// stretches of a waveform are long).
+constexpr int kVjpSpan = 16;
+constexpr int kVjpArrays = 16;   // q, running max, esperance, soft-where weight, 5 accumulators, dist and hit
+                                 // cotangents, class hit and dist values, scratch, class, representative
+
 __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va) {
   extern __shared__ __align__(16) float sm[];
   const ProbArgs &a = va.f;
   float *qs = sm, *cm = qs + kProbMaxT, *esp = cm + kProbMaxT, *sw = esp + kProbMaxT;
   float *Aq0 = sw + kProbMaxT, *Aqs = Aq0 + kProbMaxT, *Am0 = Aqs + kProbMaxT, *Am1 = Am0 + kProbMaxT;
-  float *Aesp = Am1 + kProbMaxT, *Gd = Aesp + kProbMaxT, *tmp = Gd + kProbMaxT;
-  float *part = tmp + kProbMaxT;   // [warps][2][kProbMaxPaths]
+  float *Aesp = Am1 + kProbMaxT, *Gd = Aesp + kProbMaxT, *Gh = Gd + kProbMaxT;
+  float *vh = Gh + kProbMaxT, *vd = vh + kProbMaxT, *tmp = vd + kProbMaxT;
+  int *cls = reinterpret_cast<int *>(tmp + kProbMaxT), *rep = cls + kProbMaxT;
+  float *part = reinterpret_cast<float *>(rep + kProbMaxT);   // [warps][2][kProbMaxPaths]
   __shared__ float red[kProbThreads / 32];
   __shared__ float pc[kProbMaxPaths], plp[kProbMaxPaths], glp_n[kProbMaxPaths], gc_n[kProbMaxPaths];
   __shared__ int pskip[kProbMaxPaths], ptop[kProbMaxPaths];
-  __shared__ int n_exec;
+  __shared__ int n_exec, n_cls;
 
   const LsimParams &p = a.p;
   const int T = a.T, K = a.K, H = p.max_adc_values, tid = threadIdx.x;
@@ -589,15 +605,34 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
     __syncthreads();
     block_scan_row<kScanMax>(cm, T, red);
     for (int t = tid; t < T - 1; t += kProbThreads) {
-      const float e = (qs[shifted(t)] + thr) - 0.5f * (qs[t + 1] + qs[t]);
+      const int s = shifted(t);
+      const float e = (qs[s] + thr) - 0.5f * (qs[t + 1] + qs[t]);
       esp[t] = e;
       sw[t] = sigmoid_f((e - thr) * 10.0f);
+      bool head = t % kVjpSpan == 0;
+      if (!head) {
+        const int sp = shifted(t - 1);
+        auto ne = [](float x, float y) { return __float_as_uint(x) != __float_as_uint(y); };
+        head = ne(cm[t], cm[t - 1]) || ne(cm[t + 1], cm[t]) || ne(qs[t], qs[t - 1]) || ne(qs[t + 1], qs[t]) ||
+               ne(qs[s], qs[sp]);
+      }
+      tmp[t] = head ? 1.0f : 0.0f;
+    }
+    __syncthreads();
+    block_scan_row<kScanSum>(tmp, T - 1, red);   // integer counts, exact in float32
+    for (int t = tid; t < T - 1; t += kProbThreads) {
+      const int u = (int)tmp[t] - 1;
+      cls[t] = u;
+      if (t == 0 || (int)tmp[t - 1] != u + 1) rep[u] = t;
+      if (t == T - 2) n_cls = u + 1;
     }
     if (tid < K) {
       glp_n[tid] = 0.f;
       gc_n[tid] = 0.f;
     }
     __syncthreads();
+    const int U = n_cls;
+    if (tid == 0) rep[U] = T - 1;     // end of the last class
 
     for (int h = n_exec - 1; h >= 0; --h) {
       // step h's input paths and selected ticks, recorded by the forward
@@ -624,13 +659,13 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
         }
       }
       __syncthreads();
-      // ---- pass 1: hit and dist log-sum-exps per tick
-      float hitv[kProbTicks], distv[kProbTicks];
+      // ---- pass 1: hit and dist log-sum-exps per class
 #pragma unroll
       for (int i = 0; i < kProbTicks; ++i) {
-        float hm = -INFINITY, hs = 0.f, dm = -INFINITY, ds = 0.f;
-        const int t = tid + i * kProbThreads;
-        if (t < T - 1) {
+        const int u = tid + i * kProbThreads;
+        if (u < U) {
+          float hm = -INFINITY, hs = 0.f, dm = -INFINITY, ds = 0.f;
+          const int t = rep[u];
           const int sidx = shifted(t);
           for (int k = 0; k < K; ++k) {
             if (pskip[k]) continue;
@@ -649,25 +684,23 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
             lse_add(hm, hs, le + lp);
             lse_add(dm, ds, lg + lp);
           }
-          hitv[i] = lse_final(hm, hs);
-          distv[i] = lse_final(dm, ds);
-        } else {
-          hitv[i] = distv[i] = 0.f;
+          vh[u] = lse_final(hm, hs);
+          vd[u] = lse_final(dm, ds);
         }
       }
+      __syncthreads();
       // ---- cotangents of the step's outputs on each tick
-      float ghit[kProbTicks], pr[kProbTicks];
       float l_sum = 0.f, t_sum = 0.f, a_sum = 0.f;
+      float pr[kProbTicks];
 #pragma unroll
       for (int i = 0; i < kProbTicks; ++i) {
         const int t = tid + i * kProbThreads;
-        ghit[i] = 0.f;
         pr[i] = 0.f;
         if (t < T - 1) {
           const int64_t o = (pix * H + h) * (int64_t)(T - 1) + t;
-          if (va.g_log_prob) ghit[i] = va.g_log_prob[o];
+          Gh[t] = va.g_log_prob ? va.g_log_prob[o] : 0.f;
           if (va.g_charge) Aesp[t] += va.g_charge[o];
-          pr[i] = expf(hitv[i]);
+          pr[i] = expf(vh[cls[t]]);
           l_sum += pr[i];
           t_sum += (float)t * pr[i];
           a_sum += digitize(p, esp[t]) * pr[i];
@@ -690,26 +723,45 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
           if (t < T - 1) {
             const float adc = digitize(p, esp[t]);
             const float gp = gl + gt * (float)t / den + ga * adc / den + on * gden;
-            ghit[i] += gp * pr[i];
+            Gh[t] += gp * pr[i];
             Aesp[t] += digitize_vjp(p, esp[t], ga * pr[i] / den);
           }
         }
       }
-      float gdist[kProbTicks];
+      __syncthreads();
+      // ---- per class: sums of the ticks' cotangents
+      float Hs[kProbTicks], Ds[kProbTicks];
+      bool anyH[kProbTicks], anyD[kProbTicks];
 #pragma unroll
       for (int i = 0; i < kProbTicks; ++i) {
-        const int t = tid + i * kProbThreads;
-        gdist[i] = t < T - 1 ? Gd[t] : 0.f;
+        const int u = tid + i * kProbThreads;
+        Hs[i] = Ds[i] = 0.f;
+        anyH[i] = anyD[i] = false;
+        if (u < U)
+          for (int t = rep[u]; t < rep[u + 1]; ++t) {
+            const float gh = Gh[t], gd = Gd[t];
+            Hs[i] += gh;
+            Ds[i] += gd;
+            anyH[i] |= gh != 0.f;
+            anyD[i] |= gd != 0.f;
+          }
       }
-      // ---- pass 2: derivatives per tick and path
+      // ---- pass 2: the partials per class and path, folded into seven
+      // per-class coefficients of the ticks' (hit, dist) cotangents
+      float co[kProbTicks][7];
+#pragma unroll
+      for (int i = 0; i < kProbTicks; ++i)
+#pragma unroll
+        for (int j = 0; j < 7; ++j) co[i][j] = 0.f;
       for (int k = 0; k < K; ++k) {
         float glp = 0.f, gc = 0.f;
         if (!pskip[k]) {
           const float c = pc[k], lp = plp[k];
 #pragma unroll
           for (int i = 0; i < kProbTicks; ++i) {
-            const int t = tid + i * kProbThreads;
-            if (t >= T - 1 || (ghit[i] == 0.f && gdist[i] == 0.f)) continue;
+            const int u = tid + i * kProbThreads;
+            if (u >= U || !(anyH[i] || anyD[i])) continue;
+            const int t = rep[u];
             const int sidx = shifted(t);
             const float zm0 = ((cm[t] - c) - thr) * z, zm1 = ((cm[t + 1] - c) - thr) * z;
             const float LM0 = log_ndtr_f(zm0), LM1 = log_ndtr_f(zm1);
@@ -725,22 +777,22 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
             const float le2 = kProbFloor + softplus_f(le1 - kProbFloor);
             const float wt = sw[t];
             const float le = wt * le2 + (1.0f - wt) * kProbFloor;
-            const float al = ghit[i] != 0.f ? expf((le + lp) - hitv[i]) : 0.f;
-            const float be = gdist[i] != 0.f ? expf((lg + lp) - distv[i]) : 0.f;
-            const float g_le = ghit[i] * al;
-            glp += g_le + gdist[i] * be;
-            // le = w le2 + (1 - w)(-1000); w = sigmoid((esp - thr) 10)
-            Aesp[t] += g_le * (le2 - kProbFloor) * wt * (1.0f - wt) * 10.0f;
-            const float g_le1 = g_le * wt * sigmoid_f(le1 - kProbFloor);
+            // d(hit log-sum-exp)/d(le + lp) and d(dist log-sum-exp)/d(lg + lp)
+            const float al = anyH[i] ? expf((le + lp) - vh[u]) : 0.f;
+            const float be = anyD[i] ? expf((lg + lp) - vd[u]) : 0.f;
+            glp += al * Hs[i] + be * Ds[i];
+            // per unit hit cotangent: le = w le2 + (1 - w)(-1000), w = sigmoid((esp - thr) 10)
+            const float gl1 = al * wt * sigmoid_f(le1 - kProbFloor);
             const float s_lep = lep < lg ? 1.f : (lep == lg ? 0.5f : 0.f);
-            const float g_lep = g_le1 * s_lep, g_lg = g_le1 * (1.f - s_lep) + gdist[i] * be;
-            const float gzqs = g_lep * g_qs, gzq0 = g_lep * g_q0;
-            const float gzm1 = g_lg * g_m1, gzm0 = g_lg * g_m0;
-            Aq0[t] += gzq0 * z;
-            Aqs[t] += gzqs * z;
-            Am0[t] += gzm0 * z;
-            Am1[t] += gzm1 * z;
-            gc -= (gzq0 + gzqs + gzm0 + gzm1) * z;
+            const float hl = gl1 * s_lep, hg = gl1 * (1.f - s_lep);
+            co[i][0] += hl * g_q0 * z;
+            co[i][1] += hl * g_qs * z;
+            co[i][2] += hg * g_m0 * z;
+            co[i][3] += be * g_m0 * z;
+            co[i][4] += hg * g_m1 * z;
+            co[i][5] += be * g_m1 * z;
+            co[i][6] += al * (le2 - kProbFloor) * wt * (1.0f - wt) * 10.0f;
+            gc -= (Hs[i] * (hl * (g_q0 + g_qs) + hg * (g_m0 + g_m1)) + Ds[i] * be * (g_m0 + g_m1)) * z;
           }
         }
         glp = warp_sum(glp);
@@ -748,6 +800,20 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
         if (lane == 0) {
           part[(wid * 2) * kProbMaxPaths + k] = glp;
           part[(wid * 2 + 1) * kProbMaxPaths + k] = gc;
+        }
+      }
+      // spread the coefficients to the class's ticks with their cotangents
+#pragma unroll
+      for (int i = 0; i < kProbTicks; ++i) {
+        const int u = tid + i * kProbThreads;
+        if (u >= U || !(anyH[i] || anyD[i])) continue;
+        for (int t = rep[u]; t < rep[u + 1]; ++t) {
+          const float gh = Gh[t], gd = Gd[t];
+          Aq0[t] += gh * co[i][0];
+          Aqs[t] += gh * co[i][1];
+          Am0[t] += gh * co[i][2] + gd * co[i][3];
+          Am1[t] += gh * co[i][4] + gd * co[i][5];
+          Aesp[t] += gh * co[i][6];
         }
       }
       __syncthreads();
@@ -879,7 +945,7 @@ int run_fee_prob_vjp(const LsimParams &p, const float *wfs, int64_t n_pix, int32
   va.g_e_adc = g_e_adc;
   va.g_lam = g_lam;
   va.g_wfs = g_wfs;
-  const size_t smem = sizeof(float) * (11 * kProbMaxT + 2 * (kProbThreads / 32) * kProbMaxPaths);
+  const size_t smem = sizeof(float) * ((kVjpArrays + 1) * kProbMaxT + 2 * (kProbThreads / 32) * kProbMaxPaths);
   if (cudaFuncSetAttribute(k_fee_prob_vjp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return LSIM_ERR_CUDA;
   int per_sm = 0;

@@ -87,10 +87,31 @@ def _functional(p, w, top, n_exec, gl, gq, red):
     return val
 
 
-@pytest.mark.parametrize("kind", ["reductions", "distributions"])
-def test_fee_prob_vjp_matches_frozen_fd(cuda, case, kind):
-    p, w = case
-    rng = np.random.default_rng(11 if kind == "reductions" else 12)
+@pytest.fixture(scope="module")
+def case_flat():
+    """Rows as simulated, with their flat stretches (no charge arriving):
+    long runs of ticks with identical inputs, which the adjoint evaluates
+    once per run."""
+    from larndsim_gb300 import workloads
+    from oracle import reference_np as R
+    p = small_params(n_neighbors=1, RESET_NOISE_CHARGE=900)
+    tmpl = R.load_lut_templates(workloads.synthetic_response(seed=0, nx=25, ny=25), p)
+    tracks, fields = workloads.muon_event(seed=8, n_tracks=3)
+    w, u = R.simulate_wfs(p, tmpl, tracks, fields, history={})
+    w = w[u >= 0][:12]
+    assert (w == 0).mean() > 0.5
+    return p, w.astype(np.float32)
+
+
+@pytest.mark.parametrize("kind", ["reductions", "distributions", "reductions-flat", "distributions-flat"])
+def test_fee_prob_vjp_matches_frozen_fd(cuda, case, case_flat, kind):
+    """On flat rows the perturbations leave the flat stretches flat (zero
+    where the row is zero), so tied running maxima stay tied and the
+    direction does not depend on how their cotangent is shared."""
+    flat = kind.endswith("-flat")
+    kind = kind.replace("-flat", "")
+    p, w = case_flat if flat else case
+    rng = np.random.default_rng((11 if kind == "reductions" else 12) + (100 if flat else 0))
     P, T = w.shape
     H = int(p.MAX_ADC_VALUES)
     gl = gq = red = None
@@ -105,7 +126,7 @@ def test_fee_prob_vjp_matches_frozen_fd(cuda, case, kind):
     assert n_exec >= 2 and np.all(np.isfinite(g))
     w64 = w.astype(np.float64)
     for d in range(3):
-        delta = rng.standard_normal(w.shape)
+        delta = rng.standard_normal(w.shape) * (w != 0 if flat else 1.0)
         eps = 1e-2
         fp = _functional(p, w64 + eps * delta, top, n_exec, gl, gq, red)
         fm = _functional(p, w64 - eps * delta, top, n_exec, gl, gq, red)
