@@ -38,6 +38,7 @@ Usage: python tests/golden/make_grad_golden.py /path/to/larnd-sim-jax   (or LARN
 """
 
 import json
+import os
 import sys
 import tempfile
 from pathlib import Path
@@ -61,6 +62,8 @@ CASES = {
                                 n_templates=10, lut=15, theta_seed=1),
     "grad_two_events_box_n2": dict(event=("two_events", dict(seed=62)), n=2, L=150, mode="BOX", n_templates=12,
                                    lut=25, theta_seed=2),
+    "grad_muons_birks_n4": dict(event=("muon", dict(seed=64, n_tracks=2)), n=4, L=150, mode="BIRKS",
+                                n_templates=10, lut=45, theta_seed=4),
 }
 
 
@@ -68,10 +71,18 @@ def main():
     C, F, S, base = load_reference(x64=True)
     import jax.numpy as jnp
 
+    # GRAD_GOLDEN_CASES (comma-separated) regenerates only those cases and
+    # keeps the others of an existing file
+    only = [c for c in os.environ.get("GRAD_GOLDEN_CASES", "").split(",") if c]
     out = {}
+    if only and OUT.exists():
+        with np.load(OUT) as old:
+            out = {k: old[k] for k in old.files if k.split("/")[0] not in only}
     tmp = Path(tempfile.mkdtemp())
     borders32 = np.asarray(base.tpc_borders, np.float32).astype(np.float64)
     for name, case in CASES.items():
+        if only and name not in only:
+            continue
         nodes = consts.jax_linspace_f32(0.001, 10, case["n_templates"]).astype(np.float64)
         p0 = base.replace(long_diff_template=jnp.asarray(nodes), tpc_borders=jnp.asarray(borders32),
                           number_pix_neighbors=case["n"], signal_length=case["L"], time_window=case["L"],

@@ -23,8 +23,8 @@ tolerances of tests/test_gpu_fee_prob.py.  The gradient
 (tests/golden/grad_ref.npz, tests/golden/make_grad_golden.py: central
 differences of the reference's own chain in float64 at fixed decisions)
 is compared as the vector-Jacobian product for the reference's cotangent,
-within 2e-4 relative per component (the GPU-against-oracle bound of
-tests/test_gpu_grad.py, 1e-4, plus the oracle's observed 4.3e-5).  The fit losses
+within 1e-4 relative per component (the gradient tolerance of the
+reference-parity contract), at number_pix_neighbors 1, 2 and 4.  The fit losses
 (tests/golden/loss_ref.npz, tests/golden/make_loss_golden.py) are compared
 at the tolerances of tests/test_gpu_losses.py: values within 1e-5
 relative, gradients within 1e-4 of the largest central difference.
@@ -176,11 +176,14 @@ def test_cuda_gradient_matches_reference_central_differences(cuda, name):
         pytest.skip("the GPU's float32 forward took another crossing decision than the reference's 32-bit run")
     cot = torch.from_numpy(ggold[f"{name}/cotangent"].astype(np.float32)).cuda()
     got = dict(zip(grad.GRAD_PARAMS, [float(v) for v in chain.vjp(p, cot)]))
+    worst = 0.0
     for k, r in zip(cfg["grad_params"], ggold[f"{name}/fd_vjp"]):
         if r == 0.0:
             assert got[k] == 0.0, k
         else:
-            assert abs(got[k] - r) <= 2e-4 * abs(r), (k, got[k], r)
+            worst = max(worst, abs(got[k] - r) / abs(r))
+            assert abs(got[k] - r) <= 1e-4 * abs(r), (k, got[k], r)
+    print(f"\n{name}: largest relative deviation from the reference's float64 central differences {worst:.2e}")
 
 
 @pytest.mark.parametrize("name", ["mse_adc", "chamfer_3d", "nll_loss"])
