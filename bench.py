@@ -299,6 +299,9 @@ def run_ours(args):
     # ---- the plain forward drop-in on the same batch (after the timed region)
     fwd, (wfs_f, unique_f) = lut_forward_record(args, params, tmpl, tracks, fields, dev, flush)
     rec["forward"] = fwd
+    # ---- the one-event plain forward (12 muons, about 900 segments): launch-
+    # and sync-bound, reported for the configuration the reference runs on CPU
+    rec["forward_one_event"] = one_event_forward_record(params, tmpl, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rec["cpu_baseline"] = cpu_baseline(tracks, fields, params, pp, resp, sample_events=1)
         # the oracle reads the template bank the GPU built (the builder itself is
@@ -768,6 +771,42 @@ def lut_forward_record(args, params, tmpl, tracks, fields, dev, flush):
                        "algorithmic_bytes": int(algo), "kernel_ms": k_ms, "pixels": n_valid,
                        "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None}
     return rec, (wfs, unique)
+
+
+def one_event_forward_record(params, tmpl, dev, reps=20):
+    """simulate_wfs + simulate_stochastic on one event of 12 straight muons
+    cut into 0.4 cm segments (about 900 segments), through the public
+    functions with the reference's host synchronisation points: median
+    device-inclusive wall time per call with the tracks on the device, and
+    e2e from pinned host tracks to host hits."""
+    import torch
+    from larndsim_gb300 import sim, workloads
+    tracks, fields = workloads.muon_event(seed=0, n_tracks=12)
+    t_dev = torch.from_numpy(tracks).to(dev)
+    host = torch.from_numpy(tracks).pin_memory()
+
+    def call(tr):
+        wfs, unique = sim.simulate_wfs(params, tmpl, tr, fields)
+        return sim.simulate_stochastic(params, wfs, unique)
+
+    for _ in range(3):
+        call(t_dev)
+    torch.cuda.synchronize()
+    dev_s, e2e_s = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out = call(t_dev)
+        torch.cuda.synchronize()
+        dev_s.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        out = [o.cpu() for o in call(host.to(dev, non_blocking=True))]
+        e2e_s.append(time.perf_counter() - t0)
+    ms, e2e_ms = 1e3 * float(np.median(dev_s)), 1e3 * float(np.median(e2e_s))
+    n = int(tracks.shape[0])
+    return {"workload": f"one event, 12 straight muons, {n} segments, n_neighbors=4, L=150, full template bank",
+            "segments": n, "ms": ms, "segments_per_s": n / (ms * 1e-3), "e2e_ms": e2e_ms,
+            "e2e_segments_per_s": n / (e2e_ms * 1e-3), "hits": int(out[0].shape[0]),
+            "timing": "host wall clock per call (median of 20), the call's own device-to-host syncs included"}
 
 
 def run_forward(args, param_mode=False):
