@@ -302,11 +302,19 @@ def run_ours(args):
     # ---- the one-event plain forward (12 muons, about 900 segments): launch-
     # and sync-bound, reported for the configuration the reference runs on CPU
     rec["forward_one_event"] = one_event_forward_record(params, tmpl, dev)
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rec["cpu_baseline"] = cpu_baseline(tracks, fields, params, pp, resp, sample_events=1)
+    cpu_leg = rank == 0 and world == 1 and not args.no_cpu_baseline
+    if cpu_leg:
         # the oracle reads the template bank the GPU built (the builder itself is
         # compared with the oracle's load_lut in the tests)
         rec["parity"] = forward_parity(params, tmpl.cpu().numpy(), tracks, fields, wfs_f, unique_f)
+    del wfs_f, unique_f
+    if world == 1:
+        # ---- the one-event 500k-segment shower, recompute and store variants
+        rec["large_event"] = large_event_record(params, tmpl, dev)
+        # ---- the fit loop with the reference's default flags (200 steps)
+        rec["fit_loop"] = fit_loop_record(params, tmpl, dev)
+    if cpu_leg:
+        rec["cpu_baseline"] = cpu_baseline(tracks, fields, params, pp, resp, sample_events=8)
     if rank == 0:
         print(json.dumps(rec), flush=True)
     if pg:
@@ -773,6 +781,45 @@ def lut_forward_record(args, params, tmpl, tracks, fields, dev, flush):
     return rec, (wfs, unique)
 
 
+def large_event_record(params, tmpl, dev, reps=5):
+    """Forward + adjoint of the SSE-ADC loss on one 500k-segment shower
+    event (40 sub-tracks): the recomputing adjoint (waveforms never stored)
+    against the store-the-waveforms variant, device time per gradient call
+    (CUDA events around stage 1 + the gradient call) and peak device memory
+    of each: the bytes torch's allocator held for this event at its peak
+    (tracks, stage-1 workspace, transient buffers of the call) above what
+    was resident before, plus the template bank it reads."""
+    import torch
+    from larndsim_gb300 import grad, workloads
+    tracks, fields = workloads.large_shower_event(seed=0, n_segments=500_000, n_subtracks=40)
+    torch.cuda.synchronize()
+    resident = torch.cuda.memory_allocated(dev)
+    bank = tmpl.numel() * tmpl.element_size()
+    chain = grad.LUTChain(params, tmpl, torch.from_numpy(tracks).to(dev), fields)
+    target = chain.target(params)
+    pp = perturbed(params)
+    out = {"workload": f"one shower event, {tracks.shape[0]} segments around 40 sub-tracks, n_neighbors=4, L=150",
+           "segments": int(tracks.shape[0])}
+    for name, fn in (("recompute", lambda: chain.loss_and_grad_device(pp, target)),
+                     ("store", lambda: chain.loss_and_grad_stored(pp, target))):
+        fn()
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats(dev)
+        before = torch.cuda.memory_allocated(dev)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for a, b in ev:
+            a.record()
+            fn()
+            b.record()
+        torch.cuda.synchronize()
+        ms = float(np.median([a.elapsed_time(b) for a, b in ev]))
+        out[name] = {"ms": ms, "segments_per_s": tracks.shape[0] / (ms * 1e-3),
+                     "peak_device_bytes": int(torch.cuda.max_memory_allocated(dev) - resident + bank),
+                     "call_transient_bytes": int(torch.cuda.max_memory_allocated(dev) - before)}
+    out["pixels"] = int(chain._stage.n_valid)
+    return out
+
+
 def one_event_forward_record(params, tmpl, dev, reps=20):
     """simulate_wfs + simulate_stochastic on one event of 12 straight muons
     cut into 0.4 cm segments (about 900 segments), through the public
@@ -874,26 +921,20 @@ def run_forward(args, param_mode=False):
 FIT_EVENTS, FIT_SEGMENTS, FIT_STEPS, FIT_LR, FIT_SEED = 32, 20_000, 200, 1e-3, 77
 
 
-def run_fit(args):
+def fit_loop_record(params, tmpl, dev, steps=FIT_STEPS):
     """The fit loop of the reference's GradientDescentFitter with its default
     flags (sigmoid normalisation, optax.adam, no clipping; optimize/
-    fit_params.py:781-895, example_run.py) on 32 events x 20k segments: 200
-    steps on the 7 parameters the loss depends on (vdrift does not enter),
-    target simulated at hidden parameters drawn from N(nominal, 5 %) inside
-    the ranges.  value: steps/s of the device-resident loop (stage 1,
-    forward + adjoint, optimiser update replayed as one CUDA graph per
-    step); e2e: pinned host tracks in, the fit set up, 200 steps, the final
-    parameters read back."""
+    fit_params.py:781-895, example_run.py) on 32 events x 20k segments:
+    ``steps`` steps on the 7 parameters the loss depends on (vdrift does not
+    enter), target simulated at hidden parameters drawn from N(nominal, 5 %)
+    inside the ranges.  Device steps/s of the loop (stage 1, forward +
+    adjoint, optimiser update replayed as one CUDA graph per step) and e2e
+    (pinned host tracks in, the fit set up, the steps, the final parameters
+    read back)."""
     import torch
-    from larndsim_gb300 import fit, grad, sim, workloads
+    from larndsim_gb300 import fit, grad, workloads
     from larndsim_gb300.grad import GRAD_PARAMS
-    rank, world, local = dist_env()
-    if rank != 0:
-        return
-    torch.cuda.set_device(local)
     names = tuple(k for k in GRAD_PARAMS if k != "vdrift")
-    params = nominal_params()
-    tmpl, params = sim.load_lut(workloads.synthetic_response(seed=0), params)
     tracks, fields = workloads.batched_events(seed=FIT_SEED, n_events=FIT_EVENTS, min_segments=FIT_SEGMENTS,
                                               max_segments=FIT_SEGMENTS + 1)
     rng = np.random.default_rng(FIT_SEED)
@@ -902,12 +943,12 @@ def run_fit(args):
         r = fit.RANGES[k]
         hid[k] = float(np.clip(float(getattr(params, k)) * (1.0 + 0.05 * rng.standard_normal()), r["down"], r["up"]))
     hidden = params.replace(**hid)
-    t_dev = torch.from_numpy(tracks).cuda()
+    t_dev = torch.from_numpy(tracks).to(dev)
     target = grad.LUTChain(params, tmpl, t_dev, fields).target(hidden)
 
     def make(tr):
         return fit.DeviceFit(params, tmpl, tr, fields, target, fit_params=names, lr=FIT_LR,
-                             normalization_scheme="sigmoid", max_steps=FIT_STEPS + 8)
+                             normalization_scheme="sigmoid", max_steps=steps + 8)
 
     f = make(t_dev)
     f.capture()
@@ -915,37 +956,55 @@ def run_fit(args):
     clocks = ClockSampler(torch.cuda.current_device())
     torch.cuda.synchronize()
     start.record()
-    for _ in range(FIT_STEPS):
+    for _ in range(steps):
         f.graph.replay()
     end.record()
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms = start.elapsed_time(end) / FIT_STEPS
+    ms = start.elapsed_time(end) / steps
     loss, th = f.history()
     err = {k: float(th[-1, GRAD_PARAMS.index(k)] / hid[k] - 1.0) for k in names}
     err0 = {k: float(float(getattr(params, k)) / hid[k] - 1.0) for k in names}
     host = torch.from_numpy(tracks).pin_memory()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    g = make(host.to("cuda", non_blocking=True))
-    g.run(FIT_STEPS, graph=True)
+    g = make(host.to(dev, non_blocking=True))
+    g.run(steps, graph=True)
     final = g.theta.cpu()
     e2e_s = time.perf_counter() - t0
-    rec = {"metric": "fit steps/s", "value": 1e3 / ms, "unit": "steps/s", "n_gpus": 1, "steps": FIT_STEPS,
-           "warmup": 1, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f32", "data": "synthetic (seeded tracks and LUT)",
-           "config": {"workload": f"GradientDescentFitter loop, {FIT_EVENTS} events x {FIT_SEGMENTS} segments "
-                                  f"({tracks.shape[0]} segments), n_neighbors=4, L=150, 100x45x45x1950 templates, "
-                                  f"SSE-ADC loss, 7 parameters, sigmoid normalisation, Adam lr {FIT_LR}",
-                      "segments": int(tracks.shape[0]),
-                      "step": "stage 1 + forward + adjoint + optimiser update, one CUDA graph replay per step",
+    return {"workload": f"GradientDescentFitter loop, {FIT_EVENTS} events x {FIT_SEGMENTS} segments "
+                        f"({tracks.shape[0]} segments), n_neighbors=4, L=150, 100x45x45x1950 templates, SSE-ADC "
+                        f"loss, 7 parameters, sigmoid normalisation, Adam lr {FIT_LR}, {steps} steps",
+            "segments": int(tracks.shape[0]), "steps": steps, "ms_per_step": ms, "steps_per_s": 1e3 / ms,
+            "step": "stage 1 + forward + adjoint + optimiser update, one CUDA graph replay per step",
+            "loss_first": float(loss[0]), "loss_last": float(loss[-1]),
+            "start_rel_error": err0, "final_rel_error": err,
+            "e2e": {"steps_per_s": steps / e2e_s, "seconds": e2e_s, "h2d_bytes": int(tracks.nbytes)},
+            "final_theta": [float(x) for x in final], "clocks": clk}
+
+
+def run_fit(args):
+    """``fit_loop_record`` as its own line (metric fit steps/s)."""
+    import torch
+    from larndsim_gb300 import sim, workloads
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    params = nominal_params()
+    tmpl, params = sim.load_lut(workloads.synthetic_response(seed=0), params)
+    r = fit_loop_record(params, tmpl, dev)
+    rec = {"metric": "fit steps/s", "value": r["steps_per_s"], "unit": "steps/s", "n_gpus": 1, "steps": r["steps"],
+           "warmup": 1, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tracks and LUT)",
+           "config": {"workload": r["workload"], "segments": r["segments"], "step": r["step"],
                       "l2": "inputs and work set larger than L2"},
-           "fit": {"loss_first": float(loss[0]), "loss_last": float(loss[-1]),
-                   "start_rel_error": err0, "final_rel_error": err},
-           "e2e": {"value": FIT_STEPS / e2e_s, "unit": "steps/s", "seconds": e2e_s,
-                   "h2d_bytes_per_step": int(tracks.nbytes) // FIT_STEPS, "d2h_bytes_per_step": 4 * 8 // FIT_STEPS},
-           "gpu_launches": (KERNELS_PER_STEP + 1) * FIT_STEPS, "clocks": clk,
-           "final_theta": [float(x) for x in final]}
+           "fit": {k: r[k] for k in ("loss_first", "loss_last", "start_rel_error", "final_rel_error")},
+           "e2e": {"value": r["e2e"]["steps_per_s"], "unit": "steps/s", "seconds": r["e2e"]["seconds"],
+                   "h2d_bytes_per_step": r["e2e"]["h2d_bytes"] // r["steps"], "d2h_bytes_per_step": 0},
+           "gpu_launches": (KERNELS_PER_STEP + 1) * r["steps"], "clocks": r["clocks"],
+           "final_theta": r["final_theta"]}
     print(json.dumps(rec), flush=True)
 
 
