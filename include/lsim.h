@@ -530,6 +530,57 @@ int lsim_chamfer_3d(const float *x, const float *y, const float *z, const int32_
                     const int32_t *ref_event, const float *ref_w, int64_t n_ref, float *out, float *grad_w,
                     float *grad_z, void *ws, size_t ws_bytes, void *stream);
 
+/* ---------------------------------------------------------------- likelihood losses on distributions */
+
+/* Workspace bytes of lsim_prob_llhd for n_hits target hits. */
+size_t lsim_prob_llhd_workspace_bytes(int64_t n_hits);
+
+/* ProbabilisticLossStrategy.compute, optimize/strategies.py:338-567: the
+ * likelihood of the target hits (pixel id, tick, ADC count; n_hits) under
+ * the probabilistic front end's distributions of the simulated pixels
+ * (sim_pixels [n_pix], sorted ascending, -1 pads first; log_prob and
+ * adcs_distrib [n_pix][n_values][n_ticks]).  Each hit is matched by a
+ * lower-bound search, its occurrence index within its run of equal target
+ * ids (compute_occurrence_indices, :14-40) picks the hit row, and the
+ * entry at its tick (jax.numpy indexing: negative from the end, clamped)
+ * gives T = sum of max(log_prob, log(eps)) over matched hits + log(eps) x
+ * the number of hits whose lower bound holds another id, and C = sum of
+ * -0.5 ((q_tgt - q) / s)^2 - 0.5 log(2 pi s^2), s = sigma_charge / 1000,
+ * q = adc2charge of the distribution's ADC (0 for unmatched hits).
+ * out[0..3] = loss sqrt(T C), -C, -T, -penalty (the reference's loss and
+ * aux).  With g_log_prob or g_adcs (dense, same shape as the
+ * distributions; zeroed here) the gradient of the loss times g_loss[0]
+ * (device float, null = 1) is written; ties of the log(eps) clamp get 1/2,
+ * as jax.lax.max's derivative gives.  n_hits > 0 needs n_pix > 0. */
+int lsim_prob_llhd(const LsimParams *p, const int32_t *sim_pixels, int64_t n_pix, int32_t n_values, int32_t n_ticks,
+                   const float *log_prob, const float *adcs_distrib, const int32_t *tgt_pixels,
+                   const int32_t *tgt_ticks, const float *tgt_adcs, int64_t n_hits, double sigma_charge, double eps,
+                   const float *g_loss, float *out, float *g_log_prob, float *g_adcs, void *ws, size_t ws_bytes,
+                   void *stream);
+
+/* Workspace bytes of lsim_llhd_loss for n_rows rows. */
+size_t lsim_llhd_workspace_bytes(int64_t n_rows);
+
+/* llhd_loss, src/larndsim/losses_jax.py:414-441: out[0] = -sum over rows i
+ * of [log(p_i + 1e-10) + c_i] where tick_i < n_ticks - 3 and
+ * log(no_hit_prob_i + 1e-10) otherwise, p_i = ticks_prob[i][tick_i],
+ * c_i = -0.5 ((charge_mc_i - charge_distrib[i][tick_i]) / sigma)^2 -
+ * 0.5 log(2 pi sigma^2).  Optional gradients (times g_loss[0], device float,
+ * null = 1): dense g_ticks_prob and g_charge_distrib [n_rows][n_ticks]
+ * (zeroed here), g_no_hit_prob and g_charge_mc [n_rows]. */
+int lsim_llhd_loss(const float *ticks_prob, const int32_t *ticks_mc, const float *no_hit_prob,
+                   const float *charge_distrib, const float *charge_mc, int64_t n_rows, int32_t n_ticks, double sigma,
+                   const float *g_loss, float *out, float *g_ticks_prob, float *g_no_hit_prob, float *g_charge_distrib,
+                   float *g_charge_mc, void *ws, size_t ws_bytes, void *stream);
+
+/* Workspace bytes of lsim_occurrence_indices for n ids. */
+size_t lsim_occurrence_workspace_bytes(int64_t n);
+
+/* compute_occurrence_indices, optimize/strategies.py:14-40: out[i] = i minus
+ * the start of the run of equal consecutive ids holding i (a max-scan of
+ * run starts); n < 2^31 - 1. */
+int lsim_occurrence_indices(const int32_t *ids, int64_t n, int32_t *out, void *ws, size_t ws_bytes, void *stream);
+
 /* ---------------------------------------------------------------- parametrised mode */
 
 /* Stage 1 of simulate_parametrized: shift, quench, drift, Monte-Carlo

@@ -508,6 +508,67 @@ int lsim_chamfer_3d(const float *x, const float *y, const float *z, const int32_
               "lsim_chamfer_3d");
 }
 
+size_t lsim_prob_llhd_workspace_bytes(int64_t n_hits) { return n_hits < 0 ? 0 : prob_llhd_workspace_bytes(n_hits); }
+
+int lsim_prob_llhd(const LsimParams *p, const int32_t *sim_pixels, int64_t n_pix, int32_t n_values, int32_t n_ticks,
+                   const float *log_prob, const float *adcs_distrib, const int32_t *tgt_pixels,
+                   const int32_t *tgt_ticks, const float *tgt_adcs, int64_t n_hits, double sigma_charge, double eps,
+                   const float *g_loss, float *out, float *g_log_prob, float *g_adcs, void *ws, size_t ws_bytes,
+                   void *stream) {
+  g_err.clear();
+  if (!p || n_pix < 0 || n_hits < 0 || n_values <= 0 || n_ticks <= 0 || !out)
+    return fail(LSIM_ERR_INVALID, "lsim_prob_llhd: bad arguments");
+  if (n_hits > 0 && n_pix == 0)
+    return fail(LSIM_ERR_INVALID, "lsim_prob_llhd: %lld target hits but no simulated pixels", (long long)n_hits);
+  if (n_pix > 0 && n_pix > INT64_MAX / n_values / n_ticks)
+    return fail(LSIM_ERR_INVALID, "lsim_prob_llhd: distributions too large");
+  if (n_pix > 0 && (!sim_pixels || !log_prob || !adcs_distrib))
+    return fail(LSIM_ERR_INVALID, "lsim_prob_llhd: null prediction array");
+  if (n_hits > 0 && (!tgt_pixels || !tgt_ticks || !tgt_adcs))
+    return fail(LSIM_ERR_INVALID, "lsim_prob_llhd: null target array");
+  if (!(sigma_charge > 0.0) || !(eps > 0.0))
+    return fail(LSIM_ERR_INVALID, "lsim_prob_llhd: sigma_charge %g, eps %g", sigma_charge, eps);
+  if (!ws || ws_bytes < prob_llhd_workspace_bytes(n_hits))
+    return fail(LSIM_ERR_CAPACITY, "lsim_prob_llhd: workspace %zu < %zu bytes", ws_bytes,
+                prob_llhd_workspace_bytes(n_hits));
+  return wrap(run_prob_llhd(*p, sim_pixels, n_pix, n_values, n_ticks, log_prob, adcs_distrib, tgt_pixels, tgt_ticks,
+                            tgt_adcs, n_hits, sigma_charge, eps, g_loss, out, g_log_prob, g_adcs, ws,
+                            (cudaStream_t)stream),
+              "lsim_prob_llhd");
+}
+
+size_t lsim_llhd_workspace_bytes(int64_t n_rows) { return n_rows < 0 ? 0 : llhd_workspace_bytes(n_rows); }
+
+int lsim_llhd_loss(const float *ticks_prob, const int32_t *ticks_mc, const float *no_hit_prob,
+                   const float *charge_distrib, const float *charge_mc, int64_t n_rows, int32_t n_ticks, double sigma,
+                   const float *g_loss, float *out, float *g_ticks_prob, float *g_no_hit_prob, float *g_charge_distrib,
+                   float *g_charge_mc, void *ws, size_t ws_bytes, void *stream) {
+  g_err.clear();
+  if (n_rows < 0 || n_ticks <= 0 || !out) return fail(LSIM_ERR_INVALID, "lsim_llhd_loss: bad arguments");
+  if (n_rows > INT64_MAX / n_ticks) return fail(LSIM_ERR_INVALID, "lsim_llhd_loss: distributions too large");
+  if (n_rows > 0 && (!ticks_prob || !ticks_mc || !no_hit_prob || !charge_distrib || !charge_mc))
+    return fail(LSIM_ERR_INVALID, "lsim_llhd_loss: null input array");
+  if (!(sigma > 0.0)) return fail(LSIM_ERR_INVALID, "lsim_llhd_loss: sigma %g", sigma);
+  if (!ws || ws_bytes < llhd_workspace_bytes(n_rows))
+    return fail(LSIM_ERR_CAPACITY, "lsim_llhd_loss: workspace %zu < %zu bytes", ws_bytes,
+                llhd_workspace_bytes(n_rows));
+  return wrap(run_llhd(ticks_prob, ticks_mc, no_hit_prob, charge_distrib, charge_mc, n_rows, n_ticks, sigma, g_loss,
+                       out, g_ticks_prob, g_no_hit_prob, g_charge_distrib, g_charge_mc, ws, (cudaStream_t)stream),
+              "lsim_llhd_loss");
+}
+
+size_t lsim_occurrence_workspace_bytes(int64_t n) { return n < 0 ? 0 : occurrence_workspace_bytes(n); }
+
+int lsim_occurrence_indices(const int32_t *ids, int64_t n, int32_t *out, void *ws, size_t ws_bytes, void *stream) {
+  g_err.clear();
+  if (n < 0 || n > INT32_MAX - 1 || (n > 0 && (!ids || !out)))
+    return fail(LSIM_ERR_INVALID, "lsim_occurrence_indices: bad arguments");
+  if (n > 0 && (!ws || ws_bytes < occurrence_workspace_bytes(n)))
+    return fail(LSIM_ERR_CAPACITY, "lsim_occurrence_indices: workspace %zu < %zu bytes", ws_bytes,
+                occurrence_workspace_bytes(n));
+  return wrap(run_occurrence(ids, (int32_t)n, out, ws, (cudaStream_t)stream), "lsim_occurrence_indices");
+}
+
 int lsim_gather_tracks(const float *table, int64_t n_table, int32_t n_fields, const int64_t *rows, int64_t n_rows,
                        int32_t event_col, const float *event_values, float *out, int32_t *status_dev, void *stream) {
   g_err.clear();

@@ -73,6 +73,19 @@ int run_fee_prob(const LsimParams &p, const float *wfs, int64_t n_pix, int32_t n
                  float stop_threshold, float *log_prob, float *charge, float *e_tick, float *e_adc, float *lam,
                  void *ws, cudaStream_t st);
 
+// lsim_prob_loss.cu
+size_t prob_llhd_workspace_bytes(int64_t n_hits);
+int run_prob_llhd(const LsimParams &p, const int32_t *sim, int64_t n_pix, int32_t n_values, int32_t n_ticks,
+                  const float *log_prob, const float *adcs, const int32_t *tgt_pix, const int32_t *tgt_tick,
+                  const float *tgt_adc, int64_t n_hits, double sigma_charge, double eps, const float *g_loss,
+                  float *out, float *g_log_prob, float *g_adcs, void *ws, cudaStream_t st);
+size_t llhd_workspace_bytes(int64_t n_rows);
+int run_llhd(const float *tpd, const int32_t *ticks, const float *nohit, const float *cd, const float *cmc,
+             int64_t n_rows, int32_t n_ticks, double sigma, const float *g_loss, float *out, float *g_tpd,
+             float *g_nohit, float *g_cd, float *g_cmc, void *ws, cudaStream_t st);
+size_t occurrence_workspace_bytes(int64_t n);
+int run_occurrence(const int32_t *ids, int32_t n, int32_t *out, void *ws, cudaStream_t st);
+
 // lsim_losses.cu
 size_t mse_adc_workspace_bytes(int64_t n, int64_t m);
 int run_mse_adc(const float *x, const float *y, const float *z, const int32_t *event, const float *w, int64_t n,

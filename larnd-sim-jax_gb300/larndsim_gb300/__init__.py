@@ -12,7 +12,7 @@ from .sim import (average_hit_values, get_adc_values, get_adc_values_average_noi
                   get_average_hit_values, load_lut, pad_size, prepare_lut, simulate_parametrized,
                   simulate_probabilistic, simulate_stochastic, simulate_wfs)
 from .fee import digitize  # noqa: F401
-from .losses import adc2charge, chamfer_3d, mse_adc, nll_loss  # noqa: F401
+from .losses import adc2charge, chamfer_3d, llhd_loss, mse_adc, nll_loss  # noqa: F401
 from .dataio import DataLoader, TgtTracksDataset, TracksDataset, chop_tracks  # noqa: F401
 from .detsim import (validate_event_ids_for_packing, validate_local_event_ids,  # noqa: F401
                      validate_packed_ids_for_decoding)
@@ -23,7 +23,7 @@ __all__ = [
     "load_detector_properties", "get_adc_values", "load_lut", "pad_size", "prepare_lut",
     "simulate_parametrized", "simulate_stochastic", "simulate_wfs", "digitize", "adc2charge", "chop_tracks",
     "simulate_probabilistic", "get_adc_values_average_noise_vmap", "get_average_hit_values", "average_hit_values",
-    "mse_adc", "nll_loss", "chamfer_3d", "hit_records", "write_hits_npz", "write_hits_h5", "write_hits_groups_npz",
+    "mse_adc", "nll_loss", "chamfer_3d", "llhd_loss", "hit_records", "write_hits_npz", "write_hits_h5", "write_hits_groups_npz",
     "TracksDataset", "TgtTracksDataset", "DataLoader", "validate_event_ids_for_packing",
     "validate_local_event_ids", "validate_packed_ids_for_decoding",
 ]

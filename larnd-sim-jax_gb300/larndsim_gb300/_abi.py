@@ -131,6 +131,14 @@ _SIGNATURES = {
     "lsim_chamfer_workspace_bytes": (_sz, [_i64, _i64]),
     "lsim_chamfer_3d": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
                                   _sz, _vp]),
+    "lsim_prob_llhd_workspace_bytes": (_sz, [_i64]),
+    "lsim_prob_llhd": (C.c_int, [_PP, _vp, _i64, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _i64, C.c_double, C.c_double,
+                                 _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "lsim_llhd_workspace_bytes": (_sz, [_i64]),
+    "lsim_llhd_loss": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, _i32, C.c_double, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                 _sz, _vp]),
+    "lsim_occurrence_workspace_bytes": (_sz, [_i64]),
+    "lsim_occurrence_indices": (C.c_int, [_vp, _i64, _vp, _vp, _sz, _vp]),
     "lsim_hit_records_workspace_bytes": (_sz, [_i64]),
     "lsim_hit_records": (C.c_int, [_PP, C.c_float, C.POINTER(LsimHitColumns), _i64, C.POINTER(LsimHitColumns), _vp,
                                    _vp, _vp, _vp, _vp, _vp, _sz, _vp]),

@@ -17,7 +17,7 @@ PKG_DIR = Path(__file__).resolve().parent
 CSRC = PKG_DIR.parent / "csrc"
 INCLUDE = PKG_DIR.parent.parent / "include"
 LIB_PATH = PKG_DIR / "liblsim.so"
-SOURCES = ("lsim_segments.cu", "lsim_accum.cu", "lsim_main.cu", "lsim_fee.cu", "lsim_lut.cu", "lsim_chop.cu", "lsim_records.cu", "lsim_tracks.cu", "lsim_fee_prob.cu", "lsim_losses.cu", "lsim_api.cu")
+SOURCES = ("lsim_segments.cu", "lsim_accum.cu", "lsim_main.cu", "lsim_fee.cu", "lsim_lut.cu", "lsim_chop.cu", "lsim_records.cu", "lsim_tracks.cu", "lsim_fee_prob.cu", "lsim_losses.cu", "lsim_prob_loss.cu", "lsim_api.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

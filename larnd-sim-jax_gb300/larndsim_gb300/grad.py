@@ -269,7 +269,7 @@ def _hit_z(params, theta, ticks, plane):
     v = torch.tensor(np.float32(get_vdrift(pe)), dtype=torch.float32, device=ticks.device)
     v = v + (e - e.detach()).to(torch.float32) * float(get_vdrift_derivative(pe))
     b = torch.as_tensor(np.asarray(params.tpc_borders, np.float32), device=ticks.device)[plane.long()]
-    za, zh = b[:, 2, 0], b[:, 2, 1]
+    za, zh = b[..., 2, 0], b[..., 2, 1]
     return za + ticks * (np.float32(params.t_sampling) * v) * torch.sign(zh - za)
 
 

@@ -172,3 +172,59 @@ def chamfer_3d(params, Q, x, y, z, ticks, hit_prob, event, ref_Q, ref_x, ref_y, 
                                _pad(_f32(ref_z, dev), new_ref).contiguous(),
                                _pad(_i32(ref_event, dev), new_ref).contiguous())
     return loss, dict()
+
+
+class _LlhdFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, tpd, nohit, cd, cm, ticks, sigma):
+        from . import _abi, sim
+        lib = _abi.load()
+        n, t = tpd.shape
+        ws = torch.empty(max(lib.lsim_llhd_workspace_bytes(n), 1), dtype=torch.uint8, device=tpd.device)
+        out = torch.empty(1, dtype=torch.float32, device=tpd.device)
+        p = sim._ptr
+        _abi.check(lib, lib.lsim_llhd_loss(p(tpd), p(ticks), p(nohit), p(cd), p(cm), n, t, float(sigma), None,
+                                           p(out), None, None, None, None, p(ws), ws.numel(), sim._stream()))
+        ctx.save_for_backward(tpd, nohit, cd, cm, ticks)
+        ctx.sigma = sigma
+        return out[0]
+
+    @staticmethod
+    def backward(ctx, g):
+        from . import _abi, sim
+        lib = _abi.load()
+        tpd, nohit, cd, cm, ticks = ctx.saved_tensors
+        n, t = tpd.shape
+        ws = torch.empty(max(lib.lsim_llhd_workspace_bytes(n), 1), dtype=torch.uint8, device=tpd.device)
+        out = torch.empty(1, dtype=torch.float32, device=tpd.device)
+        g_t, g_c = torch.empty_like(tpd), torch.empty_like(cd)
+        g_nh, g_cm = torch.empty_like(nohit), torch.empty_like(cm)
+        gl = g.detach().to(torch.float32).reshape(1).contiguous()
+        p = sim._ptr
+        _abi.check(lib, lib.lsim_llhd_loss(p(tpd), p(ticks), p(nohit), p(cd), p(cm), n, t, float(ctx.sigma), p(gl),
+                                           p(out), p(g_t), p(g_nh), p(g_c), p(g_cm), p(ws), ws.numel(),
+                                           sim._stream()))
+        return g_t, g_nh, g_c, g_cm, None, None
+
+
+def llhd_loss(ticks_prob_distrib, ticks_mc, no_hit_prob, charge_distrib, charge_mc, sigma=500):
+    """losses_jax.py:414-441: the negative log-likelihood of observed hit
+    ticks and charges under per-row tick distributions (N, T): log(p[tick]
+    + 1e-10), or log(no_hit_prob + 1e-10) where tick >= T - 3, plus a
+    Gaussian charge term of width ``sigma`` at the distribution's charge.
+    Returns (loss, {}); the loss is differentiable with respect to the four
+    float inputs (lsim_llhd_loss)."""
+    tpd = torch.as_tensor(ticks_prob_distrib, dtype=torch.float32)
+    dev = tpd.device if tpd.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    tpd = tpd.to(dev).contiguous()
+    if tpd.dim() != 2:
+        raise ValueError(f"ticks_prob_distrib must be (rows, ticks), got {tuple(tpd.shape)}")
+    cd = torch.as_tensor(charge_distrib, dtype=torch.float32).to(dev).contiguous()
+    if cd.shape != tpd.shape:
+        raise ValueError(f"charge_distrib {tuple(cd.shape)} does not match ticks_prob_distrib {tuple(tpd.shape)}")
+    nohit = torch.as_tensor(no_hit_prob, dtype=torch.float32).to(dev).reshape(-1).contiguous()
+    cm = torch.as_tensor(charge_mc, dtype=torch.float32).to(dev).reshape(-1).contiguous()
+    ticks = _i32(torch.as_tensor(ticks_mc), dev)
+    if not (nohit.shape[0] == cm.shape[0] == ticks.shape[0] == tpd.shape[0]):
+        raise ValueError("ticks_mc, no_hit_prob and charge_mc need one entry per row")
+    return _LlhdFn.apply(tpd, nohit, cd, cm, ticks, sigma), dict()

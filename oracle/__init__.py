@@ -15,6 +15,11 @@ Contents
                   indices, reset masks) frozen from a float32 forward pass,
                   plus central finite differences: the pathwise gradient the
                   reference's ``jax.value_and_grad`` computes.
+``losses_np``     float64 restatement of the hit-level fit losses.
+``prob_loss_np``  restatement of the likelihood losses on the probabilistic
+                  front end's distributions (ProbabilisticLossStrategy,
+                  compute_occurrence_indices, llhd_loss) and their
+                  gradients.
 
 Parity status: PARTIALLY PINNED.  The reference is JAX and JAX is not
 installable on the machines this builds on, and its LUT-mode golden outputs

@@ -390,6 +390,21 @@ def cummax(operand, axis=0, reverse=False):
     return _x32(np.maximum.accumulate(a, axis=axis))
 
 
+def associative_scan(fn, elems, reverse=False, axis=0):
+    """Inclusive scan of a binary associative ``fn`` along ``axis``,
+    evaluated left to right (the result of an associative fn does not
+    depend on the grouping)."""
+    if reverse:
+        raise NotImplementedError("associative_scan(reverse=True)")
+    a = np.moveaxis(_arg(np.asarray(elems)), axis, 0)
+    if a.shape[0] == 0:
+        return _x32(np.moveaxis(a, 0, axis))
+    out = [a[0]]
+    for i in range(1, a.shape[0]):
+        out.append(_arg(np.asarray(fn(out[-1], a[i]))))
+    return _x32(np.moveaxis(np.stack(out), 0, axis))
+
+
 def top_k(operand, k):
     a = _arg(np.asarray(operand))
     idx = np.argsort(-a, axis=-1, kind="stable")[..., :k]
@@ -508,7 +523,7 @@ def install(yaml_loads, x64=False):
     _X64[0] = bool(x64)
     jnp = _make_jnp()
     lax = _module("jax.lax", scan=scan, cummax=cummax, top_k=top_k, cond=cond, fori_loop=fori_loop,
-                  stop_gradient=_identity)
+                  stop_gradient=_identity, associative_scan=associative_scan)
     random = _module("jax.random", key=prng_key, PRNGKey=prng_key, split=split, normal=normal, uniform=uniform)
     special = _SpecialNamespace("jax.scipy.special")
     stats = _module("jax.scipy.stats", norm=_Norm())

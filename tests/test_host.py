@@ -302,3 +302,33 @@ def test_fit_options_follow_the_reference_checks():
         fit.fit_options(("Ab",), 0.1, init, "sigmoid", 0.0)
     with pytest.raises(ValueError, match="cannot fit"):
         fit.fit_options(("shift_x",), 0.1, init)
+
+
+def test_likelihood_loss_entry_points_reject_bad_arguments_without_gpu(lib):
+    """lsim_prob_llhd, lsim_llhd_loss and lsim_occurrence_indices validate
+    their arguments before any launch."""
+    V = ctypes.c_void_p
+    p = _abi.make_params(consts.Params())
+    big = 1 << 30
+    assert lib.lsim_prob_llhd_workspace_bytes(1000) >= 8 * 3 * 4
+    assert lib.lsim_prob_llhd_workspace_bytes(-1) == 0
+    assert lib.lsim_prob_llhd(p, V(16), 0, 10, 2000, V(16), V(16), V(16), V(16), V(16), 5, 500.0, 1e-10, None,
+                              V(16), None, None, V(256), big, None) == _abi.LSIM_ERR_INVALID   # hits, no pixels
+    assert b"no simulated pixels" in lib.lsim_last_error()
+    assert lib.lsim_prob_llhd(p, V(16), 4, 0, 2000, V(16), V(16), V(16), V(16), V(16), 5, 500.0, 1e-10, None,
+                              V(16), None, None, V(256), big, None) == _abi.LSIM_ERR_INVALID   # n_values
+    assert lib.lsim_prob_llhd(p, V(16), 4, 10, 2000, V(16), V(16), V(16), V(16), V(16), 5, 0.0, 1e-10, None,
+                              V(16), None, None, V(256), big, None) == _abi.LSIM_ERR_INVALID   # sigma
+    assert lib.lsim_prob_llhd(p, V(16), 4, 10, 2000, None, V(16), V(16), V(16), V(16), 5, 500.0, 1e-10, None,
+                              V(16), None, None, V(256), big, None) == _abi.LSIM_ERR_INVALID   # null ids
+    assert lib.lsim_prob_llhd(p, V(16), 4, 10, 2000, V(16), V(16), V(16), V(16), V(16), 5, 500.0, 1e-10, None,
+                              V(16), None, None, V(256), 8, None) == _abi.LSIM_ERR_CAPACITY
+    assert lib.lsim_llhd_loss(V(16), V(16), V(16), V(16), V(16), 4, 0, 500.0, None, V(16), None, None, None, None,
+                              V(256), big, None) == _abi.LSIM_ERR_INVALID                     # n_ticks
+    assert lib.lsim_llhd_loss(V(16), None, V(16), V(16), V(16), 4, 100, 500.0, None, V(16), None, None, None, None,
+                              V(256), big, None) == _abi.LSIM_ERR_INVALID                     # null ticks
+    assert lib.lsim_llhd_loss(V(16), V(16), V(16), V(16), V(16), 4, 100, 500.0, None, V(16), None, None, None, None,
+                              V(256), 0, None) == _abi.LSIM_ERR_CAPACITY
+    assert lib.lsim_occurrence_indices(V(16), -1, V(16), V(256), big, None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_occurrence_indices(V(16), 1 << 31, V(16), V(256), big, None) == _abi.LSIM_ERR_INVALID
+    assert lib.lsim_occurrence_indices(V(16), 5000, V(16), V(256), 16, None) == _abi.LSIM_ERR_CAPACITY
