@@ -38,8 +38,12 @@ constexpr float kProbFloor = -1000.0f;
 // jax.scipy.special.ndtr / log_ndtr in float32 (the published piecewise
 // form: erf near zero and erfc in the tails for ndtr; -ndtr(-x) above 5,
 // log(ndtr(x)) down to -10, the order-3 asymptotic series below).
+// ndtr, log_ndtr, log_diff_ndtr and its log term are called, not inlined:
+// inlined at every call site of the per-path loops their erf/erfc/log
+// bodies overflowed the instruction cache (the beam search ran 1.9x and
+// its adjoint 2.2x slower, with identical results).
 
-__device__ __forceinline__ float ndtr_f(float x) {
+__device__ __noinline__ float ndtr_f(float x) {
   const float hs2 = 0.70710678118654752f;
   const float w = x * hs2;
   const float z = fabsf(w);
@@ -47,7 +51,7 @@ __device__ __forceinline__ float ndtr_f(float x) {
   return 0.5f * y;
 }
 
-__device__ __forceinline__ float log_ndtr_f(float x) {
+__device__ __noinline__ float log_ndtr_f(float x) {
   // above 15, erfc(x / sqrt 2) < 1e-50 is 0 in float32: -ndtr(-x) = -0
   if (x > 15.0f) return -0.0f;
   if (x > 5.0f) return -ndtr_f(-x);
@@ -71,7 +75,7 @@ __device__ __forceinline__ float softplus_f(float y) {
 __device__ __forceinline__ float sigmoid_f(float x) { return 1.0f / (1.0f + expf(-x)); }
 
 // The clamped log(1 - exp(safe)) term of log_diff_ndtr.
-__device__ __forceinline__ float ldn_log_term(float safe) {
+__device__ __noinline__ float ldn_log_term(float safe) {
   const float neg = -expm1f(safe);
   const float neg_safe = 1e-30f + softplus_f((neg - 1e-30f) * 1e10f) / 1e10f;
   // neg_safe >= 1e-30, so lt >= -69.1 and the clamp's softplus argument
@@ -84,7 +88,7 @@ __device__ __forceinline__ float ldn_log_term(float safe) {
 // log_ndtr(a), log_ndtr(b); term_m1 = ldn_log_term(-1), the value every
 // a <= b takes (safe = -1 there), so flat stretches (a == b, w = 1/2 exactly)
 // need no transcendental function at all.
-__device__ __forceinline__ float log_diff_ndtr_f(float a, float b, float la, float lb, float term_m1) {
+__device__ __noinline__ float log_diff_ndtr_f(float a, float b, float la, float lb, float term_m1) {
   if (a == b) return 0.5f * (la + term_m1) + 0.5f * kProbFloor;
   const float lts = a > b ? ldn_log_term(lb - la) : term_m1;
   const float lp = la + lts;
