@@ -564,17 +564,20 @@ struct ProbVjpArgs {
 // every kVjpSpan ticks, so the per-class loops over ticks stay short (flat
 // stretches of a waveform are long).
 constexpr int kVjpSpan = 16;
-constexpr int kVjpArrays = 16;   // q, running max, esperance, soft-where weight, 5 accumulators, dist and hit
-                                 // cotangents, class hit and dist values, scratch, class, representative
+constexpr int kVjpArrays = 13;   // q, running max, 5 accumulators, dist and hit cotangents, class hit and
+                                 // dist values (the hit values double as scratch), class, representative;
+                                 // the esperance and the soft-where weight are recomputed from q, so two
+                                 // blocks fit on an SM
 
-__global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va) {
+__global__ void __launch_bounds__(kProbThreads, 2) k_fee_prob_vjp(ProbVjpArgs va) {
   extern __shared__ __align__(16) float sm[];
   const ProbArgs &a = va.f;
-  float *qs = sm, *cm = qs + kProbMaxT, *esp = cm + kProbMaxT, *sw = esp + kProbMaxT;
-  float *Aq0 = sw + kProbMaxT, *Aqs = Aq0 + kProbMaxT, *Am0 = Aqs + kProbMaxT, *Am1 = Am0 + kProbMaxT;
+  float *qs = sm, *cm = qs + kProbMaxT;
+  float *Aq0 = cm + kProbMaxT, *Aqs = Aq0 + kProbMaxT, *Am0 = Aqs + kProbMaxT, *Am1 = Am0 + kProbMaxT;
   float *Aesp = Am1 + kProbMaxT, *Gd = Aesp + kProbMaxT, *Gh = Gd + kProbMaxT;
-  float *vh = Gh + kProbMaxT, *vd = vh + kProbMaxT, *tmp = vd + kProbMaxT;
-  int *cls = reinterpret_cast<int *>(tmp + kProbMaxT), *rep = cls + kProbMaxT;
+  float *vh = Gh + kProbMaxT, *vd = vh + kProbMaxT;
+  float *tmp = vh;   // scratch before and after the steps, when the class values are not in use
+  int *cls = reinterpret_cast<int *>(vd + kProbMaxT), *rep = cls + kProbMaxT;
   float *part = reinterpret_cast<float *>(rep + kProbMaxT);   // [warps][2][kProbMaxPaths]
   __shared__ float red[kProbThreads / 32];
   __shared__ float pc[kProbMaxPaths], plp[kProbMaxPaths], glp_n[kProbMaxPaths], gc_n[kProbMaxPaths];
@@ -587,6 +590,9 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
   const float z = a.z, thr = a.thr;
   const float term_m1 = ldn_log_term(-1.0f);
   auto shifted = [&](int t) { return min(t + a.interval + 1, T - 1); };
+  // the esperance and the soft-where weight of tick t, recomputed from q
+  auto esp_at = [&](int t) { return (qs[shifted(t)] + thr) - 0.5f * (qs[t + 1] + qs[t]); };
+  auto sw_at = [&](float e) { return sigmoid_f((e - thr) * 10.0f); };
   if (tid == 0) {
     int first = H;
     for (int h = 1; h < H; ++h)
@@ -610,9 +616,6 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
     block_scan_row<kScanMax>(cm, T, red);
     for (int t = tid; t < T - 1; t += kProbThreads) {
       const int s = shifted(t);
-      const float e = (qs[s] + thr) - 0.5f * (qs[t + 1] + qs[t]);
-      esp[t] = e;
-      sw[t] = sigmoid_f((e - thr) * 10.0f);
       bool head = t % kVjpSpan == 0;
       if (!head) {
         const int sp = shifted(t - 1);
@@ -671,6 +674,7 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
           float hm = -INFINITY, hs = 0.f, dm = -INFINITY, ds = 0.f;
           const int t = rep[u];
           const int sidx = shifted(t);
+          const float swt = sw_at(esp_at(t));
           for (int k = 0; k < K; ++k) {
             if (pskip[k]) continue;
             const float c = pc[k], lp = plp[k];
@@ -684,7 +688,7 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
             float le = log_diff_ndtr_f(zqs, zq0, LQs, LQ0, term_m1);
             le = fminf(le, lg);
             le = kProbFloor + softplus_f(le - kProbFloor);
-            le = sw[t] * le + (1.0f - sw[t]) * kProbFloor;
+            le = swt * le + (1.0f - swt) * kProbFloor;
             lse_add(hm, hs, le + lp);
             lse_add(dm, ds, lg + lp);
           }
@@ -707,7 +711,7 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
           pr[i] = expf(vh[cls[t]]);
           l_sum += pr[i];
           t_sum += (float)t * pr[i];
-          a_sum += digitize(p, esp[t]) * pr[i];
+          a_sum += digitize(p, esp_at(t)) * pr[i];
         }
       }
       if (va.g_lam) {
@@ -725,10 +729,11 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
         for (int i = 0; i < kProbTicks; ++i) {
           const int t = tid + i * kProbThreads;
           if (t < T - 1) {
-            const float adc = digitize(p, esp[t]);
+            const float et = esp_at(t);
+            const float adc = digitize(p, et);
             const float gp = gl + gt * (float)t / den + ga * adc / den + on * gden;
             Gh[t] += gp * pr[i];
-            Aesp[t] += digitize_vjp(p, esp[t], ga * pr[i] / den);
+            Aesp[t] += digitize_vjp(p, et, ga * pr[i] / den);
           }
         }
       }
@@ -779,7 +784,7 @@ __global__ void __launch_bounds__(kProbThreads, 1) k_fee_prob_vjp(ProbVjpArgs va
                                        g_qs, g_q0);
             const float le1 = fminf(lep, lg);
             const float le2 = kProbFloor + softplus_f(le1 - kProbFloor);
-            const float wt = sw[t];
+            const float wt = sw_at(esp_at(t));
             const float le = wt * le2 + (1.0f - wt) * kProbFloor;
             // d(hit log-sum-exp)/d(le + lp) and d(dist log-sum-exp)/d(lg + lp)
             const float al = anyH[i] ? expf((le + lp) - vh[u]) : 0.f;
@@ -949,7 +954,7 @@ int run_fee_prob_vjp(const LsimParams &p, const float *wfs, int64_t n_pix, int32
   va.g_e_adc = g_e_adc;
   va.g_lam = g_lam;
   va.g_wfs = g_wfs;
-  const size_t smem = sizeof(float) * ((kVjpArrays + 1) * kProbMaxT + 2 * (kProbThreads / 32) * kProbMaxPaths);
+  const size_t smem = sizeof(float) * (kVjpArrays * kProbMaxT + 2 * (kProbThreads / 32) * kProbMaxPaths);
   if (cudaFuncSetAttribute(k_fee_prob_vjp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return LSIM_ERR_CUDA;
   int per_sm = 0;
