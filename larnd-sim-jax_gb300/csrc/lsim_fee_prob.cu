@@ -38,9 +38,9 @@ constexpr float kProbFloor = -1000.0f;
 // jax.scipy.special.ndtr / log_ndtr in float32 (the published piecewise
 // form: erf near zero and erfc in the tails for ndtr; -ndtr(-x) above 5,
 // log(ndtr(x)) down to -10, the order-3 asymptotic series below).
-// ndtr, log_ndtr, log_diff_ndtr and its log term are called, not inlined:
+// ndtr, log_ndtr and log_diff_ndtr's log term are called, not inlined:
 // inlined at every call site of the per-path loops their erf/erfc/log
-// bodies overflowed the instruction cache (the beam search ran 1.9x and
+// bodies overflowed the instruction cache (the beam search ran 2.0x and
 // its adjoint 2.2x slower, with identical results).
 
 __device__ __noinline__ float ndtr_f(float x) {
@@ -88,7 +88,7 @@ __device__ __noinline__ float ldn_log_term(float safe) {
 // log_ndtr(a), log_ndtr(b); term_m1 = ldn_log_term(-1), the value every
 // a <= b takes (safe = -1 there), so flat stretches (a == b, w = 1/2 exactly)
 // need no transcendental function at all.
-__device__ __noinline__ float log_diff_ndtr_f(float a, float b, float la, float lb, float term_m1) {
+__device__ __forceinline__ float log_diff_ndtr_f(float a, float b, float la, float lb, float term_m1) {
   if (a == b) return 0.5f * (la + term_m1) + 0.5f * kProbFloor;
   const float lts = a > b ? ldn_log_term(lb - la) : term_m1;
   const float lp = la + lts;
