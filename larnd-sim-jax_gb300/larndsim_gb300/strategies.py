@@ -108,7 +108,7 @@ def _hit_z(params, ticks, plane, theta=None):
     v = np.float32(get_vdrift(params))
     b = torch.as_tensor(np.asarray(params.tpc_borders, np.float32), device=ticks.device)[plane.long()]
     za, zh = b[..., 2, 0], b[..., 2, 1]
-    return za + ticks * (np.float32(params.t_sampling) * v) * torch.sign(zh - za)
+    return za + ((ticks * np.float32(params.t_sampling)) * v) * torch.sign(zh - za)
 
 
 class LossStrategy:
