@@ -31,7 +31,8 @@ constexpr int kProbMaxT = kProbThreads * kProbTicks;
 constexpr int kProbMaxPaths = 32;
 constexpr int kProbArrays = 10;  // q, running max, suffix max, esperance, soft-where weight, 3 class values, class, representative
 // plus 6 partial sums per thread and the per-warp top-K candidates (value, index)
-constexpr int kProbExtraFloats = 6 * kProbThreads + 2 * (kProbThreads / 32) * kProbMaxPaths;
+constexpr int kProbExtraFloats = 6 * kProbThreads + 2 * (kProbThreads / 32) * kProbMaxPaths + kProbMaxT;
+static_assert(6 * kProbThreads >= kProbMaxT, "the path-group partials hold one tick array");
 constexpr float kProbFloor = -1000.0f;
 
 // ---------------------------------------------------------------- special functions
@@ -231,6 +232,10 @@ __global__ void __launch_bounds__(kProbThreads, 2) k_fee_prob(ProbArgs a) {
   float *part = reinterpret_cast<float *>(rep + kProbMaxT);   // [kProbThreads][6] partial sums of path groups
   float *cand_v = part + 6 * kProbThreads;                     // [warps][K] per-warp top-K candidates
   int *cand_i = reinterpret_cast<int *>(cand_v + (kProbThreads / 32) * kProbMaxPaths);
+  // per-tick log_ndtr of the running maximum and of q for one path, shared by
+  // neighbouring classes on dense pixels (the path-group partials, unused
+  // then, hold the first)
+  float *lmv = part, *lqv = reinterpret_cast<float *>(cand_i + (kProbThreads / 32) * kProbMaxPaths);
   __shared__ float red[kProbThreads / 32];
   __shared__ float pc[kProbMaxPaths], plp[kProbMaxPaths], nc[kProbMaxPaths], nlp[kProbMaxPaths];
   __shared__ int pskip[kProbMaxPaths];
@@ -288,6 +293,10 @@ __global__ void __launch_bounds__(kProbThreads, 2) k_fee_prob(ProbArgs a) {
     const int grp = G > 1 ? tid / U : 0;
     const int n_own = G > 1 ? (grp < G ? 1 : 0) : kProbTicks;
     const int r0 = G > 1 ? tid - grp * U : tid;
+    // dense pixels: per path, log_ndtr at every tick (2 T calls) instead of
+    // four per class (the running maximum at t + 1 and q at the shifted tick
+    // are other ticks' values at t)
+    const bool tick_mode = G == 1 && 2 * U > T;
 
     for (int h = 0; h < H; ++h) {
       // paths whose charge repeats that of a path more than 110 log units
@@ -313,6 +322,14 @@ __global__ void __launch_bounds__(kProbThreads, 2) k_fee_prob(ProbArgs a) {
       for (int k = grp; n_own > 0 && k < K; k += G) {
         if (pskip[k]) continue;
         const float c = pc[k], lp = plp[k];
+        if (tick_mode) {
+          __syncthreads();   // the previous path's reads are done
+          for (int t = tid; t < T; t += kProbThreads) {
+            lmv[t] = log_ndtr_f(((cm[t] - c) - thr) * z);
+            lqv[t] = log_ndtr_f(((qs[t] - c) - thr) * z);
+          }
+          __syncthreads();
+        }
 #pragma unroll
         for (int i = 0; i < kProbTicks; ++i) {
           const int r = r0 + i * kProbThreads;
@@ -320,12 +337,12 @@ __global__ void __launch_bounds__(kProbThreads, 2) k_fee_prob(ProbArgs a) {
             const int t = rep[r];
             const int s = shifted(t);
             const float zm0 = ((cm[t] - c) - thr) * z, zm1 = ((cm[t + 1] - c) - thr) * z;
-            const float LM0 = log_ndtr_f(zm0);
-            const float LM1 = zm1 == zm0 ? LM0 : log_ndtr_f(zm1);
+            const float LM0 = tick_mode ? lmv[t] : log_ndtr_f(zm0);
+            const float LM1 = tick_mode ? lmv[t + 1] : (zm1 == zm0 ? LM0 : log_ndtr_f(zm1));
             const float lg = log_diff_ndtr_f(zm1, zm0, LM1, LM0, term_m1);
             const float zq0 = ((qs[t] - c) - thr) * z, zqs = ((qs[s] - c) - thr) * z;
-            const float LQ0 = log_ndtr_f(zq0);
-            const float LQs = zqs == zq0 ? LQ0 : log_ndtr_f(zqs);
+            const float LQ0 = tick_mode ? lqv[t] : log_ndtr_f(zq0);
+            const float LQs = tick_mode ? lqv[s] : (zqs == zq0 ? LQ0 : log_ndtr_f(zqs));
             float le = log_diff_ndtr_f(zqs, zq0, LQs, LQ0, term_m1);
             le = fminf(le, lg);
             le = kProbFloor + softplus_f(le - kProbFloor);
