@@ -14,6 +14,8 @@
 // size) apart in x, so their kernel value exp(-d / (2 sigma^2)) is exactly 0
 // in float32 and skipping them changes nothing.  Inputs ordered by event
 // (as the hit compaction emits them) make almost all chunks skippable.
+#include <cmath>
+
 #include "lsim_internal.cuh"
 
 namespace lsim {
@@ -59,24 +61,46 @@ __global__ void k_chunk_events(const int32_t *__restrict__ event, int64_t n, int
   }
 }
 
-// s[i] = sum_j cols.w[j] K_ij; with zs, zs[i] = sum_j cols.w[j] K_ij (z_i - z_j)
+// s[i] = sum_j cols.w[j] K_ij; with zs, zs[i] = sum_j cols.w[j] K_ij (z_i - z_j).
+// Each thread owns two row hits (a block covers 2 kRbfRows rows) and reads
+// each staged column once for both (x, y, z, w in one 16-byte word).  The
+// exponent is -d / (2 sigma^2) as the reference divides; when 2 sigma^2 is a
+// power of two that is the exact product with its reciprocal (kMul).
+constexpr int kRbfPerThread = 2;
+
+__device__ __forceinline__ float rbf_term(float xi, float yi, float zi, const float4 &c, float two_sigma2,
+                                          float inv, bool mul, float *dz_out) {
+  const float dx = __fsub_rn(xi, c.x), dy = __fsub_rn(yi, c.y), dz = __fsub_rn(zi, c.z);
+  const float d = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  *dz_out = dz;
+  return expf(mul ? __fmul_rn(-d, inv) : __fdiv_rn(-d, two_sigma2)) * c.w;
+}
+
+template <bool kMul>
 __global__ void __launch_bounds__(kRbfRows) k_rbf_rows(HitSet rows, HitSet cols, const int2 *__restrict__ col_ranges,
-                                                       float two_sigma2, float *__restrict__ s,
+                                                       float two_sigma2, float inv_two_sigma2, float *__restrict__ s,
                                                        float *__restrict__ zs) {
-  __shared__ float cx[kRbfChunk], cy[kRbfChunk], cz[kRbfChunk], cw[kRbfChunk];
+  __shared__ float4 col[kRbfChunk];
   __shared__ int tile_lo, tile_hi;
-  const int64_t i = (int64_t)blockIdx.x * kRbfRows + threadIdx.x;
-  const bool ok = i < rows.n;
-  float xi = 0.f, yi = 0.f, zi = 0.f;
-  int ev = 0;
-  if (ok) {
-    xi = stacked_x(rows, i);
-    yi = rows.y[i];
-    zi = rows.z[i];
-    ev = rows.event[i];
+  const int64_t i0 = (int64_t)blockIdx.x * (kRbfPerThread * kRbfRows) + threadIdx.x, i1 = i0 + kRbfRows;
+  const bool ok0 = i0 < rows.n, ok1 = i1 < rows.n;
+  float x0 = 0.f, y0 = 0.f, z0 = 0.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
+  int a = 0x7fffffff, b = -0x7fffffff - 1;
+  if (ok0) {
+    x0 = stacked_x(rows, i0);
+    y0 = rows.y[i0];
+    z0 = rows.z[i0];
+    a = min(a, rows.event[i0]);
+    b = max(b, rows.event[i0]);
+  }
+  if (ok1) {
+    x1 = stacked_x(rows, i1);
+    y1 = rows.y[i1];
+    z1 = rows.z[i1];
+    a = min(a, rows.event[i1]);
+    b = max(b, rows.event[i1]);
   }
   {
-    int a = ok ? ev : 0x7fffffff, b = ok ? ev : -0x7fffffff - 1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       a = min(a, __shfl_xor_sync(0xffffffffu, a, o));
@@ -94,7 +118,7 @@ __global__ void __launch_bounds__(kRbfRows) k_rbf_rows(HitSet rows, HitSet cols,
     __syncthreads();
   }
   const int lo = tile_lo, hi = tile_hi;
-  float acc = 0.f, accz = 0.f;
+  float acc0 = 0.f, accz0 = 0.f, acc1 = 0.f, accz1 = 0.f;
   const int64_t n_chunks = (cols.n + kRbfChunk - 1) / kRbfChunk;
   for (int64_t c = 0; c < n_chunks; ++c) {
     const int2 r = col_ranges[c];
@@ -102,27 +126,44 @@ __global__ void __launch_bounds__(kRbfRows) k_rbf_rows(HitSet rows, HitSet cols,
     const int64_t j0 = c * kRbfChunk;
     const int cnt = cols.n - j0 < kRbfChunk ? (int)(cols.n - j0) : kRbfChunk;
     __syncthreads();
-    for (int k = threadIdx.x; k < cnt; k += kRbfRows) {
-      cx[k] = stacked_x(cols, j0 + k);
-      cy[k] = cols.y[j0 + k];
-      cz[k] = cols.z[j0 + k];
-      cw[k] = cols.w[j0 + k];
-    }
+    for (int k = threadIdx.x; k < cnt; k += kRbfRows)
+      col[k] = make_float4(stacked_x(cols, j0 + k), cols.y[j0 + k], cols.z[j0 + k], cols.w[j0 + k]);
     __syncthreads();
-    if (ok) {
+    if (ok0) {
       for (int k = 0; k < cnt; ++k) {
-        const float dx = __fsub_rn(xi, cx[k]), dy = __fsub_rn(yi, cy[k]), dz = __fsub_rn(zi, cz[k]);
-        const float d = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-        const float kv = expf(__fdiv_rn(-d, two_sigma2)) * cw[k];
-        acc += kv;
-        accz = fmaf(kv, dz, accz);
+        const float4 cv = col[k];
+        float dz0, dz1;
+        const float kv0 = rbf_term(x0, y0, z0, cv, two_sigma2, inv_two_sigma2, kMul, &dz0);
+        const float kv1 = rbf_term(x1, y1, z1, cv, two_sigma2, inv_two_sigma2, kMul, &dz1);
+        acc0 += kv0;
+        accz0 = fmaf(kv0, dz0, accz0);
+        acc1 += kv1;
+        accz1 = fmaf(kv1, dz1, accz1);
       }
     }
   }
-  if (ok) {
-    s[i] = acc;
-    if (zs) zs[i] = accz;
+  if (ok0) {
+    s[i0] = acc0;
+    if (zs) zs[i0] = accz0;
   }
+  if (ok1) {
+    s[i1] = acc1;
+    if (zs) zs[i1] = accz1;
+  }
+}
+
+// k_rbf_rows over all rows, with the exponent's form chosen for 2 sigma^2
+void launch_rbf_rows(const HitSet &rows, const HitSet &cols, const int2 *col_ranges, float two_sigma2, float *s,
+                     float *zs, cudaStream_t st) {
+  if (rows.n <= 0) return;
+  int e;
+  const bool pow2 = std::frexp((double)two_sigma2, &e) == 0.5;
+  const float inv = (float)(1.0 / (double)two_sigma2);
+  const unsigned g = (unsigned)((rows.n + kRbfPerThread * kRbfRows - 1) / (kRbfPerThread * kRbfRows));
+  if (pow2)
+    k_rbf_rows<true><<<g, kRbfRows, 0, st>>>(rows, cols, col_ranges, two_sigma2, inv, s, zs);
+  else
+    k_rbf_rows<false><<<g, kRbfRows, 0, st>>>(rows, cols, col_ranges, two_sigma2, inv, s, zs);
 }
 
 struct MseAdcTotals {
@@ -513,13 +554,9 @@ int run_mse_adc(const float *x, const float *y, const float *z, const int32_t *e
   const float two_s2 = (float)(2.0 * (double)sigma * (double)sigma);
   if (n > 0) k_chunk_events<<<(unsigned)((n + kRbfChunk - 1) / kRbfChunk), kRbfChunk, 0, st>>>(event, n, s.rng_pred);
   if (m > 0) k_chunk_events<<<(unsigned)((m + kRbfChunk - 1) / kRbfChunk), kRbfChunk, 0, st>>>(revent, m, s.rng_ref);
-  if (n > 0) {
-    const unsigned g = (unsigned)((n + kRbfRows - 1) / kRbfRows);
-    k_rbf_rows<<<g, kRbfRows, 0, st>>>(pred, pred, s.rng_pred, two_s2, s.a, s.az);
-    k_rbf_rows<<<g, kRbfRows, 0, st>>>(pred, ref, s.rng_ref, two_s2, s.b, s.bz);
-  }
-  if (m > 0) k_rbf_rows<<<(unsigned)((m + kRbfRows - 1) / kRbfRows), kRbfRows, 0, st>>>(ref, ref, s.rng_ref, two_s2,
-                                                                                            s.c, nullptr);
+  launch_rbf_rows(pred, pred, s.rng_pred, two_s2, s.a, s.az, st);
+  launch_rbf_rows(pred, ref, s.rng_ref, two_s2, s.b, s.bz, st);
+  launch_rbf_rows(ref, ref, s.rng_ref, two_s2, s.c, nullptr, st);
   k_mse_adc_reduce<<<1, 1024, 0, st>>>(pred, ref, s.a, s.b, s.c, lambda_q, s.tot, out);
   if (n > 0 && (grad_w || grad_z))
     k_mse_adc_grad<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pred, s.a, s.b, s.az, s.bz, s.tot, lambda_q,
