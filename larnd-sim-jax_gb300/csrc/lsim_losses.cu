@@ -276,27 +276,66 @@ __device__ __forceinline__ void tile_event_range(bool ok, int ev, int *lo_s, int
 }
 
 // nll_loss sums: s[i] = sum_j w_j K_ij, sz[i] = sum_j w_j K_ij (z_i - z_j),
-// sq[i] = sum_j w_j K_ij (q_i - q_j), K = exp(-|4-d difference|^2 / (2 sigma^2))
+// sq[i] = sum_j w_j K_ij (q_i - q_j), K = exp(-|4-d difference|^2 / (2 sigma^2)).
+// Two row hits per thread, as k_rbf_rows.
+struct Row4 {
+  float x, y, z, q;
+};
+
+__device__ __forceinline__ float gauss4_term(const Row4 &r, const float4 &c, float w, float two_sigma2, float inv,
+                                             bool mul, float *dz_out, float *dq_out) {
+  const float dx = __fsub_rn(r.x, c.x), dy = __fsub_rn(r.y, c.y), dz = __fsub_rn(r.z, c.z);
+  const float dq = __fsub_rn(r.q, c.w);
+  const float d = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)),
+                            __fmul_rn(dq, dq));
+  *dz_out = dz;
+  *dq_out = dq;
+  return expf(mul ? __fmul_rn(-d, inv) : __fdiv_rn(-d, two_sigma2)) * w;
+}
+
+template <bool kMul>
 __global__ void __launch_bounds__(kRbfRows) k_gauss4_rows(HitSet4 rows, HitSet4 cols,
                                                           const int2 *__restrict__ col_ranges, float two_sigma2,
-                                                          float *__restrict__ s, float *__restrict__ sz,
-                                                          float *__restrict__ sq) {
-  __shared__ float cx[kRbfChunk], cy[kRbfChunk], cz[kRbfChunk], cq[kRbfChunk], cw[kRbfChunk];
+                                                          float inv_two_sigma2, float *__restrict__ s,
+                                                          float *__restrict__ sz, float *__restrict__ sq) {
+  __shared__ float4 col[kRbfChunk];
+  __shared__ float cw[kRbfChunk];
   __shared__ int lo_s, hi_s;
-  const int64_t i = (int64_t)blockIdx.x * kRbfRows + threadIdx.x;
-  const bool ok = i < rows.n;
-  float xi = 0.f, yi = 0.f, zi = 0.f, qi = 0.f;
-  int ev = 0;
-  if (ok) {
-    xi = stacked_x9(rows, i);
-    yi = rows.y[i];
-    zi = rows.z[i];
-    qi = rows.q[i];
-    ev = rows.event[i];
+  const int64_t i0 = (int64_t)blockIdx.x * (kRbfPerThread * kRbfRows) + threadIdx.x, i1 = i0 + kRbfRows;
+  const bool ok0 = i0 < rows.n, ok1 = i1 < rows.n;
+  Row4 r0{0.f, 0.f, 0.f, 0.f}, r1{0.f, 0.f, 0.f, 0.f};
+  int ev0 = 0, ev1 = 0;
+  if (ok0) {
+    r0 = Row4{stacked_x9(rows, i0), rows.y[i0], rows.z[i0], rows.q[i0]};
+    ev0 = rows.event[i0];
   }
-  int lo, hi;
-  tile_event_range(ok, ev, &lo_s, &hi_s, lo, hi);
-  float acc = 0.f, accz = 0.f, accq = 0.f;
+  if (ok1) {
+    r1 = Row4{stacked_x9(rows, i1), rows.y[i1], rows.z[i1], rows.q[i1]};
+    ev1 = rows.event[i1];
+  }
+  int a = 0x7fffffff, b = -0x7fffffff - 1;   // the tile's event range
+  if (ok0) a = b = ev0;
+  if (ok1) {
+    a = min(a, ev1);
+    b = max(b, ev1);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a = min(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  if (threadIdx.x == 0) {
+    lo_s = 0x7fffffff;
+    hi_s = -0x7fffffff - 1;
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&lo_s, a);
+    atomicMax(&hi_s, b);
+  }
+  __syncthreads();
+  const int lo = lo_s, hi = hi_s;
+  float acc0 = 0.f, accz0 = 0.f, accq0 = 0.f, acc1 = 0.f, accz1 = 0.f, accq1 = 0.f;
   const int64_t n_chunks = (cols.n + kRbfChunk - 1) / kRbfChunk;
   for (int64_t c = 0; c < n_chunks; ++c) {
     const int2 r = col_ranges[c];
@@ -305,31 +344,49 @@ __global__ void __launch_bounds__(kRbfRows) k_gauss4_rows(HitSet4 rows, HitSet4 
     const int cnt = cols.n - j0 < kRbfChunk ? (int)(cols.n - j0) : kRbfChunk;
     __syncthreads();
     for (int k = threadIdx.x; k < cnt; k += kRbfRows) {
-      cx[k] = stacked_x9(cols, j0 + k);
-      cy[k] = cols.y[j0 + k];
-      cz[k] = cols.z[j0 + k];
-      cq[k] = cols.q[j0 + k];
+      col[k] = make_float4(stacked_x9(cols, j0 + k), cols.y[j0 + k], cols.z[j0 + k], cols.q[j0 + k]);
       cw[k] = cols.w[j0 + k];
     }
     __syncthreads();
-    if (ok) {
+    if (ok0) {
       for (int k = 0; k < cnt; ++k) {
-        const float dx = __fsub_rn(xi, cx[k]), dy = __fsub_rn(yi, cy[k]), dz = __fsub_rn(zi, cz[k]);
-        const float dq = __fsub_rn(qi, cq[k]);
-        const float d = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)),
-                                  __fmul_rn(dq, dq));
-        const float kv = expf(__fdiv_rn(-d, two_sigma2)) * cw[k];
-        acc += kv;
-        accz = fmaf(kv, dz, accz);
-        accq = fmaf(kv, dq, accq);
+        const float4 cv = col[k];
+        const float w = cw[k];
+        float dz0, dq0, dz1, dq1;
+        const float kv0 = gauss4_term(r0, cv, w, two_sigma2, inv_two_sigma2, kMul, &dz0, &dq0);
+        const float kv1 = gauss4_term(r1, cv, w, two_sigma2, inv_two_sigma2, kMul, &dz1, &dq1);
+        acc0 += kv0;
+        accz0 = fmaf(kv0, dz0, accz0);
+        accq0 = fmaf(kv0, dq0, accq0);
+        acc1 += kv1;
+        accz1 = fmaf(kv1, dz1, accz1);
+        accq1 = fmaf(kv1, dq1, accq1);
       }
     }
   }
-  if (ok) {
-    s[i] = acc;
-    if (sz) sz[i] = accz;
-    if (sq) sq[i] = accq;
+  if (ok0) {
+    s[i0] = acc0;
+    if (sz) sz[i0] = accz0;
+    if (sq) sq[i0] = accq0;
   }
+  if (ok1) {
+    s[i1] = acc1;
+    if (sz) sz[i1] = accz1;
+    if (sq) sq[i1] = accq1;
+  }
+}
+
+void launch_gauss4_rows(const HitSet4 &rows, const HitSet4 &cols, const int2 *col_ranges, float two_sigma2, float *s,
+                        float *sz, float *sq, cudaStream_t st) {
+  if (rows.n <= 0) return;
+  int e;
+  const bool pow2 = std::frexp((double)two_sigma2, &e) == 0.5;
+  const float inv = (float)(1.0 / (double)two_sigma2);
+  const unsigned g = (unsigned)((rows.n + kRbfPerThread * kRbfRows - 1) / (kRbfPerThread * kRbfRows));
+  if (pow2)
+    k_gauss4_rows<true><<<g, kRbfRows, 0, st>>>(rows, cols, col_ranges, two_sigma2, inv, s, sz, sq);
+  else
+    k_gauss4_rows<false><<<g, kRbfRows, 0, st>>>(rows, cols, col_ranges, two_sigma2, inv, s, sz, sq);
 }
 
 // column weights of the second nll pass: (ref_hit_prob > 0.5) / (lambda + 1e-10)
@@ -592,12 +649,10 @@ int run_nll(const float *x, const float *y, const float *z, const float *q, cons
   if (n > 0) k_chunk_events<<<(unsigned)((n + kRbfChunk - 1) / kRbfChunk), kRbfChunk, 0, st>>>(event, n, rng_pred);
   if (m > 0) k_chunk_events<<<(unsigned)((m + kRbfChunk - 1) / kRbfChunk), kRbfChunk, 0, st>>>(revent, m, rng_ref);
   if (m > 0)   // lambda_j = sum_i hp_i K_ij
-    k_gauss4_rows<<<(unsigned)((m + kRbfRows - 1) / kRbfRows), kRbfRows, 0, st>>>(
-        HitSet4{rx, ry, rz, rq, rhp, revent, m}, pred, rng_pred, two_s2, lam, nullptr, nullptr);
+    launch_gauss4_rows(HitSet4{rx, ry, rz, rq, rhp, revent, m}, pred, rng_pred, two_s2, lam, nullptr, nullptr, st);
   if (m > 0) k_nll_colw<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(rhp, lam, m, cw);
   if (n > 0)
-    k_gauss4_rows<<<(unsigned)((n + kRbfRows - 1) / kRbfRows), kRbfRows, 0, st>>>(
-        pred, HitSet4{rx, ry, rz, rq, cw, revent, m}, rng_ref, two_s2, s, sz, sq);
+    launch_gauss4_rows(pred, HitSet4{rx, ry, rz, rq, cw, revent, m}, rng_ref, two_s2, s, sz, sq, st);
   k_nll_reduce<<<1, 1024, 0, st>>>(hp, n, rhp, lam, m, out);
   if (n > 0 && (g_q || g_z || g_hp))
     k_nll_grad<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(hp, n, s, sz, sq,
