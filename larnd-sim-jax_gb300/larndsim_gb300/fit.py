@@ -78,11 +78,25 @@ class DeviceFit:
     the learning rate in normalised units, one value or a dict per
     parameter; ``normalization_scale`` is normalization_scale_sigmoid or
     normalization_scale_exp_log.
+
+    The loss is the SSE of the ADC grids against ``target`` (the whole step
+    on the device, capturable in one CUDA graph), or, with ``loss_fn`` (a
+    hit-level loss of ``larndsim_gb300.losses`` such as ``mse_adc``, the
+    reference fitter's default) and ``ref_hits`` = (ref_Q, ref_x, ref_y,
+    ref_z, ref_ticks, ref_hit_prob, ref_event), that loss of the predicted
+    hits as GenericLossStrategy forms them (strategies.py:161-180): the
+    step then runs eagerly (the number of hits is read on the host), the
+    gradient through the loss kernel, the hit z and the LUT adjoint.
     """
 
-    def __init__(self, params, response_template, tracks, fields, target: Target, fit_params=None, lr=1e-2,
+    def __init__(self, params, response_template, tracks, fields, target: Target = None, fit_params=None, lr=1e-2,
                  normalization_scheme="sigmoid", normalization_scale=1.0, max_clip_norm_val=None,
-                 clip_from_range=False, betas=(0.9, 0.999), eps=1e-8, n_events=None, max_steps=1000, ranges=None):
+                 clip_from_range=False, betas=(0.9, 0.999), eps=1e-8, n_events=None, max_steps=1000, ranges=None,
+                 loss_fn=None, ref_hits=None, loss_kwargs=None):
+        if loss_fn is None and target is None:
+            raise ValueError("DeviceFit needs a target (SSE loss) or loss_fn with ref_hits")
+        if loss_fn is not None and ref_hits is None:
+            raise ValueError("a hit-level loss_fn needs ref_hits")
         self.lib = _abi.load()
         self.lut = sim.prepare_lut(response_template, params)
         self.fields = tuple(fields)
@@ -109,10 +123,38 @@ class DeviceFit:
         self.theta_hist = torch.zeros((self.max_steps, _abi.NPARAM), dtype=torch.float32, device=dev)
         self.step_idx = torch.zeros(1, dtype=torch.int64, device=dev)
         self.graph = None
+        self.params0 = params
+        self.loss_fn, self.loss_kwargs = loss_fn, dict(loss_kwargs or {})
+        self.ref_hits = tuple(ref_hits) if ref_hits is not None else None
+        self.chain = None
+        if loss_fn is not None:
+            from . import grad
+            self.chain = grad.LUTChain(params, self.lut, self.tracks, self.fields, n_events=self.n_events)
         _abi.check(self.lib, self.lib.lsim_fit_init(sim._ptr(self.theta), self.opts, sim._ptr(self.state),
                                                     sim._stream()))
 
+    def _launch_hits(self):
+        """One step with the hit-level loss: loss and dL/dtheta by autograd
+        through the loss kernel and the LUT adjoint, then the update."""
+        from . import grad
+        theta = self.theta.detach().clone().requires_grad_(True)
+        loss, _, _ = grad.params_loss(self.params0, self.chain, self.ref_hits, self.loss_fn, theta=theta,
+                                      **self.loss_kwargs)
+        loss.backward()
+        self.out[0] = loss.detach()
+        self.out[1:] = theta.grad
+        idx = self.step_idx.clamp(max=self.max_steps - 1)
+        self.loss_hist.index_copy_(0, idx, self.out[:1])
+        self.theta_hist.index_copy_(0, idx, self.theta.unsqueeze(0))
+        self.step_idx.add_(1)
+        p = sim._ptr
+        _abi.check(self.lib, self.lib.lsim_fit_step(p(self.theta), p(self.out[1:]), self.opts, p(self.state),
+                                                    sim._stream()))
+
     def _launch(self):
+        if self.loss_fn is not None:
+            self._launch_hits()
+            return
         s = sim._stream()
         lib, p = self.lib, sim._ptr
         _abi.check(lib, lib.lsim_lut_stage1_theta(self.lp, self.fm, p(self.tracks), self.n_rows, self.n_events,
@@ -134,7 +176,10 @@ class DeviceFit:
 
     def capture(self):
         """Capture one step in a CUDA graph (a warm-up step runs first and is
-        undone, so the trajectory starts from the current parameters)."""
+        undone, so the trajectory starts from the current parameters).  The
+        SSE loss only: a hit-level loss reads the hit count on the host."""
+        if self.loss_fn is not None:
+            raise ValueError("a fit with a hit-level loss runs eagerly (run(..., graph=False))")
         saved = [t.clone() for t in (self.theta, self.state, self.loss_hist, self.theta_hist, self.step_idx)]
         side = torch.cuda.Stream()
         side.wait_stream(torch.cuda.current_stream())
@@ -151,6 +196,7 @@ class DeviceFit:
     def run(self, n_steps, graph=True):
         """n_steps optimiser steps; returns (loss history, parameter history)
         of all steps taken so far, as numpy arrays."""
+        graph = graph and self.loss_fn is None   # a hit-level loss runs eagerly
         if graph and self.graph is None:
             self.capture()
         for _ in range(n_steps):

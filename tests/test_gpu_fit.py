@@ -193,3 +193,36 @@ def test_fit_recovers_hidden_parameters(cuda, setup, scheme, lr, steps):
     for k in GRAD_PARAMS:                       # parameters not fitted stay put
         if k not in names:
             assert th[-1, GRAD_PARAMS.index(k)] == np.float32(getattr(p, k))
+
+
+def test_fit_with_the_default_hit_level_loss(cuda):
+    """The reference fitter's default loss (mse_adc on the simulated hits,
+    GenericLossStrategy): each eager step's gradient is the one
+    grad.params_loss gives at the step's parameters, and a short fit of the
+    electron lifetime lowers the loss and moves toward the hidden value."""
+    from gpu_common import small_params
+    from larndsim_gb300 import fit, grad, losses, sim, strategies, workloads
+    p = small_params(n_neighbors=1)
+    tmpl, p = sim.load_lut(workloads.synthetic_response(seed=0, nx=15, ny=15), p)
+    tracks, fields = workloads.muon_event(seed=3, n_tracks=4)
+    hidden = p.replace(lifetime=float(p.lifetime) * 0.8)
+    h = strategies.LUTSimulation(tmpl).predict(hidden, tracks, fields, 0)
+    ref = (losses.adc2charge(h["adcs"], p), h["pixel_x"], h["pixel_y"], h["pixel_z"], h["ticks"], h["hit_prob"],
+           h["event"])
+    f = fit.DeviceFit(p, tmpl, tracks, fields, fit_params=("lifetime",), lr=3e-2, loss_fn=losses.mse_adc,
+                      ref_hits=ref, normalization_scheme="divide", max_steps=64)
+    with pytest.raises(ValueError):
+        f.capture()
+    chain = grad.LUTChain(p, tmpl, tracks, fields)
+    theta0 = grad.theta_of(p, device=cuda).requires_grad_(True)
+    l0, _, _ = grad.params_loss(p, chain, ref, losses.mse_adc, theta=theta0)
+    l0.backward()
+    f.step()
+    torch.cuda.synchronize()
+    assert abs(float(f.out[0]) - float(l0.detach())) <= 1e-6 * abs(float(l0.detach()))
+    assert torch.allclose(f.out[1:], theta0.grad.to(torch.float32), rtol=1e-5, atol=0)
+    loss, th = f.run(30)
+    assert loss.shape[0] == 31 and np.isfinite(loss).all()
+    assert loss.min() < 0.25 * loss[0] and loss[-1] < loss[0]
+    k = grad.GRAD_PARAMS.index("lifetime")
+    assert abs(th[-1, k] - float(hidden.lifetime)) < abs(th[0, k] - float(hidden.lifetime))
