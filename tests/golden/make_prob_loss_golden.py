@@ -19,6 +19,12 @@ Values are taken in a 32-bit run (JAX's default types) and a 64-bit run;
 the 64-bit run also gives central differences of the loss with respect to
 the log-probability and the ADC entries the first 16 valid hits read.
 
+The CollapsedProbabilisticLossStrategy cases (with mse_adc): 48 pixels x
+10 hits x 120 ticks of peaked tick probabilities, collapsed to one
+pseudo-hit per (pixel, hit), and a sparse variant expanded to one
+pseudo-hit per entry above the hit threshold; loss values from a 32-bit
+run.
+
 The llhd_loss case: 64 rows x 120 ticks, probabilities uniform in
 [1e-6, 1], ticks with about a fifth at or beyond T - 3 (the no-hit
 branch), central differences with respect to the gathered probability and
@@ -38,7 +44,7 @@ sys.path.insert(0, str(HERE))
 
 OUT = HERE / "prob_loss_ref.npz"
 N_FD = 16
-PROB_SEED, LLHD_SEED = 7, 8
+PROB_SEED, LLHD_SEED, COLLAPSED_SEED = 7, 8, 9
 
 
 def prob_loss_inputs(seed=PROB_SEED, n_pix=160, n_pad=16, H=10, T=120):
@@ -71,6 +77,40 @@ def llhd_inputs(seed=LLHD_SEED, N=64, T=120):
     nohit = rng.uniform(1e-4, 1.0, N).astype(np.float32)
     cmc = rng.uniform(0.0, 200.0, N).astype(np.float32)
     return tpd, ticks.astype(np.int32), nohit, cd, cmc
+
+
+def collapsed_inputs(seed=COLLAPSED_SEED, n_pix=48, H=10, T=120, n_ref=150, sparse=False):
+    """Prediction and target dictionaries of the CollapsedProbabilisticLossStrategy
+    cases: per (pixel, hit) a peaked tick distribution of total probability
+    below 1 (``sparse``: only three ticks non-zero, so that the entries
+    above the hit threshold stay few), ADC distributions, pixel centres on
+    a 0.4 cm grid in two planes and two events; the target hits nearby."""
+    rng = np.random.default_rng(seed)
+    t = np.arange(T)
+    mu = rng.uniform(10, T - 10, (n_pix, H, 1))
+    w = rng.uniform(2.0, 6.0, (n_pix, H, 1))
+    prob = np.exp(-0.5 * ((t - mu) / w) ** 2)
+    prob = prob / prob.sum(axis=2, keepdims=True) * rng.uniform(0.05, 0.95, (n_pix, H, 1))
+    if sparse:
+        keep = np.zeros_like(prob, bool)
+        for k in range(3):
+            idx = np.clip(np.round(mu[..., 0]).astype(int) + k - 1, 0, T - 1)
+            np.put_along_axis(keep, idx[..., None], True, axis=2)
+        prob = np.where(keep, prob, 0.0)
+    pred = {"hit_prob": prob.astype(np.float32),
+            "adcs_distrib": rng.uniform(20.0, 200.0, (n_pix, H, T)).astype(np.float32),
+            "pixel_x": (0.4 * rng.integers(0, 60, n_pix)).astype(np.float32),
+            "pixel_y": (0.4 * rng.integers(0, 60, n_pix)).astype(np.float32),
+            "pixel_plane": rng.integers(0, 2, n_pix).astype(np.int32),
+            "event": rng.integers(0, 2, n_pix).astype(np.int32)}
+    tgt = {"adcs": rng.uniform(20.0, 200.0, n_ref).astype(np.float32),
+           "pixel_x": (0.4 * rng.integers(0, 60, n_ref)).astype(np.float32),
+           "pixel_y": (0.4 * rng.integers(0, 60, n_ref)).astype(np.float32),
+           "pixel_z": rng.uniform(-30.0, 30.0, n_ref).astype(np.float32),
+           "ticks": rng.uniform(0, T, n_ref).astype(np.float32),
+           "hit_prob": np.ones(n_ref, np.float32),
+           "event": rng.integers(0, 2, n_ref).astype(np.int32)}
+    return pred, tgt
 
 
 def main():
@@ -148,8 +188,19 @@ def main():
             g[i] = (lcall(*plus, True) - lcall(*minus, True)) / (2 * h)
         out[f"llhd/fd_{name}"] = g
     print(f"llhd_loss: 32-bit {l32:.9g}, 64-bit {l64:.12g}")
+    # CollapsedProbabilisticLossStrategy with the fitter's default mse_adc,
+    # collapsed (one pseudo-hit per pixel and hit) and per distribution entry
     jax_numpy_standin._X64[0] = False
-    out["config"] = np.array(json.dumps(dict(n_fd=N_FD, prob_seed=PROB_SEED, llhd_seed=LLHD_SEED)))
+    for name, sparse, collapsed in (("collapsed", False, True), ("entries", True, False)):
+        pred, tgt = collapsed_inputs(sparse=sparse)
+        st = St.CollapsedProbabilisticLossStrategy(Lj.mse_adc, collapsed=collapsed)
+        S.size_history_dict.clear()
+        v, _ = st.compute(base, {k: jnp.asarray(a) for k, a in pred.items()},
+                          {k: jnp.asarray(a) for k, a in tgt.items()})
+        out[f"{name}/loss32"] = np.array(float(np.asarray(v)))
+        print(f"CollapsedProbabilisticLossStrategy ({name}): {float(np.asarray(v)):.9g}")
+    out["config"] = np.array(json.dumps(dict(n_fd=N_FD, prob_seed=PROB_SEED, llhd_seed=LLHD_SEED,
+                                             collapsed_seed=COLLAPSED_SEED)))
     np.savez_compressed(OUT, **out)
     print(OUT, OUT.stat().st_size, "bytes")
 

@@ -233,3 +233,20 @@ def test_collapsed_strategy_pseudo_hits(cuda):
     loss, _ = st.compute(pp, pred, target)
     loss.backward()
     assert torch.isfinite(theta.grad).all()
+
+
+@pytest.mark.parametrize("name,sparse,collapsed", [("collapsed", False, True), ("entries", True, False)])
+def test_collapsed_strategy_matches_reference(cuda, params, name, sparse, collapsed):
+    """CollapsedProbabilisticLossStrategy with mse_adc (expected values per
+    (pixel, hit), or one pseudo-hit per entry above the hit threshold)
+    against the reference's own strategy run on the numpy stand-in, 1e-5
+    relative (float32 sums in a different order)."""
+    from make_prob_loss_golden import collapsed_inputs
+    gold = np.load(GOLDEN / "prob_loss_ref.npz")
+    pred, tgt = collapsed_inputs(sparse=sparse)
+    pred_t = {k: torch.from_numpy(v).to(cuda) for k, v in pred.items()}
+    tgt_t = {k: torch.from_numpy(v).to(cuda) for k, v in tgt.items()}
+    st = strategies.CollapsedProbabilisticLossStrategy(losses.mse_adc, collapsed=collapsed)
+    loss, _ = st.compute(params, pred_t, tgt_t)
+    ref = float(gold[f"{name}/loss32"])
+    assert abs(float(loss.detach()) - ref) <= 1e-5 * abs(ref), (float(loss.detach()), ref)

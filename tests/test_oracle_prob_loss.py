@@ -97,3 +97,39 @@ def test_prob_llhd_hand_case(cst):
     g_lp, g_ad = PL.prob_llhd_grad(sim, lp, ad, tp, tt, ta, cst)
     assert g_lp[1, 0, 5] != 0 and g_lp[2, 0, 0] != 0 and g_lp[2, 1, 1] != 0 and g_lp[2, 1, 3] == 0
     assert loss > 0
+
+
+def _collapsed_oracle(params, pred, tgt, collapsed, threshold=1e-8):
+    """CollapsedProbabilisticLossStrategy.compute (strategies.py:262-335)
+    with mse_adc, composed from the oracle's pieces."""
+    from oracle import losses_np as L
+    from oracle import reference_np as R
+    tp, ad = pred["hit_prob"], pred["adcs_distrib"]
+    P, H, T = tp.shape
+    if collapsed:
+        et, ea, hp = R.get_average_hit_values(tp, ad)
+        Q = R.adc2charge(ea, params)
+        z = R.get_hit_z(params, et, np.repeat(pred["pixel_plane"][:, None], H, axis=1))
+        rep = lambda v: np.repeat(np.asarray(v)[:, None], H, axis=1)   # noqa: E731
+    else:
+        mask = tp > np.float32(threshold)
+        hp = tp[mask]
+        Q = R.adc2charge(ad[mask], params)
+        ticks = np.broadcast_to(np.arange(T, dtype=np.float32), tp.shape)[mask]
+        z = R.get_hit_z(params, ticks, np.broadcast_to(pred["pixel_plane"][:, None, None], tp.shape)[mask])
+        rep = lambda v: np.broadcast_to(np.asarray(v)[:, None, None], tp.shape)[mask]   # noqa: E731
+    x = rep(pred["pixel_x"]).astype(np.float32)
+    y = rep(pred["pixel_y"]).astype(np.float32)
+    ev = rep(pred["event"])
+    ref_Q = R.adc2charge(tgt["adcs"], params)
+    return L.mse_adc(np.ravel(Q), np.ravel(x), np.ravel(y), np.ravel(z), np.ravel(hp), np.ravel(ev), ref_Q,
+                     tgt["pixel_x"], tgt["pixel_y"], tgt["pixel_z"], tgt["hit_prob"], tgt["event"])[0]
+
+
+@pytest.mark.parametrize("name,sparse,collapsed", [("collapsed", False, True), ("entries", True, False)])
+def test_collapsed_strategy_oracle_matches_reference(gold, name, sparse, collapsed):
+    from make_prob_loss_golden import collapsed_inputs
+    pred, tgt = collapsed_inputs(sparse=sparse)
+    v = _collapsed_oracle(consts.Params(), pred, tgt, collapsed)
+    ref = float(gold[f"{name}/loss32"])
+    assert abs(v - ref) <= 1e-5 * abs(ref), (v, ref)
